@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""bench.py — batched ratio_match over a 240-view zone on one GB300.
+
+Workload (the headline configuration): 3 cameras x 80 positions = 240 views,
+n_v ~ U[300, 2000] SIFT-like descriptors per view, candidate_pairs(views, 5, 4,
+16) = 3663 image pairs, overlapping pairs sharing 30-60 % of descriptors
+(noisy copies, sigma 0.05). Seeded synthetic data (no dataset exists for it).
+
+A step is one pass of the hot path over the zone: ratio_match(fa, fb, 0.8,
+true) for every pair (crates/core/src/pipeline.rs:485-493, matching half) as
+one planned batch replayed from a CUDA graph.
+
+  value  image pairs/s with the descriptor store resident in HBM; device time
+         of each step by CUDA events on the library stream; L2 flushed between
+         steps outside the events.
+  e2e    the same through the C ABI with host buffers: every step re-uploads
+         all views from pinned host memory (slm_store_add_views), runs the
+         batch and reads the match lists back (slm_plan_results).
+The match lists of the main arm are checked against the oracle (bit-exact) on
+a sample of pairs before timing. `--impl reference` times the CPU restatement
+of the reference (oracle/, all host threads) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "skylens-stream-rs_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+METRIC = "image pairs/s, batched ratio_match: BF16 shortlist vs FP32 GPU, bit-exact"
+WORKLOAD = "zone240"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="slm", choices=["slm", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16", "fp8"])
+    ap.add_argument("--positions", type=int, default=80)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--verify-pairs", type=int, default=400, help="pairs checked against the oracle (0: none, -1: all)")
+    ap.add_argument("--fp32-steps", type=int, default=3, help="timed steps of the plain FP32 arm")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--x2", action="store_true", help="FP32 kernel with packed f32x2 arithmetic")
+    ap.add_argument("--json-out", default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        loaded = [s for s in sm if mx and s >= 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0}, \
+        "fallback"
+
+
+def cpu_baseline(z, budget_s: float, threads: int):
+    """The oracle's blocked ratio_match (64-row blocks over `threads` host threads,
+    pairs serial as in benches/pipeline.rs:247-253) on pairs in a fixed order until
+    the time budget is used."""
+    import oracle as O
+    order = np.random.Generator(np.random.PCG64(123)).permutation(len(z.pairs))
+    done, dist = 0, 0
+    t0 = time.perf_counter()
+    while done < len(order) and time.perf_counter() - t0 < budget_s:
+        k = int(order[done])
+        u, v = int(z.pairs[k, 0]), int(z.pairs[k, 1])
+        O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=threads)
+        dist += int(z.counts[u]) * int(z.counts[v])
+        done += 1
+    dt = time.perf_counter() - t0
+    return done / dt, dist / dt, done, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from skylens_match import synth
+    z = synth.zone(positions=args.positions, seed=args.seed)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(z, min(per_step, 1.0), threads)
+    rates, drates, npairs = [], [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, dr, n, _dt = cpu_baseline(z, per_step, threads)
+        rates.append(r)
+        drates.append(dr)
+        npairs.append(n)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(rates))
+    line = {"metric": METRIC, "value": value, "unit": "image pairs/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "views": len(z.counts), "pairs": int(len(z.pairs)),
+                       "distances": z.distances, "sample": "pairs in a fixed random order, each step "
+                       f"~{per_step:.1f}s of CPU time ({int(np.mean(npairs))} pairs/step)"},
+            "distances_per_s": float(np.mean(drates)),
+            "cpu_baseline": {"value": value, "unit": "image pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"{int(np.mean(npairs))} of {len(z.pairs)} zone pairs per step"},
+            "e2e": {"value": value, "unit": "image pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    import oracle as O
+    import skylens_match as sm
+    from skylens_match import synth
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist = None
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    built = getattr(sm, "BUILT_PRECISIONS", ("fp32",))
+    prec = args.precision if args.precision != "auto" else ("bf16" if "bf16" in built else "fp32")
+
+    # ---- workload (each rank its own zone: replicas, weak scaling)
+    z = synth.zone(positions=args.positions, seed=args.seed + rank)
+    n_rows = int(z.counts.sum())
+    pinned = torch.from_numpy(z.desc).pin_memory()
+    m = sm.Matcher(device=dev)
+    ext = torch.cuda.ExternalStream(m.stream)
+    store = m.store(n_rows, len(z.counts))
+    store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
+    tune_graph = 1 | (16 if args.x2 else 0)
+    plan = store.plan(z.pairs, 0.8, True, prec, use_graph=tune_graph)
+    plan_fp32 = plan if prec == "fp32" else store.plan(z.pairs, 0.8, True, "fp32", use_graph=tune_graph)
+
+    # ---- correctness against the oracle on a sample of pairs
+    plan.launch()
+    got, off = plan.results()
+    nverify = len(z.pairs) if args.verify_pairs < 0 else min(args.verify_pairs, len(z.pairs))
+    sel = np.random.Generator(np.random.PCG64(7)).permutation(len(z.pairs))[:nverify]
+    mism = 0
+    for k in sel:
+        u, v = int(z.pairs[k, 0]), int(z.pairs[k, 1])
+        ref = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=os.cpu_count() or 1)
+        mism += not np.array_equal(got[int(off[k]):int(off[k + 1])], ref)
+    bit_exact = mism == 0
+    stats_main = dict(plan.stats)
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(p, steps, warm):
+        for _ in range(warm):
+            with torch.cuda.stream(ext):
+                flush.zero_()
+            p.launch()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        evs = []
+        kern = []
+        for _ in range(steps):
+            with torch.cuda.stream(ext):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+            p.launch()
+            with torch.cuda.stream(ext):
+                e1.record()
+            e1.synchronize()
+            p.results()  # reads main-kernel time; not part of the device-timed region
+            kern.append(p.stats["kernel_ms"])
+            evs.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return evs, kern
+
+    clocks = Clocks(dev)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    step_ms, kern_ms = timed(plan, args.steps, args.warmup)
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    ms = float(np.mean(step_ms))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * len(z.pairs) / (ms / 1e3)
+
+    fp32 = None
+    if plan_fp32 is not plan:
+        f_ms, f_kern = timed(plan_fp32, max(1, args.fp32_steps), 1)
+        fms = float(np.mean(f_ms))
+        fp32 = {"value": len(z.pairs) / (fms / 1e3), "unit": "image pairs/s", "ms_per_step": fms,
+                "kernel_ms": float(np.mean(f_kern))}
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    out_bytes = 0
+    if not args.no_e2e:
+        for _ in range(2):
+            store.clear()
+            store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
+            plan.launch()
+            plan.results()
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            store.clear()
+            store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
+            plan.launch()
+            pr, of = plan.results()
+            t.append(time.perf_counter() - t0)
+            out_bytes = pr.nbytes + of.nbytes
+        e2e_s = float(np.mean(t))
+        e2e = {"value": ws * len(z.pairs) / e2e_s, "unit": "image pairs/s", "ms_per_step": 1e3 * e2e_s,
+               "h2d_bytes_per_step": int(z.desc.nbytes), "d2h_bytes_per_step": int(out_bytes)}
+
+    # ---- roofline of the dominant kernel
+    pk, pk_kind = peaks()
+    kms = float(np.mean(kern_ms))
+    dist_n = z.distances
+    if prec in ("bf16", "fp8"):
+        flops = 2.0 * 128 * dist_n  # one 128-long dot product per distance
+        achieved = flops / (kms / 1e3) / 1e12
+        peak = pk["bf16_tflops"] * (2 if prec == "fp8" else 1)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "kernel": f"shortlist_{prec}", "peak_source": pk_kind}
+    else:
+        # 384 FP32 instructions per distance (sub, mul, add per component, matching.rs:146-155)
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = clk.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+        peak = sm_count * 128 * mhz * 1e6 / 1e12  # FP32 lane-instructions/s (T/s)
+        achieved = 384.0 * dist_n / (kms / 1e3) / 1e12
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "T FP32 instr/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "exact_kernel",
+                "peak_source": f"{sm_count} SMs x 128 lanes x {mhz:.0f} MHz (sampled)"}
+    prof = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            roof["traffic"] = json.load(open(prof)).get(roof["kernel"])
+        except Exception:
+            pass
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r, dr, n, dt = cpu_baseline(z, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": r, "unit": "image pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{n} of {len(z.pairs)} zone pairs in a fixed random order ({dt:.1f} s)",
+               "distances_per_s": dr}
+
+    line = {"metric": METRIC, "value": value, "unit": "image pairs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[prec],
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": prec, "views": len(z.counts), "pairs": int(len(z.pairs)),
+                       "distances": dist_n, "descriptors": n_rows, "ratio": 0.8, "mutual": True,
+                       "l2": "flushed between steps (512 MiB write, outside the events)",
+                       "parallelism": f"replicas{ws}"},
+            "distances_per_s": ws * dist_n / (ms / 1e3),
+            "bit_exact": {"ok": bit_exact, "pairs_checked": int(nverify), "mismatched_pairs": int(mism)},
+            "fp32_plain": fp32,
+            "kernel_ms": kms, "stats": stats_main,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(stats_main.get("kernel_launches", 0)) * args.steps,
+            "clocks": clk, "wall_s_timed": t_wall}
+    if rank == 0:
+        s = json.dumps(line)
+        print(s, flush=True)
+        if args.json_out:
+            open(args.json_out, "w").write(s + "\n")
+    plan.close()
+    if plan_fp32 is not plan:
+        plan_fp32.close()
+    store.close()
+    m.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

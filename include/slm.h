@@ -1,0 +1,193 @@
+/*
+ * slm.h — C ABI of libslm, the GB300 (sm_103a) descriptor matcher.
+ *
+ * libslm replaces the descriptor-matching hot path of skylens-stream-rs:
+ *   ratio_match      crates/core/src/matching.rs:167  (all-pairs squared L2,
+ *                    best/second-best per row, Lowe ratio, mutual check)
+ *   candidate_pairs  crates/core/src/matching.rs:18   (image-pair generator)
+ *   scheduled_pairs  crates/core/src/matching.rs:103  (run's pair generator)
+ *   match_pairs      crates/core/src/pipeline.rs:485  (per-pair loop that
+ *                    calls ratio_match(fa, fb, 0.8, true) over the pairs)
+ *
+ * Conventions
+ *   - Descriptors are row-major float32 arrays of n x 128 (Feature::desc,
+ *     features.rs:499-502, marshalled contiguously by the caller).
+ *   - A match is slm_pair {i, j}: row i of `a` matched to row j of `b`. Lists
+ *     are in ascending i with each i at most once, exactly as ratio_match
+ *     returns them; the results are bit-identical to the reference.
+ *   - Every entry point returns an slm_status; no exception or abort crosses
+ *     the ABI. On SLM_CAPACITY the required count is still written to the
+ *     count output so the caller can grow its buffer and call again.
+ *   - There is no CPU fallback: without a usable CUDA device calls return
+ *     SLM_NO_DEVICE.
+ *   - A context may be used from several host threads at once (the reference
+ *     calls ratio_match from rayon workers, pipeline.rs:487-492, and from a
+ *     second OS thread, pipeline.rs:2894-2918). Stores and plans are owned by
+ *     one thread at a time.
+ */
+#ifndef SLM_H
+#define SLM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLM_DESC_LEN 128 /* features.rs:496 DESC_LEN */
+
+typedef enum {
+    SLM_OK = 0,
+    SLM_INVALID_ARG = 1, /* NULL pointer, ratio not finite, bad view id, ... */
+    SLM_CAPACITY = 2,    /* output buffer too small; required count reported */
+    SLM_OOM = 3,         /* device allocation failed or HBM budget exceeded */
+    SLM_CUDA_ERROR = 4,  /* a CUDA runtime call failed (see slm_last_error) */
+    SLM_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    SLM_NO_DEVICE = 6,   /* no CUDA device / device is not sm_103 */
+    SLM_INTERNAL = 7     /* invariant violated inside the library */
+} slm_status;
+
+typedef enum {
+    SLM_PREC_FP32 = 0, /* plain exact FP32 kernel */
+    SLM_PREC_BF16 = 1, /* tcgen05 BF16 shortlist + exact FP32 rescore */
+    SLM_PREC_FP8 = 2   /* tcgen05 FP8 E4M3 shortlist + exact FP32 rescore */
+} slm_precision;
+
+typedef struct {
+    uint32_t i, j;
+} slm_pair;
+
+/* Counters of one call. All fields are filled by every matching entry point. */
+typedef struct {
+    uint64_t pairs;             /* image pairs matched */
+    uint64_t distances;         /* sum over pairs of na*nb */
+    uint64_t matches;           /* pairs written */
+    uint64_t rows_recomputed;   /* shortlist rows rescanned exactly */
+    uint64_t cols_recomputed;   /* mutual checks settled by an exact column scan */
+    uint64_t rows_rescored;     /* rows whose shortlist was rescored exactly */
+    float kernel_ms;            /* device time of the main matching kernel, last launch */
+    float max_abs_err;          /* max |approx - exact| seen on rescored pairs */
+    uint64_t kernel_launches;   /* kernels one launch of the batch runs */
+} slm_stats;
+
+typedef struct slm_ctx slm_ctx;
+typedef struct slm_store slm_store;
+typedef struct slm_plan slm_plan;
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    void *stream;        /* cudaStream_t for all work; NULL: the context creates one */
+    uint64_t hbm_budget; /* bytes the context may allocate; 0 = free HBM at creation */
+} slm_opts;
+
+/* ------------------------------------------------------------ context */
+
+const char *slm_status_str(slm_status s);
+/* Detail of the last failing call on this host thread ("" if none). */
+const char *slm_last_error(void);
+slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out);
+slm_status slm_ctx_destroy(slm_ctx *ctx);
+/* The cudaStream_t the context launches on. */
+void *slm_ctx_stream(slm_ctx *ctx);
+/* Bytes currently allocated by the context and its stores/plans. */
+uint64_t slm_ctx_bytes_in_use(slm_ctx *ctx);
+
+/* ------------------------------------------------------ single pair */
+
+/* Drop-in for ratio_match(a, b, ratio, mutual) (matching.rs:167-215).
+ * a: na x 128 float32, b: nb x 128 float32 in host memory. Writes the match
+ * list to out (capacity cap pairs; na pairs always suffice) and its length to
+ * *n_out. Empty a or b, or nb < 2, gives an empty list (matching.rs:160-166).
+ * Blocks until the result is in host memory. st may be NULL. */
+slm_status slm_ratio_match(slm_ctx *ctx, const float *a, uint32_t na, const float *b, uint32_t nb, float ratio,
+                           int mutual, slm_precision prec, slm_pair *out, uint32_t cap, uint32_t *n_out,
+                           slm_stats *st);
+
+/* The same on device memory: d_a, d_b, d_out (cap pairs) and d_count (one
+ * uint32) are device pointers; work is enqueued on the context stream and the
+ * call returns without synchronising. */
+slm_status slm_ratio_match_device(slm_ctx *ctx, const float *d_a, uint32_t na, const float *d_b, uint32_t nb,
+                                  float ratio, int mutual, slm_precision prec, slm_pair *d_out, uint32_t cap,
+                                  uint32_t *d_count);
+
+/* ---------------------------------------------------- pair generators */
+
+/* candidate_pairs (matching.rs:18-40). views: 2*nv uint64 (camera, position).
+ * Writes up to cap pairs (view indices i < j, sorted) and the total to *n_out;
+ * SLM_CAPACITY when the total exceeds cap. Host-only, no device needed. */
+slm_status slm_candidate_pairs(const uint64_t *views, uint32_t nv, uint64_t temporal, uint64_t cross,
+                               uint64_t pow2_max, slm_pair *out, uint64_t cap, uint64_t *n_out);
+
+/* CrossSchedule (matching.rs:48-71) and PairSchedule (:74-101). */
+typedef struct {
+    uint64_t temporal; /* PAIR_TEMPORAL = 5 */
+    uint64_t pow2_max; /* PAIR_POW2_MAX = 16 */
+    int spec;          /* 1: CrossSchedule::Spec{range}; 0: Formation */
+    uint64_t range;    /* Spec: cross-camera position gap 0..=range */
+    uint64_t right_min, left_min, max, step; /* Formation (FORMATION = 20, 20, 40, 4) */
+} slm_pair_schedule;
+
+/* PairSchedule::default() (matching.rs:82-90) / PairSchedule::spec() (:94-100). */
+slm_pair_schedule slm_pair_schedule_default(void);
+slm_pair_schedule slm_pair_schedule_spec(void);
+
+/* scheduled_pairs (matching.rs:103-142). Same output contract as
+ * slm_candidate_pairs. */
+slm_status slm_scheduled_pairs(const uint64_t *views, uint32_t nv, const slm_pair_schedule *sch, slm_pair *out,
+                               uint64_t cap, uint64_t *n_out);
+
+/* ------------------------------------------- device descriptor store */
+
+/* A device-resident set of views (images). Capacity is fixed at creation. */
+slm_status slm_store_create(slm_ctx *ctx, uint64_t max_descs, uint32_t max_views, slm_store **out);
+slm_status slm_store_destroy(slm_store *st);
+/* Append one view: copies n x 128 host floats to the device and lays them out
+ * for the kernels (asynchronous on the context stream; desc must stay valid
+ * until the next synchronising call). Returns its id in *view_id. */
+slm_status slm_store_add_view(slm_store *st, const float *desc, uint32_t n, uint32_t *view_id);
+/* Append many views from one host buffer: view v has counts[v] rows starting
+ * at row offsets[v] of desc. ids[v] receives its id. */
+slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets, const uint32_t *counts,
+                               uint32_t nviews, uint32_t *ids);
+/* Forget every view (capacity is kept). */
+slm_status slm_store_clear(slm_store *st);
+uint32_t slm_store_num_views(slm_store *st);
+
+/* ------------------------------------------------- batched matching */
+
+/* Tuning knobs; zero fields take the autotuned or default values. */
+typedef struct {
+    uint32_t items_per_sm;  /* FP32: target work items per SM when splitting columns */
+    uint32_t shortlist_k;   /* shortlist slots per row (BF16/FP8) */
+    uint32_t use_graph;     /* 1: replay a captured CUDA graph (default), 2: plain launches */
+} slm_tune;
+
+/* Plan the matching of np image pairs (view-id pairs in `pairs`, the
+ * match_pairs loop of pipeline.rs:485-493) on a store. The plan owns its
+ * device scratch and a CUDA graph of the whole batch. */
+slm_status slm_plan_create(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                           int mutual, slm_precision prec, const slm_tune *tune, slm_plan **out);
+slm_status slm_plan_destroy(slm_plan *p);
+/* Enqueue one run of the plan on the context stream (no host sync). */
+slm_status slm_plan_launch(slm_plan *p);
+/* Wait for the last launch, then copy results to the host. Pair k's matches
+ * are out[offsets[k] .. offsets[k+1]) (offsets has np+1 entries). On
+ * SLM_CAPACITY offsets[np] holds the required capacity. st may be NULL. */
+slm_status slm_plan_results(slm_plan *p, slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *st);
+/* Device-side results of the last launch: per-pair match counts (np uint32)
+ * and the padded match slots (pair k at row offset slot_offsets[k]). */
+slm_status slm_plan_device_results(slm_plan *p, const uint32_t **d_counts, const slm_pair **d_slots,
+                                   const uint64_t **h_slot_offsets);
+/* Bytes of device scratch the plan holds. */
+uint64_t slm_plan_bytes(slm_plan *p);
+
+/* One-shot: plan, launch, read back, destroy. */
+slm_status slm_match_batch(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                           int mutual, slm_precision prec, slm_pair *out, uint64_t cap, uint64_t *offsets,
+                           slm_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLM_H */

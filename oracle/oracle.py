@@ -1,0 +1,244 @@
+"""ctypes front end of the C oracle (oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and
+by the ``cpu_baseline`` / ``--impl reference`` legs of bench.py, always as the
+checker or the timed CPU baseline, never as the product path.
+
+Each wrapper names the reference function it restates (paths inside
+skylens-stream-rs).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "oracle.c")
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.c with gcc (-O3, no FMA contraction) into _build/liboracle.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-o", tmp, SRC, "-lm", "-lpthread"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB)
+            P = ctypes.POINTER
+            u64p = P(ctypes.c_uint64)
+            f32p = P(ctypes.c_float)
+            u32p = P(ctypes.c_uint32)
+            i64 = ctypes.c_int64
+            L.orc_lcg_next.argtypes = [u64p]
+            L.orc_lcg_next.restype = ctypes.c_double
+            L.orc_lcg_gauss.argtypes = [u64p]
+            L.orc_lcg_gauss.restype = ctypes.c_double
+            L.orc_feature.argtypes = [u64p, f32p]
+            L.orc_perturb.argtypes = [u64p, f32p, ctypes.c_float]
+            L.orc_match_fixture_copies.argtypes = [i64]
+            L.orc_match_fixture_copies.restype = i64
+            L.orc_match_fixture.argtypes = [ctypes.c_uint64, i64, i64, f32p, f32p]
+            L.orc_sq_dist.argtypes = [f32p, f32p]
+            L.orc_sq_dist.restype = ctypes.c_float
+            L.orc_sq_dist_seq.argtypes = [f32p, f32p]
+            L.orc_sq_dist_seq.restype = ctypes.c_float
+            L.orc_sq_dist_f64.argtypes = [f32p, f32p]
+            L.orc_sq_dist_f64.restype = ctypes.c_double
+            L.orc_dist_matrix.argtypes = [f32p, i64, f32p, i64, f32p]
+            L.orc_dist_matrix_f64.argtypes = [f32p, i64, f32p, i64, P(ctypes.c_double)]
+            L.orc_ratio_match.argtypes = [f32p, i64, f32p, i64, ctypes.c_float, ctypes.c_int, ctypes.c_int, u32p]
+            L.orc_ratio_match.restype = i64
+            L.orc_ratio_match_naive.argtypes = [f32p, i64, f32p, i64, ctypes.c_float, ctypes.c_int, u32p]
+            L.orc_ratio_match_naive.restype = i64
+            L.orc_ratio_states.argtypes = [f32p, i64, f32p, i64, u32p, f32p, f32p, u32p, f32p]
+            L.orc_pairs_hash.argtypes = [u32p, i64]
+            L.orc_pairs_hash.restype = ctypes.c_uint64
+            L.orc_candidate_pairs.argtypes = [u64p, i64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, u32p, i64]
+            L.orc_candidate_pairs.restype = i64
+            L.orc_scheduled_pairs.argtypes = [u64p, i64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                              ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                              ctypes.c_uint64, u32p, i64]
+            L.orc_scheduled_pairs.restype = i64
+            L.orc_match_pairs.argtypes = [f32p, P(ctypes.c_int64), P(ctypes.c_int64), u32p, i64, ctypes.c_float,
+                                          ctypes.c_int, ctypes.c_int, P(ctypes.c_int64)]
+            L.orc_match_pairs.restype = i64
+            _lib = L
+    return _lib
+
+
+def _f32(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return x
+
+
+def _p(x: np.ndarray, t):
+    return x.ctypes.data_as(ctypes.POINTER(t))
+
+
+class Lcg:
+    """matching.rs:1140-1153 (test Lcg): 64-bit LCG with Box-Muller gauss."""
+
+    def __init__(self, seed: int):
+        self.s = ctypes.c_uint64(seed)
+
+    def next(self) -> float:
+        return lib().orc_lcg_next(ctypes.byref(self.s))
+
+    def gauss(self) -> float:
+        return lib().orc_lcg_gauss(ctypes.byref(self.s))
+
+    def feature(self) -> np.ndarray:
+        """matching.rs:1580-1596 (`feature`): unit-length uniform descriptor."""
+        out = np.empty(128, np.float32)
+        lib().orc_feature(ctypes.byref(self.s), _p(out, ctypes.c_float))
+        return out
+
+    def features(self, n: int) -> np.ndarray:
+        return np.stack([self.feature() for _ in range(n)]) if n else np.zeros((0, 128), np.float32)
+
+    def perturb(self, h: np.ndarray, scale: float) -> np.ndarray:
+        """h[k] += scale * (f32)gauss() for k in 0..128 (matching.rs:1649-1651)."""
+        h = np.array(h, dtype=np.float32, copy=True)
+        lib().orc_perturb(ctypes.byref(self.s), _p(h, ctypes.c_float), ctypes.c_float(scale))
+        return h
+
+
+def match_fixture(seed: int, na: int, extra: int):
+    """matching.rs:1638-1656 (`match_fixture`)."""
+    L = lib()
+    nb = L.orc_match_fixture_copies(na) + extra
+    a = np.empty((na, 128), np.float32)
+    b = np.empty((nb, 128), np.float32)
+    L.orc_match_fixture(seed, na, extra, _p(a, ctypes.c_float), _p(b, ctypes.c_float))
+    return a, b
+
+
+def sq_dist(p, r) -> float:
+    """matching.rs:144-155 spec order (8 lanes, then lanes 0..7)."""
+    p, r = _f32(p), _f32(r)
+    return float(np.float32(lib().orc_sq_dist(_p(p, ctypes.c_float), _p(r, ctypes.c_float))))
+
+
+def sq_dist_seq(p, r) -> float:
+    """matching.rs:2373-2377: sequential fold."""
+    p, r = _f32(p), _f32(r)
+    return float(np.float32(lib().orc_sq_dist_seq(_p(p, ctypes.c_float), _p(r, ctypes.c_float))))
+
+
+def dist_matrix(a, b) -> np.ndarray:
+    a, b = _f32(a).reshape(-1, 128), _f32(b).reshape(-1, 128)
+    out = np.empty((len(a), len(b)), np.float32)
+    lib().orc_dist_matrix(_p(a, ctypes.c_float), len(a), _p(b, ctypes.c_float), len(b), _p(out, ctypes.c_float))
+    return out
+
+
+def dist_matrix_f64(a, b) -> np.ndarray:
+    a, b = _f32(a).reshape(-1, 128), _f32(b).reshape(-1, 128)
+    out = np.empty((len(a), len(b)), np.float64)
+    lib().orc_dist_matrix_f64(_p(a, ctypes.c_float), len(a), _p(b, ctypes.c_float), len(b),
+                              _p(out, ctypes.c_double))
+    return out
+
+
+def ratio_match(a, b, ratio: float, mutual: bool, threads: int = 1) -> list[tuple[int, int]]:
+    """matching.rs:167-215 (`ratio_match`): blocked spec-order version."""
+    return [tuple(p) for p in ratio_match_np(a, b, ratio, mutual, threads).tolist()]
+
+
+def ratio_match_np(a, b, ratio: float, mutual: bool, threads: int = 1) -> np.ndarray:
+    a, b = _f32(a).reshape(-1, 128), _f32(b).reshape(-1, 128)
+    out = np.empty((max(len(a), 1), 2), np.uint32)
+    n = lib().orc_ratio_match(_p(a, ctypes.c_float), len(a), _p(b, ctypes.c_float), len(b),
+                              ctypes.c_float(ratio), int(bool(mutual)), int(threads), _p(out, ctypes.c_uint32))
+    return out[:n].copy()
+
+
+def ratio_match_naive(a, b, ratio: float, mutual: bool) -> list[tuple[int, int]]:
+    """matching.rs:1597-1636 (`ratio_match_reference`): sequential sums."""
+    a, b = _f32(a).reshape(-1, 128), _f32(b).reshape(-1, 128)
+    out = np.empty((max(len(a), 1), 2), np.uint32)
+    n = lib().orc_ratio_match_naive(_p(a, ctypes.c_float), len(a), _p(b, ctypes.c_float), len(b),
+                                    ctypes.c_float(ratio), int(bool(mutual)), _p(out, ctypes.c_uint32))
+    return [tuple(p) for p in out[:n].tolist()]
+
+
+def ratio_states(a, b):
+    """Exact per-row (j1, d1, d2) and per-column (i1, d1) states."""
+    a, b = _f32(a).reshape(-1, 128), _f32(b).reshape(-1, 128)
+    na, nb = len(a), len(b)
+    rj = np.empty(na, np.uint32)
+    rd1 = np.empty(na, np.float32)
+    rd2 = np.empty(na, np.float32)
+    ci = np.empty(nb, np.uint32)
+    cd = np.empty(nb, np.float32)
+    lib().orc_ratio_states(_p(a, ctypes.c_float), na, _p(b, ctypes.c_float), nb, _p(rj, ctypes.c_uint32),
+                           _p(rd1, ctypes.c_float), _p(rd2, ctypes.c_float), _p(ci, ctypes.c_uint32),
+                           _p(cd, ctypes.c_float))
+    return rj, rd1, rd2, ci, cd
+
+
+def pairs_hash(m) -> int:
+    """matching.rs:1866-1878 (`pairs_hash`): FNV-1a 64."""
+    arr = np.ascontiguousarray(np.asarray(m, dtype=np.uint32).reshape(-1, 2))
+    return int(lib().orc_pairs_hash(_p(arr, ctypes.c_uint32), len(arr)))
+
+
+def _views(views) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(views, dtype=np.uint64).reshape(-1, 2))
+
+
+def candidate_pairs(views, temporal: int, cross: int, pow2_max: int) -> list[tuple[int, int]]:
+    """matching.rs:14-40."""
+    v = _views(views)
+    n = lib().orc_candidate_pairs(_p(v, ctypes.c_uint64), len(v), temporal, cross, min(pow2_max, 2**64 - 1),
+                                  None, 0)
+    out = np.empty((max(n, 1), 2), np.uint32)
+    lib().orc_candidate_pairs(_p(v, ctypes.c_uint64), len(v), temporal, cross, min(pow2_max, 2**64 - 1),
+                              _p(out, ctypes.c_uint32), n)
+    return [tuple(p) for p in out[:n].tolist()]
+
+
+def scheduled_pairs(views, temporal=5, pow2_max=16, spec_range=None, formation=(20, 20, 40, 4)):
+    """matching.rs:103-142. spec_range given -> CrossSchedule::Spec, else Formation."""
+    v = _views(views)
+    spec = spec_range is not None
+    rm, lm, mx, st = formation
+    args = (_p(v, ctypes.c_uint64), len(v), temporal, pow2_max, int(spec), spec_range or 0, rm, lm, mx, st)
+    n = lib().orc_scheduled_pairs(*args, None, 0)
+    out = np.empty((max(n, 1), 2), np.uint32)
+    lib().orc_scheduled_pairs(*args, _p(out, ctypes.c_uint32), n)
+    return [tuple(p) for p in out[:n].tolist()]
+
+
+def match_pairs(desc, view_off, view_n, pairs, ratio: float, mutual: bool, threads: int):
+    """Serial loop over pairs, each ratio_match'ed with `threads` (benches/pipeline.rs:247-253).
+    Returns (total matches, per-pair counts)."""
+    desc = _f32(desc)
+    vo = np.ascontiguousarray(view_off, dtype=np.int64)
+    vn = np.ascontiguousarray(view_n, dtype=np.int64)
+    pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.uint32).reshape(-1, 2))
+    counts = np.empty(len(pr), np.int64)
+    tot = lib().orc_match_pairs(_p(desc, ctypes.c_float), _p(vo, ctypes.c_int64), _p(vn, ctypes.c_int64),
+                                _p(pr, ctypes.c_uint32), len(pr), ctypes.c_float(ratio), int(bool(mutual)),
+                                int(threads), _p(counts, ctypes.c_int64))
+    return tot, counts

@@ -1,0 +1,95 @@
+// k_compact.cu — turns per-pair match slots into one dense list.
+//
+// Each pair owns a slot range sized for its row count (a row matches at most
+// once, matching.rs:204-214). After matching, the per-pair counts are scanned
+// into offsets and the slots gathered into a dense array in pair order, so a
+// batch comes back to the host as two copies (offsets, pairs).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "slm.h"
+
+namespace slm {
+
+// Single CTA: offsets[k] = sum of counts[0..k), offsets[np] = total.
+__global__ void __launch_bounds__(1024) scan_counts_kernel(const uint32_t *__restrict__ counts, uint32_t np,
+                                                           uint64_t *__restrict__ offsets) {
+    __shared__ uint64_t warp_sum[32];
+    __shared__ uint64_t carry_sh;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_sh = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < np; base += 1024) {
+        const uint32_t k = base + tid;
+        uint64_t v = k < np ? counts[k] : 0;
+        uint64_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint64_t w = warp_sum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sum[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint64_t carry = carry_sh;
+        const uint64_t excl = carry + (wid ? warp_sum[wid - 1] : 0) + x - v;
+        if (k < np) offsets[k] = excl;
+        __syncthreads();
+        if (tid == 1023) carry_sh = excl + v;
+        __syncthreads();
+    }
+    if (tid == 0) offsets[np] = carry_sh;
+}
+
+// One CTA per pair: dense[offsets[k] + t] = slots[slot_off[k] + t].
+__global__ void __launch_bounds__(256) gather_kernel(const uint2 *__restrict__ slots,
+                                                     const uint64_t *__restrict__ slot_off,
+                                                     const uint32_t *__restrict__ counts,
+                                                     const uint64_t *__restrict__ offsets, uint2 *__restrict__ dense,
+                                                     uint64_t cap) {
+    const uint32_t k = blockIdx.x;
+    const uint32_t n = counts[k];
+    const uint64_t src = slot_off[k], dst = offsets[k];
+    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x)
+        if (dst + t < cap) dense[dst + t] = slots[src + t];
+}
+
+// Single pair into a caller buffer: copies min(total, cap) pairs and writes
+// the full count.
+__global__ void copy_pairs_kernel(const uint2 *__restrict__ src, const uint64_t *__restrict__ total,
+                                  slm_pair *__restrict__ dst, uint32_t cap, uint32_t *__restrict__ d_count) {
+    const uint64_t n = *total;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n && t < cap;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 v = src[t];
+        dst[t].i = v.x;
+        dst[t].j = v.y;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = (uint32_t)n;
+}
+
+void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s) {
+    scan_counts_kernel<<<1, 1024, 0, s>>>(counts, np, offsets);
+}
+
+void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
+                   uint32_t np, uint2 *dense, uint64_t cap, cudaStream_t s) {
+    if (np) gather_kernel<<<np, 256, 0, s>>>(slots, slot_off, counts, offsets, dense, cap);
+}
+
+void launch_copy_pairs(const uint2 *src, const uint64_t *total, slm_pair *dst, uint32_t cap, uint32_t *d_count,
+                       cudaStream_t s) {
+    copy_pairs_kernel<<<64, 256, 0, s>>>(src, total, dst, cap, d_count);
+}
+
+}  // namespace slm

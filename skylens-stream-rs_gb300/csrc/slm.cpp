@@ -1,0 +1,873 @@
+// slm.cpp — host side of libslm: the C ABI declared in include/slm.h.
+//
+// Contexts own a stream and an HBM budget; stores hold device-resident
+// descriptors laid out for the kernels; plans turn a list of image pairs into
+// work items, scratch buffers and a captured CUDA graph. The single-pair entry
+// points (the ratio_match drop-in) run through a pool of workspaces so that
+// concurrent host threads (rayon workers in the reference) never share one.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "slm.h"
+#include "slm_internal.h"
+
+using namespace slm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+slm_status fail(slm_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define SLM_CU(call)                                                                                   \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            if (e_ == cudaErrorMemoryAllocation) return fail(SLM_OOM, std::string(#call) + ": out of memory"); \
+            return fail(SLM_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_));           \
+        }                                                                                              \
+    } while (0)
+
+#define SLM_TRY(expr)                \
+    do {                             \
+        slm_status s_ = (expr);      \
+        if (s_ != SLM_OK) return s_; \
+    } while (0)
+
+uint64_t pad_rows(uint64_t n) { return (n + kTile - 1) / kTile * kTile; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+
+struct Workspace;
+
+struct slm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 0;
+    uint64_t budget = 0;
+    std::atomic<uint64_t> used{0};
+    std::mutex mu;
+    std::vector<Workspace *> idle;  // single-pair workspaces not in use
+    std::vector<Workspace *> all;
+
+    slm_status alloc(void **p, size_t bytes) {
+        *p = nullptr;
+        if (bytes == 0) return SLM_OK;
+        uint64_t now = used.fetch_add(bytes) + bytes;
+        if (budget && now > budget) {
+            used.fetch_sub(bytes);
+            return fail(SLM_OOM, "HBM budget exceeded: need " + std::to_string(now) + " > budget " +
+                                     std::to_string(budget) + " bytes");
+        }
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            used.fetch_sub(bytes);
+            cudaGetLastError();
+            return fail(SLM_OOM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        }
+        return SLM_OK;
+    }
+    void release(void *p, size_t bytes) {
+        if (!p) return;
+        cudaFree(p);
+        used.fetch_sub(bytes);
+    }
+};
+
+// Device buffer owned by a context, grown on demand.
+struct DevBuf {
+    slm_ctx *ctx = nullptr;
+    void *p = nullptr;
+    size_t bytes = 0;
+    slm_status ensure(slm_ctx *c, size_t need) {
+        ctx = c;
+        if (need <= bytes) return SLM_OK;
+        ctx->release(p, bytes);
+        p = nullptr;
+        bytes = 0;
+        size_t want = need + need / 4;
+        SLM_TRY(ctx->alloc(&p, want));
+        bytes = want;
+        return SLM_OK;
+    }
+    void reset() {
+        if (ctx) ctx->release(p, bytes);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
+    ~DevBuf() { reset(); }
+};
+
+extern "C" const char *slm_status_str(slm_status s) {
+    switch (s) {
+        case SLM_OK: return "SLM_OK";
+        case SLM_INVALID_ARG: return "SLM_INVALID_ARG";
+        case SLM_CAPACITY: return "SLM_CAPACITY";
+        case SLM_OOM: return "SLM_OOM";
+        case SLM_CUDA_ERROR: return "SLM_CUDA_ERROR";
+        case SLM_TIMEOUT: return "SLM_TIMEOUT";
+        case SLM_NO_DEVICE: return "SLM_NO_DEVICE";
+        case SLM_INTERNAL: return "SLM_INTERNAL";
+    }
+    return "SLM_UNKNOWN";
+}
+
+extern "C" const char *slm_last_error(void) { return g_last_error.c_str(); }
+
+// --------------------------------------------------------------------- store
+
+struct slm_store {
+    slm_ctx *ctx = nullptr;
+    uint64_t max_rows = 0;  // padded rows
+    uint32_t max_views = 0;
+    DevBuf raw;             // row-major FP32, padded rows per view
+    DevBuf tiled;           // FP32 tiles [slot][row]
+    std::vector<uint32_t> row0, n;
+    uint64_t rows_used = 0;
+    uint64_t version = 0;   // bumps when views are added or cleared
+};
+
+// ---------------------------------------------------------------------- plan
+
+struct slm_plan {
+    slm_ctx *ctx = nullptr;
+    slm_store *st = nullptr;
+    uint32_t np = 0;
+    float ratio = 0.8f;
+    int mutual = 1;
+    slm_precision prec = SLM_PREC_FP32;
+    slm_tune tune{};
+    cudaStream_t stream = nullptr;   // all uploads and launches of this plan
+    std::vector<PairMeta> meta;
+    std::vector<Item> items;
+    std::vector<uint64_t> slot_off;  // np + 1
+    uint64_t n_parts = 0, n_cols = 0, n_slots = 0, distances = 0;
+    DevBuf d_meta, d_items, d_parts, d_colbest, d_slots, d_counts, d_ctl, d_offsets, d_dense;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel
+    uint64_t kernels = 0;                      // kernels per launch
+    bool launched = false;
+    ~slm_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+};
+
+// Dense compaction of per-pair slots (device) into out + offsets.
+namespace slm {
+void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s);
+void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
+                   uint32_t np, uint2 *dense, uint64_t cap, cudaStream_t s);
+}  // namespace slm
+
+namespace {
+
+// Plan the exact-path work items: one per (pair, 128-row tile, column chunk).
+// Columns are split only when the batch has too few row tiles to fill the GPU.
+void plan_items(slm_plan *p) {
+    const slm_store *st = p->st;
+    uint64_t row_tiles = 0;
+    for (uint32_t k = 0; k < p->np; ++k) row_tiles += (p->meta[k].na + kTile - 1) / kTile;
+    const uint64_t want = (uint64_t)std::max(1, p->ctx->sms) * (p->tune.items_per_sm ? p->tune.items_per_sm : 4);
+    uint32_t split = 1;
+    if (row_tiles && row_tiles < want) split = (uint32_t)((want + row_tiles - 1) / row_tiles);
+    p->items.clear();
+    uint32_t part = 0;
+    for (uint32_t k = 0; k < p->np; ++k) {
+        PairMeta &m = p->meta[k];
+        const uint32_t rt_n = (m.na + kTile - 1) / kTile;
+        const uint32_t ct_n = (m.nb + kTile - 1) / kTile;
+        uint32_t chunks = std::max(1u, std::min(split, ct_n));
+        m.nchunk = chunks;
+        m.part_base = part;
+        for (uint32_t rt = 0; rt < rt_n; ++rt)
+            for (uint32_t c = 0; c < chunks; ++c) {
+                Item it{};
+                it.pair = k;
+                it.rt = rt;
+                it.ct0 = (uint32_t)((uint64_t)ct_n * c / chunks);
+                it.ct1 = (uint32_t)((uint64_t)ct_n * (c + 1) / chunks);
+                it.part = part + rt * chunks + c;
+                p->items.push_back(it);
+            }
+        part += rt_n * chunks;
+        (void)st;
+    }
+    p->n_parts = part;
+    // Longest items first (cost ~ rows x columns) for the dynamic queue.
+    std::stable_sort(p->items.begin(), p->items.end(), [&](const Item &x, const Item &y) {
+        const uint64_t cx = (uint64_t)(x.ct1 - x.ct0), cy = (uint64_t)(y.ct1 - y.ct0);
+        return cx > cy;
+    });
+}
+
+slm_status plan_build(slm_plan *p, const slm_pair *pairs) {
+    slm_store *st = p->st;
+    p->meta.resize(p->np);
+    p->slot_off.assign(p->np + 1, 0);
+    uint64_t col = 0, slot = 0, dist = 0;
+    for (uint32_t k = 0; k < p->np; ++k) {
+        const uint32_t u = pairs[k].i, v = pairs[k].j;
+        if (u >= st->row0.size() || v >= st->row0.size())
+            return fail(SLM_INVALID_ARG, "pair " + std::to_string(k) + " names a view not in the store");
+        PairMeta &m = p->meta[k];
+        m.a_row0 = st->row0[u];
+        m.b_row0 = st->row0[v];
+        m.na = st->n[u];
+        m.nb = st->n[v];
+        m.col_base = col;
+        m.slot_off = slot;
+        p->slot_off[k] = slot;
+        col += m.nb;
+        slot += m.na;
+        dist += (uint64_t)m.na * m.nb;
+    }
+    p->slot_off[p->np] = slot;
+    p->n_cols = col;
+    p->n_slots = slot;
+    p->distances = dist;
+    plan_items(p);
+    slm_ctx *c = p->ctx;
+    SLM_TRY(p->d_meta.ensure(c, sizeof(PairMeta) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_colbest.ensure(c, sizeof(unsigned long long) * std::max<uint64_t>(1, col)));
+    SLM_TRY(p->d_slots.ensure(c, sizeof(uint2) * std::max<uint64_t>(1, slot)));
+    SLM_TRY(p->d_counts.ensure(c, sizeof(uint32_t) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_ctl.ensure(c, 64));
+    SLM_TRY(p->d_offsets.ensure(c, sizeof(uint64_t) * (p->np + 1) * 2));
+    SLM_TRY(p->d_dense.ensure(c, sizeof(uint2) * std::max<uint64_t>(1, slot)));
+    cudaStream_t s = p->stream;
+    SLM_CU(cudaMemcpyAsync(p->d_meta.p, p->meta.data(), sizeof(PairMeta) * p->np, cudaMemcpyHostToDevice, s));
+    // slot offsets live in the second half of d_offsets
+    SLM_CU(cudaMemcpyAsync(p->d_offsets.as<uint64_t>() + (p->np + 1), p->slot_off.data(),
+                           sizeof(uint64_t) * (p->np + 1), cudaMemcpyHostToDevice, s));
+    SLM_TRY(p->d_items.ensure(c, sizeof(Item) * std::max<size_t>(1, p->items.size())));
+    SLM_TRY(p->d_parts.ensure(c, sizeof(RowPart) * kTile * std::max<uint64_t>(1, p->n_parts)));
+    SLM_CU(cudaMemcpyAsync(p->d_items.p, p->items.data(), sizeof(Item) * p->items.size(), cudaMemcpyHostToDevice, s));
+    return SLM_OK;
+}
+
+// Enqueue the whole batch on stream s (also used for graph capture).
+slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
+    uint32_t *ctl = p->d_ctl.as<uint32_t>();  // [0] work counter, [1] error word, [2..] shortlist counters
+    SLM_CU(cudaMemsetAsync(ctl, 0, 64, s));
+    if (p->mutual) launch_fill_u64(p->d_colbest.as<unsigned long long>(), p->n_cols, ~0ull, s);
+    const float ratio2 = p->ratio * p->ratio;
+    {
+        ExactArgs a{};
+        a.tiled = p->st->tiled.as<float>();
+        a.items = p->d_items.as<Item>();
+        a.n_items = (uint32_t)p->items.size();
+        a.pairs = p->d_meta.as<PairMeta>();
+        a.parts = p->d_parts.as<RowPart>();
+        a.colbest = p->d_colbest.as<unsigned long long>();
+        a.work = ctl;
+        a.err = ctl + 1;
+        a.mutual = p->mutual;
+        a.x2 = (p->tune.use_graph & 16) ? 1 : 0;
+        SLM_CU(cudaEventRecord(p->ev0, s));
+        if (a.n_items) launch_exact(a, std::min<int>(p->ctx->sms, (int)a.n_items), s);
+        SLM_CU(cudaEventRecord(p->ev1, s));
+        p->kernels = (p->mutual ? 1 : 0) + (a.n_items ? 1 : 0) + (p->np ? 1 : 0) + 1 + (p->np ? 1 : 0);
+        FinalizeArgs f{};
+        f.pairs = p->d_meta.as<PairMeta>();
+        f.npairs = p->np;
+        f.parts = p->d_parts.as<RowPart>();
+        f.colbest = p->d_colbest.as<unsigned long long>();
+        f.ratio2 = ratio2;
+        f.mutual = p->mutual;
+        f.slots = p->d_slots.as<uint2>();
+        f.counts = p->d_counts.as<uint32_t>();
+        launch_finalize(f, s);
+    }
+    uint64_t *offsets = p->d_offsets.as<uint64_t>();
+    launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
+    launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
+                  p->d_dense.as<uint2>(), p->n_slots, s);
+    SLM_CU(cudaGetLastError());
+    return SLM_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- workspaces
+
+// Everything one single-pair call needs: its own stream, a two-view store
+// and a plan, reused across calls of similar size.
+struct Workspace {
+    cudaStream_t stream = nullptr;
+    slm_store store;
+    slm_plan plan;
+};
+
+namespace {
+
+slm_status ctx_check_device(slm_ctx *c) {
+    SLM_CU(cudaSetDevice(c->device));
+    return SLM_OK;
+}
+
+slm_status ws_acquire(slm_ctx *c, Workspace **out) {
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        if (!c->idle.empty()) {
+            *out = c->idle.back();
+            c->idle.pop_back();
+            return SLM_OK;
+        }
+    }
+    Workspace *w = new (std::nothrow) Workspace();
+    if (!w) return fail(SLM_OOM, "host allocation failed");
+    cudaError_t e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete w;
+        return fail(SLM_CUDA_ERROR, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    w->store.ctx = c;
+    w->plan.ctx = c;
+    w->plan.st = &w->store;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        c->all.push_back(w);
+    }
+    *out = w;
+    return SLM_OK;
+}
+
+void ws_release(slm_ctx *c, Workspace *w) {
+    std::lock_guard<std::mutex> g(c->mu);
+    c->idle.push_back(w);
+}
+
+// Reserve room for rows in a store (grows the device buffers if needed).
+slm_status store_reserve(slm_store *st, uint64_t rows) {
+    slm_ctx *c = st->ctx;
+    SLM_TRY(st->raw.ensure(c, rows * kDesc * sizeof(float)));
+    SLM_TRY(st->tiled.ensure(c, rows * kDesc * sizeof(float)));
+    st->max_rows = std::max<uint64_t>(st->max_rows, st->raw.bytes / (kDesc * sizeof(float)));
+    return SLM_OK;
+}
+
+slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool device_src, cudaStream_t s,
+                        uint32_t *id) {
+    const uint64_t padded = pad_rows(n);
+    if (st->row0.size() >= st->max_views && st->max_views)
+        return fail(SLM_CAPACITY, "store view capacity " + std::to_string(st->max_views) + " reached");
+    if (st->rows_used + padded > st->max_rows)
+        return fail(SLM_CAPACITY, "store descriptor capacity exceeded: " + std::to_string(st->rows_used + padded) +
+                                      " > " + std::to_string(st->max_rows) + " padded rows");
+    if (st->rows_used + padded >= (1ull << 32)) return fail(SLM_CAPACITY, "store exceeds 2^32 rows");
+    float *raw = st->raw.as<float>() + st->rows_used * kDesc;
+    if (n) {
+        SLM_CU(cudaMemcpyAsync(raw, desc, (size_t)n * kDesc * sizeof(float),
+                               device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        launch_pack_fp32(raw, n, st->tiled.as<float>(), (uint32_t)(st->rows_used / kTile), s);
+        SLM_CU(cudaGetLastError());
+    }
+    if (id) *id = (uint32_t)st->row0.size();
+    st->row0.push_back((uint32_t)st->rows_used);
+    st->n.push_back(n);
+    st->rows_used += padded;
+    st->version++;
+    return SLM_OK;
+}
+
+slm_status check_status_word(slm_plan *p) {
+    uint32_t err = 0;
+    SLM_CU(cudaMemcpy(&err, p->d_ctl.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (err) return fail(SLM_TIMEOUT, "device wait gave up (code " + std::to_string(err) + ")");
+    return SLM_OK;
+}
+
+slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
+    if (!st) return SLM_OK;
+    std::memset(st, 0, sizeof(*st));
+    st->pairs = p->np;
+    st->distances = p->distances;
+    st->matches = matches;
+    st->kernel_launches = p->kernels;
+    if (p->launched && p->ev0 && p->ev1) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p->ev0, p->ev1) == cudaSuccess) st->kernel_ms = ms;
+        cudaGetLastError();
+    }
+    return SLM_OK;
+}
+
+slm_status validate_ratio(float ratio) {
+    if (!std::isfinite(ratio)) return fail(SLM_INVALID_ARG, "ratio must be finite");
+    return SLM_OK;
+}
+
+}  // namespace
+
+extern "C" slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out) {
+    if (!out) return fail(SLM_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SLM_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    const int dev = opts ? opts->device : 0;
+    if (dev < 0 || dev >= ndev) return fail(SLM_INVALID_ARG, "device ordinal out of range");
+    cudaDeviceProp prop{};
+    SLM_CU(cudaGetDeviceProperties(&prop, dev));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(SLM_NO_DEVICE, "libslm is built for sm_103a; device " + std::to_string(dev) + " is sm_" +
+                                       std::to_string(prop.major) + std::to_string(prop.minor));
+    SLM_CU(cudaSetDevice(dev));
+    {
+        cudaError_t ke = init_exact_kernels();
+        if (ke != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SLM_NO_DEVICE, std::string("kernels do not load on this device: ") + cudaGetErrorString(ke));
+        }
+    }
+    auto *c = new (std::nothrow) slm_ctx();
+    if (!c) return fail(SLM_OOM, "host allocation failed");
+    c->device = dev;
+    c->sms = prop.multiProcessorCount;
+    if (opts && opts->stream) {
+        c->stream = static_cast<cudaStream_t>(opts->stream);
+    } else {
+        cudaError_t se = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (se != cudaSuccess) {
+            delete c;
+            return fail(SLM_CUDA_ERROR, std::string("cudaStreamCreate: ") + cudaGetErrorString(se));
+        }
+        c->own_stream = true;
+    }
+    size_t fre = 0, tot = 0;
+    cudaMemGetInfo(&fre, &tot);
+    c->budget = (opts && opts->hbm_budget) ? opts->hbm_budget : (uint64_t)fre;
+    *out = c;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_ctx_destroy(slm_ctx *c) {
+    if (!c) return SLM_OK;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (Workspace *w : c->all) {
+        if (w->stream) cudaStreamDestroy(w->stream);
+        delete w;
+    }
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return SLM_OK;
+}
+
+extern "C" void *slm_ctx_stream(slm_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
+
+extern "C" uint64_t slm_ctx_bytes_in_use(slm_ctx *c) { return c ? c->used.load() : 0; }
+
+// ------------------------------------------------------------------ stores
+
+extern "C" slm_status slm_store_create(slm_ctx *c, uint64_t max_descs, uint32_t max_views, slm_store **out) {
+    if (!c || !out) return fail(SLM_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    SLM_TRY(ctx_check_device(c));
+    auto *st = new (std::nothrow) slm_store();
+    if (!st) return fail(SLM_OOM, "host allocation failed");
+    st->ctx = c;
+    st->max_views = max_views;
+    // every view may waste up to 127 padding rows
+    const uint64_t rows = pad_rows(max_descs) + (uint64_t)max_views * kTile;
+    slm_status s = store_reserve(st, rows);
+    if (s != SLM_OK) {
+        delete st;
+        return s;
+    }
+    st->max_rows = rows;
+    *out = st;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_store_destroy(slm_store *st) {
+    if (!st) return SLM_OK;
+    cudaSetDevice(st->ctx->device);
+    cudaStreamSynchronize(st->ctx->stream);
+    delete st;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_store_add_view(slm_store *st, const float *desc, uint32_t n, uint32_t *view_id) {
+    if (!st || (!desc && n)) return fail(SLM_INVALID_ARG, "NULL argument");
+    SLM_TRY(ctx_check_device(st->ctx));
+    return store_append(st, desc, n, false, st->ctx->stream, view_id);
+}
+
+extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets,
+                                          const uint32_t *counts, uint32_t nviews, uint32_t *ids) {
+    if (!st || (!desc && nviews) || (nviews && (!offsets || !counts))) return fail(SLM_INVALID_ARG, "NULL argument");
+    SLM_TRY(ctx_check_device(st->ctx));
+    for (uint32_t v = 0; v < nviews; ++v) {
+        uint32_t id = 0;
+        SLM_TRY(store_append(st, desc + offsets[v] * kDesc, counts[v], false, st->ctx->stream, &id));
+        if (ids) ids[v] = id;
+    }
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_store_clear(slm_store *st) {
+    if (!st) return fail(SLM_INVALID_ARG, "NULL store");
+    st->row0.clear();
+    st->n.clear();
+    st->rows_used = 0;
+    st->version++;
+    return SLM_OK;
+}
+
+extern "C" uint32_t slm_store_num_views(slm_store *st) { return st ? (uint32_t)st->row0.size() : 0; }
+
+// ------------------------------------------------------------------- plans
+
+namespace {
+
+slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                     int mutual, slm_precision prec, const slm_tune *tune, cudaStream_t stream) {
+    p->ctx = c;
+    p->stream = stream;
+    p->st = st;
+    p->np = np;
+    p->ratio = ratio;
+    p->mutual = mutual ? 1 : 0;
+    p->prec = prec;
+    p->tune = tune ? *tune : slm_tune{};
+    if (!p->tune.use_graph) p->tune.use_graph = 1;
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    if (p->graph) {
+        cudaGraphDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    p->launched = false;
+    return plan_build(p, pairs);
+}
+
+slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
+    if (!p->ev0) SLM_CU(cudaEventCreate(&p->ev0));
+    if (!p->ev1) SLM_CU(cudaEventCreate(&p->ev1));
+    if (use_graph) {
+        if (!p->exec) {
+            SLM_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            slm_status es = plan_enqueue(p, s);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (es != SLM_OK) {
+                if (g) cudaGraphDestroy(g);
+                return es;
+            }
+            if (ce != cudaSuccess) return fail(SLM_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(ce));
+            p->graph = g;
+            SLM_CU(cudaGraphInstantiate(&p->exec, g, 0));
+        }
+        SLM_CU(cudaGraphLaunch(p->exec, s));
+    } else {
+        SLM_TRY(plan_enqueue(p, s));
+    }
+    p->launched = true;
+    return SLM_OK;
+}
+
+}  // namespace
+
+extern "C" slm_status slm_plan_create(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                                      int mutual, slm_precision prec, const slm_tune *tune, slm_plan **out) {
+    if (!c || !st || !out || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (prec != SLM_PREC_FP32 && prec != SLM_PREC_BF16 && prec != SLM_PREC_FP8)
+        return fail(SLM_INVALID_ARG, "unknown precision");
+    SLM_TRY(validate_ratio(ratio));
+    *out = nullptr;
+    SLM_TRY(ctx_check_device(c));
+    auto *p = new (std::nothrow) slm_plan();
+    if (!p) return fail(SLM_OOM, "host allocation failed");
+    slm_status s = plan_init(p, c, st, pairs, np, ratio, mutual, prec, tune, c->stream);
+    if (s != SLM_OK) {
+        std::string keep = g_last_error;
+        delete p;
+        g_last_error = keep;
+        return s;
+    }
+    *out = p;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_plan_destroy(slm_plan *p) {
+    if (!p) return SLM_OK;
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->stream);
+    delete p;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_plan_launch(slm_plan *p) {
+    if (!p) return fail(SLM_INVALID_ARG, "NULL plan");
+    SLM_TRY(ctx_check_device(p->ctx));
+    return plan_launch_on(p, p->stream, (p->tune.use_graph & 15) != 2);
+}
+
+extern "C" slm_status slm_plan_results(slm_plan *p, slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *st) {
+    if (!p || !offsets || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (!p->launched) return fail(SLM_INVALID_ARG, "plan was not launched");
+    SLM_TRY(ctx_check_device(p->ctx));
+    SLM_CU(cudaStreamSynchronize(p->stream));
+    SLM_TRY(check_status_word(p));
+    SLM_CU(cudaMemcpy(offsets, p->d_offsets.p, sizeof(uint64_t) * (p->np + 1), cudaMemcpyDeviceToHost));
+    const uint64_t total = offsets[p->np];
+    SLM_TRY(fill_stats(p, st, total));
+    if (total > cap) return fail(SLM_CAPACITY, "need " + std::to_string(total) + " pairs, have " + std::to_string(cap));
+    if (total) SLM_CU(cudaMemcpy(out, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost));
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_plan_device_results(slm_plan *p, const uint32_t **d_counts, const slm_pair **d_slots,
+                                              const uint64_t **h_slot_offsets) {
+    if (!p) return fail(SLM_INVALID_ARG, "NULL plan");
+    if (d_counts) *d_counts = p->d_counts.as<uint32_t>();
+    if (d_slots) *d_slots = p->d_slots.as<slm_pair>();
+    if (h_slot_offsets) *h_slot_offsets = p->slot_off.data();
+    return SLM_OK;
+}
+
+extern "C" uint64_t slm_plan_bytes(slm_plan *p) {
+    if (!p) return 0;
+    return p->d_meta.bytes + p->d_items.bytes + p->d_parts.bytes + p->d_colbest.bytes + p->d_slots.bytes +
+           p->d_counts.bytes + p->d_ctl.bytes + p->d_offsets.bytes + p->d_dense.bytes;
+}
+
+extern "C" slm_status slm_match_batch(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                                      int mutual, slm_precision prec, slm_pair *out, uint64_t cap, uint64_t *offsets,
+                                      slm_stats *stats) {
+    slm_plan *p = nullptr;
+    SLM_TRY(slm_plan_create(c, st, pairs, np, ratio, mutual, prec, nullptr, &p));
+    slm_status s = slm_plan_launch(p);
+    if (s == SLM_OK) s = slm_plan_results(p, out, cap, offsets, stats);
+    std::string keep = g_last_error;
+    slm_plan_destroy(p);
+    g_last_error = keep;
+    return s;
+}
+
+// -------------------------------------------------------------- single pair
+
+namespace {
+
+// Run one pair through a workspace: load a and b into its two-view store,
+// plan and enqueue on its stream. The caller synchronises.
+slm_status single_pair_enqueue(slm_ctx *c, Workspace *w, const float *a, uint32_t na, const float *b, uint32_t nb,
+                               float ratio, int mutual, slm_precision prec, bool device_src) {
+    slm_store *st = &w->store;
+    const uint64_t rows = pad_rows(na) + pad_rows(nb);
+    SLM_TRY(store_reserve(st, std::max<uint64_t>(rows, kTile)));
+    slm_store_clear(st);
+    SLM_TRY(store_append(st, a, na, device_src, w->stream, nullptr));
+    SLM_TRY(store_append(st, b, nb, device_src, w->stream, nullptr));
+    const slm_pair pr{0, 1};
+    slm_tune t{};
+    t.use_graph = 2;  // one-off shapes: plain launches, no graph
+    SLM_TRY(plan_init(&w->plan, c, st, &pr, 1, ratio, mutual, prec, &t, w->stream));
+    return plan_launch_on(&w->plan, w->stream, false);
+}
+
+struct WsGuard {
+    slm_ctx *c;
+    Workspace *w;
+    ~WsGuard() {
+        if (w) ws_release(c, w);
+    }
+};
+
+slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb, float ratio,
+                           slm_precision prec) {
+    if (!c) return fail(SLM_INVALID_ARG, "NULL context");
+    if ((na && !a) || (nb && !b)) return fail(SLM_INVALID_ARG, "NULL descriptor array");
+    if (prec != SLM_PREC_FP32 && prec != SLM_PREC_BF16 && prec != SLM_PREC_FP8)
+        return fail(SLM_INVALID_ARG, "unknown precision");
+    return validate_ratio(ratio);
+}
+
+}  // namespace
+
+extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb,
+                                      float ratio, int mutual, slm_precision prec, slm_pair *out, uint32_t cap,
+                                      uint32_t *n_out, slm_stats *st) {
+    SLM_TRY(check_pair_args(c, a, na, b, nb, ratio, prec));
+    if (!n_out || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL output");
+    *n_out = 0;
+    if (st) std::memset(st, 0, sizeof(*st));
+    // matching.rs:160-166: no second neighbour (or nothing to match) -> no pairs.
+    if (na == 0 || nb < 2) {
+        if (st) st->pairs = 1, st->distances = (uint64_t)na * nb;
+        return SLM_OK;
+    }
+    SLM_TRY(ctx_check_device(c));
+    Workspace *w = nullptr;
+    SLM_TRY(ws_acquire(c, &w));
+    WsGuard guard{c, w};
+    SLM_TRY(single_pair_enqueue(c, w, a, na, b, nb, ratio, mutual, prec, false));
+    slm_plan *p = &w->plan;
+    SLM_CU(cudaStreamSynchronize(w->stream));
+    SLM_TRY(check_status_word(p));
+    uint64_t off[2] = {0, 0};
+    SLM_CU(cudaMemcpy(off, p->d_offsets.p, sizeof(off), cudaMemcpyDeviceToHost));
+    const uint64_t total = off[1];
+    *n_out = (uint32_t)total;
+    SLM_TRY(fill_stats(p, st, total));
+    if (total > cap) return fail(SLM_CAPACITY, "need " + std::to_string(total) + " pairs, have " + std::to_string(cap));
+    if (total) SLM_CU(cudaMemcpy(out, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost));
+    return SLM_OK;
+}
+
+namespace slm {
+void launch_copy_pairs(const uint2 *src, const uint64_t *total, slm_pair *dst, uint32_t cap, uint32_t *d_count,
+                       cudaStream_t s);
+}
+
+extern "C" slm_status slm_ratio_match_device(slm_ctx *c, const float *d_a, uint32_t na, const float *d_b, uint32_t nb,
+                                             float ratio, int mutual, slm_precision prec, slm_pair *d_out,
+                                             uint32_t cap, uint32_t *d_count) {
+    SLM_TRY(check_pair_args(c, d_a, na, d_b, nb, ratio, prec));
+    if (!d_count || (cap && !d_out)) return fail(SLM_INVALID_ARG, "NULL output");
+    SLM_TRY(ctx_check_device(c));
+    if (na == 0 || nb < 2) {
+        SLM_CU(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), c->stream));
+        return SLM_OK;
+    }
+    Workspace *w = nullptr;
+    SLM_TRY(ws_acquire(c, &w));
+    WsGuard guard{c, w};
+    // Order the workspace stream after prior work on the context stream and
+    // the context stream after this call, so the call behaves as if it ran on
+    // the context stream.
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SLM_CU(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+    SLM_CU(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+    SLM_CU(cudaEventRecord(e0, c->stream));
+    SLM_CU(cudaStreamWaitEvent(w->stream, e0, 0));
+    slm_status s = single_pair_enqueue(c, w, d_a, na, d_b, nb, ratio, mutual, prec, true);
+    if (s == SLM_OK) {
+        slm_plan *p = &w->plan;
+        launch_copy_pairs(p->d_dense.as<uint2>(), p->d_offsets.as<uint64_t>() + 1, d_out, cap, d_count, w->stream);
+        cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) s = fail(SLM_CUDA_ERROR, std::string("copy kernel: ") + cudaGetErrorString(le));
+    }
+    cudaEventRecord(e1, w->stream);
+    cudaStreamWaitEvent(c->stream, e1, 0);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return s;
+}
+
+// ---------------------------------------------------------- pair generators
+
+namespace {
+
+uint64_t absdiff(uint64_t x, uint64_t y) { return x > y ? x - y : y - x; }
+bool is_pow2(uint64_t d) { return d && !(d & (d - 1)); }
+
+slm_status emit_pairs(const std::vector<slm_pair> &v, slm_pair *out, uint64_t cap, uint64_t *n_out) {
+    *n_out = v.size();
+    const uint64_t n = std::min<uint64_t>(cap, v.size());
+    if (n) std::memcpy(out, v.data(), n * sizeof(slm_pair));
+    if (v.size() > cap) return fail(SLM_CAPACITY, "need " + std::to_string(v.size()) + " pairs");
+    return SLM_OK;
+}
+
+}  // namespace
+
+// matching.rs:18-40: same camera with position gap 1..=temporal or a power of
+// two <= pow2_max; different cameras with gap <= cross. i < j, sorted, unique.
+extern "C" slm_status slm_candidate_pairs(const uint64_t *views, uint32_t nv, uint64_t temporal, uint64_t cross,
+                                          uint64_t pow2_max, slm_pair *out, uint64_t cap, uint64_t *n_out) {
+    if ((!views && nv) || !n_out || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL argument");
+    std::vector<slm_pair> v;
+    for (uint32_t i = 0; i < nv; ++i)
+        for (uint32_t j = i + 1; j < nv; ++j) {
+            const uint64_t ca = views[2 * i], pa = views[2 * i + 1], cb = views[2 * j], pb = views[2 * j + 1];
+            const uint64_t d = absdiff(pa, pb);
+            const bool ok = ca == cb ? (d >= 1 && (d <= temporal || (is_pow2(d) && d <= pow2_max))) : d <= cross;
+            if (ok) v.push_back(slm_pair{i, j});
+        }
+    return emit_pairs(v, out, cap, n_out);
+}
+
+extern "C" slm_pair_schedule slm_pair_schedule_default(void) {
+    slm_pair_schedule s{};
+    s.temporal = 5;
+    s.pow2_max = 16;
+    s.spec = 0;
+    s.range = 4;
+    s.right_min = 20;
+    s.left_min = 20;
+    s.max = 40;
+    s.step = 4;
+    return s;
+}
+
+extern "C" slm_pair_schedule slm_pair_schedule_spec(void) {
+    slm_pair_schedule s = slm_pair_schedule_default();
+    s.spec = 1;
+    s.range = 4;
+    return s;
+}
+
+// matching.rs:103-142. Cameras: front 0, right 1, left 2 (matching.rs:42-45).
+extern "C" slm_status slm_scheduled_pairs(const uint64_t *views, uint32_t nv, const slm_pair_schedule *sch,
+                                          slm_pair *out, uint64_t cap, uint64_t *n_out) {
+    if ((!views && nv) || !sch || !n_out || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL argument");
+    std::vector<slm_pair> v;
+    for (uint32_t i = 0; i < nv; ++i)
+        for (uint32_t j = 0; j < nv; ++j) {
+            if (i == j) continue;
+            const uint64_t ca = views[2 * i], pa = views[2 * i + 1], cb = views[2 * j], pb = views[2 * j + 1];
+            const uint64_t d = absdiff(pa, pb);
+            bool ok;
+            if (ca == cb) {
+                ok = j > i && d >= 1 && (d <= sch->temporal || (is_pow2(d) && d <= sch->pow2_max));
+            } else if (sch->spec) {
+                ok = j > i && d <= sch->range;
+            } else {
+                bool has = false;
+                uint64_t lo = 0;
+                if (ca == 0 && cb == 1) has = true, lo = sch->right_min;
+                if (ca == 0 && cb == 2) has = true, lo = sch->left_min;
+                const uint64_t step = std::max<uint64_t>(sch->step, 1);
+                ok = has && pb >= pa + lo && pb <= pa + sch->max && (pb - pa - lo) % step == 0;
+            }
+            if (ok) v.push_back(slm_pair{std::min(i, j), std::max(i, j)});
+        }
+    std::sort(v.begin(), v.end(), [](const slm_pair &x, const slm_pair &y) {
+        return x.i != y.i ? x.i < y.i : x.j < y.j;
+    });
+    v.erase(std::unique(v.begin(), v.end(), [](const slm_pair &x, const slm_pair &y) {
+                return x.i == y.i && x.j == y.j;
+            }),
+            v.end());
+    return emit_pairs(v, out, cap, n_out);
+}

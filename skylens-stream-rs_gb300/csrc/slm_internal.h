@@ -1,0 +1,81 @@
+// slm_internal.h — data layouts and kernel launchers shared by the host
+// library (slm.cpp) and the CUDA translation units. Not part of the ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace slm {
+
+constexpr int kDesc = 128;      // descriptor length (features.rs:496)
+constexpr int kTile = 128;      // rows per store tile
+constexpr int kTileFloats = kTile * kDesc;
+
+// Component k of a descriptor goes to slot perm(k) inside a store tile so that
+// walking the slots in order walks the reference's accumulation order
+// (matching.rs:146-155: lane k % 8, step k / 8): slot = (k % 8) * 16 + k / 8.
+__host__ __device__ inline int perm_slot(int k) { return (k & 7) * 16 + (k >> 3); }
+
+// Store tile layout (FP32): tile[slot][row], 128 x 128 floats = 64 KiB.
+
+// Per-row partial state of an exact scan over a column range.
+struct __align__(16) RowPart {
+    float d1, d2;   // smallest and second smallest distance (multiset)
+    uint32_t j1;    // lowest column index attaining d1 (0xffffffff: none)
+    uint32_t pad;
+};
+
+// Per image pair, as planned on the host.
+struct PairMeta {
+    uint32_t a_row0, b_row0;  // first store row of the two views (multiples of 128)
+    uint32_t na, nb;          // descriptor counts
+    uint32_t nchunk;          // column chunks per row tile (exact path)
+    uint32_t part_base;       // first RowPart block (128 rows per block)
+    uint64_t col_base;        // first column-best entry
+    uint64_t slot_off;        // first output slot (capacity na)
+};
+
+// One unit of the exact kernel: rows [rt*128, rt*128+128) of pair `pair`
+// against store column tiles [ct0, ct1) of b.
+struct Item {
+    uint32_t pair, rt, ct0, ct1;
+    uint32_t part;  // RowPart block receiving the result
+    uint32_t pad[3];
+};
+
+struct ExactArgs {
+    const float *tiled;          // FP32 store tiles
+    const Item *items;
+    uint32_t n_items;
+    const PairMeta *pairs;
+    RowPart *parts;
+    unsigned long long *colbest; // (bits(d) << 32 | i), min-reduced
+    uint32_t *work;              // dynamic item counter (zeroed per launch)
+    uint32_t *err;               // device error word (zeroed per launch)
+    int mutual;
+    int x2;                      // 1: packed f32x2 arithmetic
+};
+
+struct FinalizeArgs {
+    const PairMeta *pairs;
+    uint32_t npairs;
+    const RowPart *parts;
+    const unsigned long long *colbest;
+    float ratio2;                // ratio * ratio in f32 (matching.rs:206)
+    int mutual;
+    uint2 *slots;                // output (i, j) slots
+    uint32_t *counts;            // per-pair match count
+};
+
+// Pack n row-major descriptors (src, n x 128) into store tiles starting at
+// tile index `tile0` (rows beyond n within the last tile are zeroed).
+void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0, cudaStream_t s);
+void launch_exact(const ExactArgs &a, int grid, cudaStream_t s);
+// Sets kernel attributes (large shared memory) once per device; called at
+// context creation, outside any stream capture. Fails if the kernel image
+// cannot load on the device.
+cudaError_t init_exact_kernels();
+void launch_finalize(const FinalizeArgs &a, cudaStream_t s);
+void launch_fill_u64(unsigned long long *p, uint64_t n, unsigned long long v, cudaStream_t s);
+
+}  // namespace slm

@@ -1,0 +1,166 @@
+"""Seeded synthetic descriptor workloads (no dataset is involved).
+
+SIFT-like descriptors follow the reference's normalisation (features.rs:575-582):
+per component |N(0,1)|, L2-normalise (f32), clip at 0.2, L2-normalise again.
+A "noisy copy" adds N(0, sigma) per component and normalises the same way.
+Random numbers come from numpy's PCG64 seeded with the workload seed.
+
+Workloads (sizes as named by the benchmark configurations):
+  pair_800        800 vs 800: 480 noisy permuted copies (sigma 0.05) + 320 fresh
+  pair_large      n vs n, a fraction of true correspondences (8192, 50 %)
+  pair_fp8        n vs n, 40 % true, sigma ~ U[0.02, 0.08] per copy (32768)
+  zone            3 cameras x P positions, n_v ~ U[300, 2000], candidate_pairs
+                  (5, 4, 16); views share landmarks so that overlapping pairs
+                  share 30-60 % of their descriptors
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+CLIP = np.float32(0.2)
+
+
+def _normalise(x: np.ndarray) -> np.ndarray:
+    x = x.astype(np.float32, copy=False)
+    n = np.sqrt(np.sum(x * x, axis=1, dtype=np.float32), dtype=np.float32)
+    n = np.where(n > 0, n, np.float32(1))
+    x = x / n[:, None]
+    x = np.minimum(x, CLIP)
+    n = np.sqrt(np.sum(x * x, axis=1, dtype=np.float32), dtype=np.float32)
+    n = np.where(n > 0, n, np.float32(1))
+    return np.ascontiguousarray((x / n[:, None]).astype(np.float32))
+
+
+def sift_like(rng: np.random.Generator, n: int) -> np.ndarray:
+    """n SIFT-like unit descriptors (n, 128) float32."""
+    return _normalise(np.abs(rng.standard_normal((n, 128), dtype=np.float32)))
+
+
+def noisy_copy(rng: np.random.Generator, x: np.ndarray, sigma) -> np.ndarray:
+    """Each row + N(0, sigma) per component, re-normalised; sigma scalar or per row."""
+    sig = np.asarray(sigma, dtype=np.float32)
+    if sig.ndim == 1:
+        sig = sig[:, None]
+    return _normalise(x + rng.standard_normal(x.shape, dtype=np.float32) * sig)
+
+
+def pair_800(seed: int = 0):
+    """800 vs 800: B = 480 noisy copies of a random permutation of A's rows
+    (sigma 0.05) plus 320 fresh draws, rows of B shuffled."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = sift_like(rng, 800)
+    perm = rng.permutation(800)[:480]
+    b = np.concatenate([noisy_copy(rng, a[perm], 0.05), sift_like(rng, 320)])
+    order = rng.permutation(len(b))
+    return a, np.ascontiguousarray(b[order])
+
+
+def pair_large(n: int = 8192, true_frac: float = 0.5, sigma=0.05, seed: int = 2):
+    """n vs n with round(true_frac*n) true correspondences (noisy copies)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = sift_like(rng, n)
+    k = int(round(true_frac * n))
+    src = rng.permutation(n)[:k]
+    if isinstance(sigma, tuple):
+        sig = rng.uniform(sigma[0], sigma[1], size=k).astype(np.float32)
+    else:
+        sig = sigma
+    b = np.concatenate([noisy_copy(rng, a[src], sig), sift_like(rng, n - k)])
+    order = rng.permutation(n)
+    return a, np.ascontiguousarray(b[order])
+
+
+def pair_fp8(n: int = 32768, seed: int = 4):
+    """n vs n, 40 % true correspondences with sigma ~ U[0.02, 0.08] per copy."""
+    return pair_large(n, 0.4, (0.02, 0.08), seed)
+
+
+def rig_views(positions: int, cameras: int = 3):
+    """(camera, position) of every view, id = cameras*pos + cam (synth.rs:284-291)."""
+    return [(c, p) for p in range(positions) for c in range(cameras)]
+
+
+@dataclass
+class Zone:
+    views: list            # (cam, pos) per view
+    desc: np.ndarray       # all descriptors, (N, 128) float32
+    offsets: np.ndarray    # first row of each view (uint64)
+    counts: np.ndarray     # rows per view (uint32)
+    pairs: np.ndarray      # (P, 2) view-id pairs from candidate_pairs
+    landmark: np.ndarray   # landmark id of each row (-1: unique to the view)
+
+    def view(self, v: int) -> np.ndarray:
+        o, n = int(self.offsets[v]), int(self.counts[v])
+        return self.desc[o:o + n]
+
+    @property
+    def distances(self) -> int:
+        c = self.counts.astype(np.int64)
+        return int(np.sum(c[self.pairs[:, 0]] * c[self.pairs[:, 1]]))
+
+    def overlap(self, u: int, v: int) -> float:
+        """Shared landmarks / min(n_u, n_v)."""
+        lu = self.landmark[int(self.offsets[u]):int(self.offsets[u]) + int(self.counts[u])]
+        lv = self.landmark[int(self.offsets[v]):int(self.offsets[v]) + int(self.counts[v])]
+        s = len(np.intersect1d(lu[lu >= 0], lv[lv >= 0]))
+        return s / max(1, min(len(lu), len(lv)))
+
+
+def candidate_pairs_np(views, temporal=5, cross=4, pow2_max=16) -> np.ndarray:
+    """Vectorised candidate_pairs (same rule as matching.rs:18-40) for workload setup."""
+    v = np.asarray(views, dtype=np.int64)
+    i, j = np.triu_indices(len(v), k=1)
+    ca, pa, cb, pb = v[i, 0], v[i, 1], v[j, 0], v[j, 1]
+    d = np.abs(pa - pb)
+    pow2 = (d > 0) & ((d & (d - 1)) == 0)
+    same = (ca == cb) & (d >= 1) & ((d <= temporal) | (pow2 & (d <= pow2_max)))
+    other = (ca != cb) & (d <= cross)
+    keep = same | other
+    return np.stack([i[keep], j[keep]], axis=1).astype(np.uint32)
+
+
+def zone(positions: int = 80, cameras: int = 3, n_range=(300, 2000), sigma: float = 0.05, seed: int = 3,
+         n_sampler=None, lifetime: int = 40, shared_frac: float = 0.6, alive: int = 1500) -> Zone:
+    """A zone of cameras x positions views whose overlapping pairs share landmarks.
+
+    Landmarks live for `lifetime` consecutive positions and carry a strength;
+    a view keeps its round(shared_frac * n_v) strongest live landmarks, each
+    as a noisy copy with sigma/sqrt(2) per component (so two observations of
+    one landmark differ by noise of sigma), and fills the rest with fresh
+    descriptors. Two views g positions apart then share about
+    shared_frac * (1 - g/lifetime) of the smaller view: 0.36-0.59 for the
+    candidate_pairs gaps (1..5, 8, 16 on one camera; 0..4 across cameras).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    views = rig_views(positions, cameras)
+    nv = len(views)
+    if n_sampler is None:
+        counts = rng.integers(n_range[0], n_range[1] + 1, size=nv).astype(np.int64)
+    else:
+        counts = np.asarray(n_sampler(rng, nv), dtype=np.int64)
+    births_per_pos = alive / lifetime
+    first = -lifetime
+    n_land = int(np.ceil((positions - first) * births_per_pos))
+    birth = np.sort(rng.uniform(first, positions, size=n_land))
+    strength = rng.random(n_land)
+    base = sift_like(rng, n_land)
+    sig_view = np.float32(sigma / np.sqrt(2.0))
+    rows, lmk = [], []
+    for v, (c, p) in enumerate(views):
+        n = int(counts[v])
+        live = np.nonzero((birth <= p) & (birth + lifetime > p))[0]
+        k = min(len(live), int(round(shared_frac * n)))
+        pick = live[np.argsort(-strength[live], kind="stable")[:k]]
+        obs = noisy_copy(rng, base[pick], sig_view)
+        fresh = sift_like(rng, n - k)
+        d = np.concatenate([obs, fresh])
+        lm = np.concatenate([pick, -np.ones(n - k, np.int64)])
+        order = rng.permutation(n)
+        rows.append(d[order])
+        lmk.append(lm[order])
+    desc = np.ascontiguousarray(np.concatenate(rows))
+    offsets = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
+    pairs = candidate_pairs_np(views)
+    return Zone(views, desc, offsets, counts.astype(np.uint32), pairs, np.concatenate(lmk))

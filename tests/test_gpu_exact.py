@@ -1,0 +1,162 @@
+"""GPU: the plain FP32 kernel against the oracle and the reference's tests.
+
+Every comparison is exact equality of match lists (bit-exact integer output).
+"""
+import threading
+
+import numpy as np
+import pytest
+
+import oracle as O
+import refcases
+import skylens_match as sm
+from skylens_match import synth
+
+pytestmark = pytest.mark.gpu
+PREC = "fp32"
+
+
+def rm_of(matcher, prec=PREC):
+    return lambda a, b, ratio, mutual: matcher.ratio_match(a, b, ratio, mutual, prec)
+
+
+@pytest.mark.parametrize("case", refcases.ALL, ids=lambda f: f.__name__)
+def test_reference_case(matcher, case):
+    case(rm_of(matcher))
+
+
+def check(matcher, a, b, ratio=0.8, mutual=True, prec=PREC, threads=8):
+    got = matcher.ratio_match_np(a, b, ratio, mutual, prec)
+    ref = O.ratio_match_np(a, b, ratio, mutual, threads=threads)
+    assert got.shape == ref.shape and np.array_equal(got, ref), (
+        f"{len(got)} vs {len(ref)} matches; first diff at "
+        f"{next((k for k in range(min(len(got), len(ref))) if tuple(got[k]) != tuple(ref[k])), None)}")
+    return got
+
+
+def test_pair_800(matcher):
+    a, b = synth.pair_800(0)
+    for mutual in (True, False):
+        check(matcher, a, b, 0.8, mutual)
+
+
+def test_pair_8192_full_size(matcher):
+    a, b = synth.pair_large(8192, 0.5, 0.05, seed=2)
+    m = check(matcher, a, b, 0.8, True, threads=16)
+    assert len(m) > 1000
+
+
+@pytest.mark.parametrize("na,nb", [(1, 2), (2, 1), (1, 1), (63, 64), (64, 63), (65, 129), (127, 128), (128, 127),
+                                   (129, 257), (255, 1), (257, 300), (1000, 3), (3, 1000), (600, 900)])
+def test_ragged_sizes(matcher, na, nb):
+    rng = np.random.Generator(np.random.PCG64(na * 1000 + nb))
+    a = synth.sift_like(rng, na)
+    k = min(na, nb) // 2
+    b = np.concatenate([synth.noisy_copy(rng, a[:k], 0.03), synth.sift_like(rng, nb - k)])
+    for ratio in (0.8, 1.0, 0.0, 1.5):
+        for mutual in (True, False):
+            check(matcher, a, b, ratio, mutual)
+
+
+def test_empty_inputs(matcher):
+    a, _ = O.match_fixture(9, 10, 0)
+    e = np.zeros((0, 128), np.float32)
+    assert matcher.ratio_match(a, e, 0.8, True) == []
+    assert matcher.ratio_match(e, a, 0.8, True) == []
+    assert matcher.ratio_match(e, e, 0.8, False) == []
+
+
+def test_exact_duplicates_and_ties(matcher):
+    """Duplicate rows of b tie at the row minimum (d1 == d2: no match); duplicate
+    rows of a tie at a column minimum (the lower i wins), across tile borders."""
+    rng = np.random.Generator(np.random.PCG64(7))
+    a = synth.sift_like(rng, 300)
+    b = synth.noisy_copy(rng, a, 0.02)
+    b[50] = b[10]
+    b[200] = b[10]
+    a[130] = a[5]
+    a[260] = a[5]
+    a[299] = a[129]
+    for mutual in (True, False):
+        check(matcher, a, b, 0.8, mutual)
+        check(matcher, b, a, 0.8, mutual)
+
+
+def test_nan_and_unnormalised_inputs(matcher):
+    rng = np.random.Generator(np.random.PCG64(8))
+    a = synth.sift_like(rng, 200) * 3.0
+    b = np.concatenate([synth.noisy_copy(rng, a[:100] / 3.0, 0.03), synth.sift_like(rng, 150)]) * 0.5
+    a[7, 3] = np.nan
+    b[11, 0] = np.nan
+    b[12] = np.inf
+    a[20] = 0.0
+    for mutual in (True, False):
+        check(matcher, a.astype(np.float32), b.astype(np.float32), 0.8, mutual)
+
+
+def test_concurrent_callers(matcher):
+    """ratio_match is called from many rayon workers at once (pipeline.rs:487-492)."""
+    z = synth.zone(positions=6, n_range=(200, 700), seed=11)
+    pairs = [tuple(map(int, p)) for p in z.pairs[:24]]
+    ref = {p: O.ratio_match_np(z.view(p[0]), z.view(p[1]), 0.8, True, threads=2) for p in pairs}
+    got, errs = {}, []
+
+    def worker(chunk):
+        try:
+            for p in chunk:
+                got[p] = matcher.ratio_match_np(z.view(p[0]), z.view(p[1]), 0.8, True, PREC)
+        except Exception as e:  # surfaced below
+            errs.append(e)
+
+    ths = [threading.Thread(target=worker, args=(pairs[k::6],)) for k in range(6)]
+    [t.start() for t in ths]
+    [t.join() for t in ths]
+    assert not errs, errs
+    for p in pairs:
+        assert np.array_equal(got[p], ref[p]), p
+
+
+def zone_check(matcher, z, prec, pairs=None, threads=16):
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    ids = st.add_views_packed(z.desc, z.offsets, z.counts)
+    assert ids == list(range(len(z.counts)))
+    pairs = z.pairs if pairs is None else pairs
+    plan = st.plan(pairs, 0.8, True, prec)
+    for rep in range(2):  # the second launch replays the captured graph
+        plan.launch()
+        per = plan.per_pair()
+        for k, (u, v) in enumerate(pairs):
+            ref = O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=threads)
+            assert np.array_equal(per[k], ref), f"pair {k} ({u},{v}) rep {rep}: {len(per[k])} vs {len(ref)}"
+    stats = plan.stats
+    plan.close()
+    st.close()
+    return stats
+
+
+def test_small_zone_batch(matcher):
+    z = synth.zone(positions=10, n_range=(100, 900), seed=5)
+    zone_check(matcher, z, PREC)
+
+
+def test_batch_with_repeated_and_reversed_pairs(matcher):
+    z = synth.zone(positions=4, n_range=(50, 400), seed=6)
+    pairs = np.array([[0, 1], [1, 0], [0, 1], [2, 2], [3, 5], [5, 3]], np.uint32)
+    zone_check(matcher, z, PREC, pairs)
+
+
+def test_device_entry_point(matcher):
+    torch = pytest.importorskip("torch")
+    a, b = synth.pair_800(1)
+    da = torch.from_numpy(a).cuda()
+    db = torch.from_numpy(b).cuda()
+    out = torch.zeros((800, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()  # inputs are ready before the library stream reads them
+    matcher.ratio_match_device(da.data_ptr(), 800, db.data_ptr(), 800, 0.8, True, PREC, out.data_ptr(), 800,
+                               cnt.data_ptr())
+    torch.cuda.ExternalStream(matcher.stream).synchronize()
+    n = int(cnt.item())
+    ref = O.ratio_match_np(a, b, 0.8, True, threads=4)
+    assert n == len(ref)
+    assert np.array_equal(out[:n].cpu().numpy().astype(np.uint32), ref)
