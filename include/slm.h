@@ -161,6 +161,7 @@ typedef struct {
     uint32_t items_per_sm;  /* FP32: target work items per SM when splitting columns */
     uint32_t shortlist_k;   /* shortlist slots per row (BF16/FP8) */
     uint32_t use_graph;     /* 1: replay a captured CUDA graph (default), 2: plain launches */
+    uint32_t variant;       /* FP32 arithmetic: 0 packed f32x2 (default), 1 scalar */
 } slm_tune;
 
 /* Plan the matching of np image pairs (view-id pairs in `pairs`, the

@@ -285,10 +285,11 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.work = ctl;
         a.err = ctl + 1;
         a.mutual = p->mutual;
-        a.x2 = (p->tune.use_graph & 16) ? 1 : 0;
-        SLM_CU(cudaEventRecord(p->ev0, s));
+        a.x2 = p->tune.variant == 1 ? 0 : 1;
+        // External records so that the events become timing nodes under graph capture.
+        SLM_CU(cudaEventRecordWithFlags(p->ev0, s, cudaEventRecordExternal));
         if (a.n_items) launch_exact(a, std::min<int>(p->ctx->sms, (int)a.n_items), s);
-        SLM_CU(cudaEventRecord(p->ev1, s));
+        SLM_CU(cudaEventRecordWithFlags(p->ev1, s, cudaEventRecordExternal));
         p->kernels = (p->mutual ? 1 : 0) + (a.n_items ? 1 : 0) + (p->np ? 1 : 0) + 1 + (p->np ? 1 : 0);
         FinalizeArgs f{};
         f.pairs = p->d_meta.as<PairMeta>();
@@ -629,7 +630,7 @@ extern "C" slm_status slm_plan_destroy(slm_plan *p) {
 extern "C" slm_status slm_plan_launch(slm_plan *p) {
     if (!p) return fail(SLM_INVALID_ARG, "NULL plan");
     SLM_TRY(ctx_check_device(p->ctx));
-    return plan_launch_on(p, p->stream, (p->tune.use_graph & 15) != 2);
+    return plan_launch_on(p, p->stream, p->tune.use_graph != 2);
 }
 
 extern "C" slm_status slm_plan_results(slm_plan *p, slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *st) {

@@ -41,7 +41,7 @@ class SlmPairSchedule(ctypes.Structure):
 
 
 class SlmTune(ctypes.Structure):
-    _fields_ = [("items_per_sm", c_u32), ("shortlist_k", c_u32), ("use_graph", c_u32)]
+    _fields_ = [("items_per_sm", c_u32), ("shortlist_k", c_u32), ("use_graph", c_u32), ("variant", c_u32)]
 
 
 class SlmError(RuntimeError):

@@ -187,22 +187,22 @@ class DescriptorStore:
             pass
 
     def plan(self, pairs, ratio: float = 0.8, mutual: bool = True, precision="fp32", *, items_per_sm: int = 0,
-             shortlist_k: int = 0, use_graph: int = 1) -> "BatchPlan":
-        return BatchPlan(self, pairs, ratio, mutual, precision, items_per_sm, shortlist_k, use_graph)
+             shortlist_k: int = 0, use_graph: int = 1, variant: int = 0) -> "BatchPlan":
+        return BatchPlan(self, pairs, ratio, mutual, precision, items_per_sm, shortlist_k, use_graph, variant)
 
 
 class BatchPlan:
     """A planned batch of image pairs (pipeline.rs:485-493), replayed as one CUDA graph."""
 
     def __init__(self, store: DescriptorStore, pairs, ratio, mutual, precision, items_per_sm=0, shortlist_k=0,
-                 use_graph=1):
+                 use_graph=1, variant=0):
         self.store = store
         self._L = store._L
         pr = _pairs_array(pairs)
         self.np = len(pr)
         self.total_rows = int(sum(store.counts[int(u)] for u, _ in pr)) if len(pr) else 0
         self.distances = int(sum(store.counts[int(u)] * store.counts[int(v)] for u, v in pr)) if len(pr) else 0
-        tune = SlmTune(items_per_sm, shortlist_k, use_graph)
+        tune = SlmTune(items_per_sm, shortlist_k, use_graph, variant)
         h = ctypes.c_void_p()
         check(self._L.slm_plan_create(store.m.handle, store.handle, pr.ctypes.data_as(ctypes.POINTER(SlmPair)),
                                       self.np, ctypes.c_float(ratio), int(bool(mutual)), _prec(precision),

@@ -122,7 +122,7 @@ def candidate_pairs_np(views, temporal=5, cross=4, pow2_max=16) -> np.ndarray:
 
 
 def zone(positions: int = 80, cameras: int = 3, n_range=(300, 2000), sigma: float = 0.05, seed: int = 3,
-         n_sampler=None, lifetime: int = 40, shared_frac: float = 0.6, alive: int = 1500) -> Zone:
+         n_sampler=None, lifetime: int = 40, shared_frac: float = 0.595, alive: int = 1500) -> Zone:
     """A zone of cameras x positions views whose overlapping pairs share landmarks.
 
     Landmarks live for `lifetime` consecutive positions and carry a strength;
