@@ -161,7 +161,9 @@ typedef struct {
     uint32_t items_per_sm;  /* FP32: target work items per SM when splitting columns */
     uint32_t shortlist_k;   /* shortlist slots per row (BF16/FP8) */
     uint32_t use_graph;     /* 1: replay a captured CUDA graph (default), 2: plain launches */
-    uint32_t variant;       /* FP32 arithmetic: 0 packed f32x2 (default), 1 scalar */
+    uint32_t variant;       /* FP32: 0 packed f32x2 arithmetic (default), 1 scalar.
+                               BF16/FP8: 2 keeps the approximate distances of pair 0
+                               for slm_plan_debug_dump (diagnostics) */
 } slm_tune;
 
 /* Plan the matching of np image pairs (view-id pairs in `pairs`, the
@@ -180,6 +182,10 @@ slm_status slm_plan_results(slm_plan *p, slm_pair *out, uint64_t cap, uint64_t *
  * and the padded match slots (pair k at row offset slot_offsets[k]). */
 slm_status slm_plan_device_results(slm_plan *p, const uint32_t **d_counts, const slm_pair **d_slots,
                                    const uint64_t **h_slot_offsets);
+/* Diagnostics: the tensor-core distance estimates d~ of the plan's first
+ * pair (na x nb floats, row-major) from its last launch. Only for plans made
+ * with slm_tune.variant = 2 and precision BF16 or FP8. */
+slm_status slm_plan_debug_dump(slm_plan *p, float *out, uint64_t cap);
 /* Bytes of device scratch the plan holds. */
 uint64_t slm_plan_bytes(slm_plan *p);
 

@@ -78,6 +78,18 @@ __global__ void copy_pairs_kernel(const uint2 *__restrict__ src, const uint64_t 
     if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = (uint32_t)n;
 }
 
+__global__ void fill_u32_kernel(uint32_t *p, uint64_t n, uint32_t v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s) {
+    if (!n) return;
+    uint64_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    fill_u32_kernel<<<(unsigned)blocks, 256, 0, s>>>(p, n, v);
+}
+
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s) {
     scan_counts_kernel<<<1, 1024, 0, s>>>(counts, np, offsets);
 }

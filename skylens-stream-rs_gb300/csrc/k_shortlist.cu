@@ -1,0 +1,899 @@
+// k_shortlist.cu — BF16 / FP8 tcgen05 shortlist path of ratio_match.
+//
+// Reference: crates/core/src/matching.rs:144-215. See slm_shortlist.h for the
+// passes and the certification rules. Every match decision is either proven
+// by the per-pair error bound eps or settled with exact spec-order FP32
+// distances (matching.rs:146-155), so results equal the reference's.
+//
+// Tensor-core kernel (sl_pass_kernel, one persistent CTA per SM, 10 warps):
+//   warp 0      TMA producer: per item the a tiles (1 or 2 x 128 rows, K-major,
+//               128B-swizzled operand images copied verbatim from the store)
+//               and their norms; per 128-column b tile the operand tile, norms
+//               (and, in pass 2, column thresholds) through a 4-slot ring.
+//   warp 1      allocates 512 TMEM columns; one thread issues tcgen05.mma
+//               (M=128, N=128, K=16 bf16 / K=32 e4m3) into a double-buffered
+//               pair of 128x128 f32 accumulators per a tile.
+//   warps 2-9   epilogue: warp w reads TMEM lane quarter w % 4 of a tile
+//               (w - 2) / 4, one thread per row, 32 columns per tcgen05.ld;
+//               d~ = |a|^2 + |b|^2 - 2 acc. Row minima use a 3-input min tree
+//               per 32 columns; column minima use redux.sync.min.f32 per
+//               column, merged across warps in shared memory and across CTAs
+//               with one atomicMin per column and tile.
+#include <cuda_fp8.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ptx.cuh"
+#include "slm_shortlist.h"
+
+namespace slm {
+
+// ------------------------------------------------------------ small helpers
+
+// Order-preserving map of f32 to u32 (unsigned order == float order).
+SLM_DEV uint32_t f2ord(float f) {
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+SLM_DEV float ord2f(uint32_t u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+
+SLM_DEV float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+SLM_DEV float warp_min_f32(float v) {
+    float r;
+    asm volatile("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
+}
+
+SLM_DEV uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Minimum of 32 values (NaN inputs are ignored by min.f32).
+SLM_DEV float min32(const float (&d)[32]) {
+    float m[11];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m[k] = min3f(d[3 * k], d[3 * k + 1], d[3 * k + 2]);
+    m[10] = fminf(d[30], d[31]);
+    const float x = min3f(m[0], m[1], m[2]);
+    const float y = min3f(m[3], m[4], m[5]);
+    const float z = min3f(m[6], m[7], m[8]);
+    return fminf(min3f(x, y, z), fminf(m[9], m[10]));
+}
+
+// Exact reference distance (matching.rs:146-155): lane k = components 8c+k.
+SLM_DEV float sq_dist_spec(const float *__restrict__ p, const float *__restrict__ r) {
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const float4 *p4 = reinterpret_cast<const float4 *>(p);
+    const float4 *r4 = reinterpret_cast<const float4 *>(r);
+#pragma unroll 4
+    for (int c = 0; c < 16; ++c) {
+        const float4 x0 = p4[2 * c], x1 = p4[2 * c + 1];
+        const float4 y0 = r4[2 * c], y1 = r4[2 * c + 1];
+        const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        const float ys[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float t = __fsub_rn(xs[k], ys[k]);
+            acc[k] = __fadd_rn(acc[k], __fmul_rn(t, t));
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s = __fadd_rn(s, acc[k]);
+    return s;
+}
+
+// ------------------------------------------------------------ store packing
+
+// One CTA (128 threads) per 128-row tile of a view: low-precision operand
+// image (K-major, 128B swizzle: 16-byte chunk c of row r at c ^ (r % 8)),
+// f32 squared norms, and the view's error statistics.
+template <bool FP8>
+__global__ void __launch_bounds__(128) pack_lowp_kernel(const float *__restrict__ raw, uint32_t row0, uint32_t n,
+                                                        uint32_t view, uint8_t *__restrict__ optiles,
+                                                        float *__restrict__ norms, float *__restrict__ qscale,
+                                                        ViewStat *__restrict__ vstats) {
+    const uint32_t r = threadIdx.x;
+    const uint32_t tile = blockIdx.x;
+    const uint32_t row = tile * kTile + r;  // row within the view
+    const bool valid = row < n;
+    const float *src = raw + (size_t)(row0 + row) * kDesc;
+    constexpr uint32_t kTileBytes = FP8 ? kFp8TileBytes : kBf16TileBytes;
+    uint8_t *dst = optiles + (size_t)(row0 / kTile + tile) * kTileBytes;
+    float x[kDesc];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+        float4 v = valid ? reinterpret_cast<const float4 *>(src)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        x[4 * q] = v.x;
+        x[4 * q + 1] = v.y;
+        x[4 * q + 2] = v.z;
+        x[4 * q + 3] = v.w;
+    }
+    float nrm = 0.f, res = 0.f, nq = 0.f, amax = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < kDesc; ++k) {
+        nrm = __fadd_rn(nrm, __fmul_rn(x[k], x[k]));
+        bad |= !isfinite(x[k]);
+        amax = fmaxf(amax, fabsf(x[k]));
+    }
+    float scale = 1.f, inv = 1.f;
+    if constexpr (FP8) {
+        // per-descriptor power-of-two scale: max |a| * scale <= 448 (E4M3 max)
+        if (amax > 0.f && isfinite(amax)) {
+            int e;
+            frexpf(448.f / amax, &e);
+            scale = ldexpf(1.f, e - 1);
+            inv = ldexpf(1.f, 1 - e);
+        }
+    }
+#pragma unroll
+    for (int c16 = 0; c16 < (FP8 ? 8 : 16); ++c16) {
+        uint32_t w[4];
+        if constexpr (FP8) {
+            // 16 components -> 16 bytes
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                uint32_t word = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int k = c16 * 16 + h * 4 + b;
+                    const __nv_fp8_storage_t q = __nv_cvt_float_to_fp8(x[k] * scale, __NV_SATFINITE, __NV_E4M3);
+                    __nv_fp8_e4m3 qq;
+                    qq.__x = q;
+                    const float back = static_cast<float>(qq) * inv;
+                    const float e = x[k] - back;
+                    res = fmaf(e, e, res);
+                    nq = fmaf(back, back, nq);
+                    word |= (uint32_t)q << (8 * b);
+                }
+                w[h] = word;
+            }
+            const uint32_t chunk = (uint32_t)c16;  // 128 bytes per row = one swizzle span
+            uint4 *d = reinterpret_cast<uint4 *>(dst + r * 128 + ((chunk ^ (r & 7)) * 16));
+            *d = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const int k = c16 * 8 + h * 2;
+                const __nv_bfloat16 lo = __float2bfloat16_rn(x[k]);
+                const __nv_bfloat16 hi = __float2bfloat16_rn(x[k + 1]);
+                const float blo = __bfloat162float(lo), bhi = __bfloat162float(hi);
+                const float e0 = x[k] - blo, e1 = x[k + 1] - bhi;
+                res = fmaf(e0, e0, fmaf(e1, e1, res));
+                nq = fmaf(blo, blo, fmaf(bhi, bhi, nq));
+                w[h] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+            }
+            const uint32_t kb = (uint32_t)c16 >> 3, chunk = (uint32_t)c16 & 7;
+            uint4 *d = reinterpret_cast<uint4 *>(dst + kb * 16384 + r * 128 + ((chunk ^ (r & 7)) * 16));
+            *d = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+    norms[row0 + row] = valid ? nrm : 0.f;
+    if constexpr (FP8) qscale[row0 + row] = inv;
+    // statistics (non-negative floats compare as their bit patterns)
+    float s_n = valid ? sqrtf(nrm) : 0.f, s_r = valid ? sqrtf(res) : 0.f, s_q = valid ? sqrtf(nq) : 0.f;
+    if (!isfinite(s_n) || !isfinite(s_r) || !isfinite(s_q)) bad = bad || valid;
+    uint32_t b = (valid && bad) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s_n = fmaxf(s_n, __shfl_xor_sync(0xffffffffu, s_n, o));
+        s_r = fmaxf(s_r, __shfl_xor_sync(0xffffffffu, s_r, o));
+        s_q = fmaxf(s_q, __shfl_xor_sync(0xffffffffu, s_q, o));
+        b |= __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((r & 31) == 0) {
+        ViewStat *vs = vstats + view;
+        if (isfinite(s_n)) atomicMax(&vs->nmax, __float_as_uint(s_n));
+        if (isfinite(s_r)) atomicMax(&vs->rho, __float_as_uint(s_r));
+        if (isfinite(s_q)) atomicMax(&vs->nqmax, __float_as_uint(s_q));
+        if (b) atomicOr(&vs->bad, 1u);
+    }
+}
+
+void launch_pack_lowp(const float *raw, uint32_t row0, uint32_t n, uint32_t view, int fp8, uint8_t *optiles,
+                      float *norms, float *qscale, ViewStat *vstats, cudaStream_t s) {
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    if (!tiles) return;
+    if (fp8)
+        pack_lowp_kernel<true><<<tiles, 128, 0, s>>>(raw, row0, n, view, optiles, norms, qscale, vstats);
+    else
+        pack_lowp_kernel<false><<<tiles, 128, 0, s>>>(raw, row0, n, view, optiles, norms, qscale, vstats);
+}
+
+// ------------------------------------------------------------ tcgen05 pieces
+
+// Shared-memory matrix descriptor (tcgen05): K-major, 128B swizzle, 8-row
+// groups 1024 bytes apart (stride byte offset), version 1, base offset 0.
+SLM_DEV uint64_t umma_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3fffu);   // start address
+    d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+    d |= (uint64_t)1 << 46;                    // descriptor version
+    d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: f32 accumulate, K-major A and B, M=128, N=128.
+// kind::f16 with bf16 inputs (format 1) or kind::f8f6f4 with e4m3 (format 0).
+__host__ __device__ constexpr uint32_t umma_idesc(bool fp8) {
+    return (1u << 4) | ((fp8 ? 0u : 1u) << 7) | ((fp8 ? 0u : 1u) << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+template <bool FP8>
+struct SlSmem {
+    static constexpr uint32_t kOp = FP8 ? kFp8TileBytes : kBf16TileBytes;
+    uint8_t A[2][kOp];
+    uint8_t B[kSlStages][kOp];
+    float bnorm[kSlStages][128];
+    float bthr[kSlStages][128];
+    float bscale[kSlStages][128];
+    float anorm[256];
+    float athr[256];
+    float ascale[256];
+    float colpart[2][8][128];
+    uint64_t a_full, a_empty;
+    uint64_t b_full[kSlStages], b_empty[kSlStages];
+    uint64_t t_full[2], t_empty[2];
+    uint64_t ep_bar;  // epilogue warps: column partials of a tile are stored
+    uint32_t tmem_base;
+    uint32_t abort_flag;
+};
+
+template <bool FP8>
+constexpr size_t sl_smem_bytes() {
+    return sizeof(SlSmem<FP8>) + 1024;  // slack for 1024-byte alignment
+}
+
+// Bounded wait (about 2 s of wall time); on timeout raises the CTA abort flag
+// and records an error so every role leaves its loop.
+SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_flag, uint32_t *err) {
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63) {
+            if (*abort_flag) return false;
+            const uint64_t now = globaltimer();
+            if (t0 == 0) t0 = now;
+            else if (now - t0 > 2000000000ull) {
+                *abort_flag = 1;
+                atomicCAS(err, 0u, (uint32_t)DERR_TIMEOUT_MMA);
+                return false;
+            }
+        }
+    }
+}
+
+template <int PASS, bool FP8>
+__global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
+    extern __shared__ uint8_t sl_smem_raw[];
+    const uint32_t pad = (1024u - (smem_u32(sl_smem_raw) & 1023u)) & 1023u;
+    SlSmem<FP8> &S = *reinterpret_cast<SlSmem<FP8> *>(sl_smem_raw + pad);
+    constexpr uint32_t kOp = SlSmem<FP8>::kOp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t *err = g.ctl + 1;
+    volatile uint32_t *abort_flag = &S.abort_flag;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&S.a_full, 1);
+        mbar_init(&S.a_empty, 1 + 8);
+        for (int s = 0; s < kSlStages; ++s) {
+            mbar_init(&S.b_full[s], 1);
+            mbar_init(&S.b_empty[s], 1 + 8);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&S.t_full[b], 1);
+            mbar_init(&S.t_empty[b], 8);
+        }
+        mbar_init(&S.ep_bar, 8);
+        S.abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(&S.tmem_base, 512);
+        tmem_relinquish();
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------- producer
+        if (lane == 0) {
+            uint32_t st = 0, sph = 0, iter = 0;
+            for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+                const SlItem item = g.items[it];
+                const PairMeta pm = g.pairs[item.pair];
+                const SlPair sp = g.spairs[item.pair];
+                if (iter > 0 && !sl_wait(&S.a_empty, (iter - 1) & 1, abort_flag, err)) break;
+                const uint32_t arow = pm.a_row0 + item.rt0 * kTile;  // store row of the first a row
+                uint32_t bytes = item.nat * kOp + item.nat * 512;
+                if (PASS == 2) bytes += item.nat * 512;
+                if (FP8) bytes += item.nat * 512;
+                mbar_arrive_expect_tx(&S.a_full, bytes);
+                for (uint32_t a = 0; a < item.nat; ++a) {
+                    bulk_g2s(S.A[a], g.optiles + (size_t)(arow / kTile + a) * kOp, kOp, &S.a_full);
+                    bulk_g2s(&S.anorm[a * 128], g.norms + arow + a * 128, 512, &S.a_full);
+                    if (PASS == 2)
+                        bulk_g2s(&S.athr[a * 128], g.rowthr + sp.rbase + (item.rt0 + a) * kTile, 512, &S.a_full);
+                    if (FP8) bulk_g2s(&S.ascale[a * 128], g.qscale + arow + a * 128, 512, &S.a_full);
+                }
+                for (uint32_t t = item.ct0; t < item.ct1; ++t) {
+                    if (!sl_wait(&S.b_empty[st], sph ^ 1, abort_flag, err)) break;
+                    const uint32_t brow = pm.b_row0 + t * kTile;
+                    uint32_t bb = kOp + 512 + (PASS == 2 ? 512 : 0) + (FP8 ? 512 : 0);
+                    mbar_arrive_expect_tx(&S.b_full[st], bb);
+                    bulk_g2s(S.B[st], g.optiles + (size_t)(brow / kTile) * kOp, kOp, &S.b_full[st]);
+                    bulk_g2s(S.bnorm[st], g.norms + brow, 512, &S.b_full[st]);
+                    if (PASS == 2) bulk_g2s(S.bthr[st], g.colthr + sp.cbase + t * kTile, 512, &S.b_full[st]);
+                    if (FP8) bulk_g2s(S.bscale[st], g.qscale + brow, 512, &S.b_full[st]);
+                    if (++st == kSlStages) st = 0, sph ^= 1;
+                }
+                if (*abort_flag) break;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------- MMA issue
+        constexpr uint32_t idesc = umma_idesc(FP8);
+        uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
+        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+            const SlItem item = g.items[it];
+            if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
+            bool ok = true;
+            for (uint32_t t = item.ct0; t < item.ct1; ++t) {
+                if (!sl_wait(&S.b_full[st], sph, abort_flag, err) || !sl_wait(&S.t_empty[tb], tph ^ 1, abort_flag, err)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                if (lane == 0) {
+                    for (uint32_t a = 0; a < item.nat; ++a) {
+                        const uint32_t d_tmem = tmem + (tb * 2 + a) * 128;
+                        const uint32_t abase = smem_u32(S.A[a]), bbase = smem_u32(S.B[st]);
+                        if constexpr (FP8) {
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)  // K = 32 e4m3 = 32 bytes per step
+                                mma_f8(d_tmem, umma_desc(abase + k * 32), umma_desc(bbase + k * 32), idesc, k > 0);
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {  // K = 16 bf16 = 32 bytes per step
+                                const uint32_t off = (k >> 2) * 16384 + (k & 3) * 32;
+                                mma_f16(d_tmem, umma_desc(abase + off), umma_desc(bbase + off), idesc, k > 0);
+                            }
+                        }
+                    }
+                    mma_commit(&S.b_empty[st]);
+                    mma_commit(&S.t_full[tb]);
+                }
+                __syncwarp();
+                if (++st == kSlStages) st = 0, sph ^= 1;
+                tb ^= 1;
+                if (tb == 0) tph ^= 1;
+            }
+            if (lane == 0) mma_commit(&S.a_empty);
+            __syncwarp();
+            if (!ok) break;
+        }
+    } else {
+        // ---------------------------------------------------------- epilogue
+        const int ep = warp - 2;            // 0..7
+        const int at = ep >> 2;             // which a tile
+        const int q = warp & 3;             // TMEM lane quarter this warp may access
+        const int r = at * 128 + q * 32 + lane;  // row within the item
+        const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+        uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0, eph = 0;
+        const float kInf = __int_as_float(0x7f800000);
+        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+            const SlItem item = g.items[it];
+            const PairMeta pm = g.pairs[item.pair];
+            const SlPair sp = g.spairs[item.pair];
+            if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
+            const bool active = at < (int)item.nat;          // warp-uniform
+            const uint32_t i = item.rt0 * kTile + r;          // row within the pair
+            const bool rvalid = active && i < pm.na;
+            const float na_i = active ? S.anorm[r] : 0.f;
+            const float thr_i = (PASS == 2 && active) ? S.athr[r] : -kInf;
+            const float sa_i = (FP8 && active) ? S.ascale[r] : 1.f;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.a_empty);
+            float m1 = kInf, m2 = kInf;
+            bool ok = true;
+            for (uint32_t t = item.ct0; t < item.ct1; ++t) {
+                if (!sl_wait(&S.b_full[st], sph, abort_flag, err) || !sl_wait(&S.t_full[tb], tph, abort_flag, err)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                if (active) {
+                    const bool any_invalid_row = __any_sync(0xffffffffu, !rvalid);
+#pragma unroll 1
+                    for (int c = 0; c < 4; ++c) {
+                        uint32_t v[32];
+                        tmem_ld32(tmem + lane_addr + (tb * 2 + at) * 128 + c * 32, v);
+                        tmem_wait_ld();
+                        const uint32_t j0 = t * kTile + c * 32;
+                        float d[32];
+                        const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][c * 32]);
+                        if constexpr (FP8) {
+                            const float4 *bs4 = reinterpret_cast<const float4 *>(&S.bscale[st][c * 32]);
+                            const float m2sa = -2.f * sa_i;
+#pragma unroll
+                            for (int k4 = 0; k4 < 8; ++k4) {
+                                const float4 nb = bn4[k4], sb = bs4[k4];
+                                const float nbv[4] = {nb.x, nb.y, nb.z, nb.w}, sbv[4] = {sb.x, sb.y, sb.z, sb.w};
+#pragma unroll
+                                for (int e = 0; e < 4; ++e)
+                                    d[4 * k4 + e] = fmaf(__uint_as_float(v[4 * k4 + e]), m2sa * sbv[e], na_i + nbv[e]);
+                            }
+                        } else {
+#pragma unroll
+                            for (int k4 = 0; k4 < 8; ++k4) {
+                                const float4 nb = bn4[k4];
+                                const float nbv[4] = {nb.x, nb.y, nb.z, nb.w};
+#pragma unroll
+                                for (int e = 0; e < 4; ++e)
+                                    d[4 * k4 + e] = fmaf(__uint_as_float(v[4 * k4 + e]), -2.f, na_i + nbv[e]);
+                            }
+                        }
+                        if (j0 + 32 > pm.nb) {  // ragged last tile: padding columns never win
+#pragma unroll
+                            for (int k = 0; k < 32; ++k)
+                                if (j0 + k >= pm.nb) d[k] = kInf;
+                        }
+                        if constexpr (PASS == 1) {
+                            if (g.dump && item.pair == 0 && rvalid) {
+#pragma unroll
+                                for (int k = 0; k < 32; ++k)
+                                    if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = d[k];
+                            }
+                            const float cm = min32(d);
+                            m2 = fminf(m2, fmaxf(m1, cm));
+                            m1 = fminf(m1, cm);
+                            if (any_invalid_row) {
+#pragma unroll
+                                for (int k = 0; k < 32; ++k) d[k] = rvalid ? d[k] : kInf;
+                            }
+                            float4 *cp = reinterpret_cast<float4 *>(&S.colpart[tb][ep][c * 32]);
+#pragma unroll
+                            for (int k4 = 0; k4 < 8; ++k4) {
+                                float4 o;
+                                o.x = warp_min_f32(d[4 * k4 + 0]);
+                                o.y = warp_min_f32(d[4 * k4 + 1]);
+                                o.z = warp_min_f32(d[4 * k4 + 2]);
+                                o.w = warp_min_f32(d[4 * k4 + 3]);
+                                if (lane == 0) cp[k4] = o;
+                            }
+                        } else {
+                            if (thr_i > -kInf) {
+                                const float cm = min32(d);
+                                if (cm <= thr_i) {
+                                    const uint32_t ridx = sp.rbase + i;
+#pragma unroll
+                                    for (int k = 0; k < 32; ++k) {
+                                        if (d[k] <= thr_i) {
+                                            const uint32_t s = atomicAdd(&g.rowcnt[ridx], 1u);
+                                            if (s < kSlRowSlots)
+                                                g.rowcand[(size_t)ridx * kSlRowSlots + s] =
+                                                    make_uint2(j0 + k, __float_as_uint(d[k]));
+                                        }
+                                    }
+                                }
+                            }
+                            if (rvalid) {
+                                const float4 *bt4 = reinterpret_cast<const float4 *>(&S.bthr[st][c * 32]);
+                                float x[32];
+#pragma unroll
+                                for (int k4 = 0; k4 < 8; ++k4) {
+                                    const float4 tt = bt4[k4];
+                                    x[4 * k4 + 0] = d[4 * k4 + 0] - tt.x;
+                                    x[4 * k4 + 1] = d[4 * k4 + 1] - tt.y;
+                                    x[4 * k4 + 2] = d[4 * k4 + 2] - tt.z;
+                                    x[4 * k4 + 3] = d[4 * k4 + 3] - tt.w;
+                                }
+                                const float xm = min32(x);
+                                if (xm <= 0.f) {
+#pragma unroll
+                                    for (int k = 0; k < 32; ++k) {
+                                        if (x[k] <= 0.f) {
+                                            const uint32_t cidx = sp.cbase + j0 + k;
+                                            const uint32_t s = atomicAdd(&g.colcnt[cidx], 1u);
+                                            if (s < kSlColSlots) g.colcand[(size_t)cidx * kSlColSlots + s] = i;
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.t_empty[tb]);
+                if constexpr (PASS == 1) {
+                    // all 8 epilogue warps have stored their column partials of this tile
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.ep_bar);
+                    if (!sl_wait(&S.ep_bar, eph, abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    eph ^= 1;
+                    const int e = threadIdx.x - 64;
+                    if (e < 128) {
+                        float m = kInf;
+                        for (int w = 0; w < 8; ++w)
+                            if ((w >> 2) < (int)item.nat) m = fminf(m, S.colpart[tb][w][e]);
+                        const uint32_t j = t * kTile + e;
+                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(m));
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.b_empty[st]);
+                if (++st == kSlStages) st = 0, sph ^= 1;
+                tb ^= 1;
+                if (tb == 0) tph ^= 1;
+            }
+            if (!ok) break;
+            if constexpr (PASS == 1) {
+                if (active) g.rowpart[(size_t)item.part * 256 + r] = make_float2(m1, m2);
+            }
+        }
+    }
+    // Everyone done: no MMA in flight (the epilogue consumed every commit).
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 512);
+    }
+}
+
+// ------------------------------------------------------------------ mid
+
+// Per pair: eps from the views' statistics, row thresholds from the pass-1
+// partials, column thresholds from the column minima.
+__global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
+    __shared__ float eps_sh;
+    __shared__ uint32_t unsafe_sh;
+    const uint32_t p = blockIdx.x;
+    const PairMeta pm = g.pairs[p];
+    SlPair &sp = g.spairs[p];
+    const float kInf = __int_as_float(0x7f800000);
+    if (threadIdx.x == 0) {
+        const ViewStat va = g.vstats[sp.view_a], vb = g.vstats[sp.view_b];
+        const double A = __uint_as_float(va.nmax), B = __uint_as_float(vb.nmax);
+        const double Ra = __uint_as_float(va.rho), Rb = __uint_as_float(vb.rho);
+        const double Qa = __uint_as_float(va.nqmax), Qb = __uint_as_float(vb.nqmax);
+        bool unsafe = va.bad || vb.bad || !(A <= 64.0) || !(B <= 64.0);
+        // |d~ - d| <= 2 |a.b - q(a).q(b)| + accumulation and rounding terms, with
+        // |a.b - q(a).q(b)| <= |a - q(a)| |b| + |q(a)| |b - q(b)| (Cauchy-Schwarz).
+        double eps = 2.0 * (Ra * B + Qa * Rb) * (1.0 + 1e-3);
+        eps += 5e-4 * Qa * Qb + 5e-5 * (A * A + B * B) + 2e-5 * (A + B) * (A + B) + 1e-6;
+        if (!(eps < 1e30)) unsafe = true;
+        eps_sh = unsafe ? kInf : (float)(eps * (1.0 + 1e-6));
+        unsafe_sh = unsafe ? 1u : 0u;
+        sp.eps = eps_sh;
+        sp.unsafe = unsafe_sh;
+    }
+    __syncthreads();
+    const float eps = eps_sh;
+    const bool unsafe = unsafe_sh != 0;
+    const double r2 = (double)g.ratio2;
+    const uint32_t na_pad = (pm.na + kTile - 1) / kTile * kTile;
+    for (uint32_t i = threadIdx.x; i < na_pad; i += blockDim.x) {
+        float thr = -kInf;
+        if (i < pm.na && !unsafe && pm.nb > 0) {
+            const uint32_t super = i / 256, r = i % 256;
+            float m1 = kInf, m2 = kInf;
+            for (uint32_t c = 0; c < sp.nchunk; ++c) {
+                const float2 v = g.rowpart[(size_t)(sp.part_base + super * sp.nchunk + c) * 256 + r];
+                m2 = fminf(fminf(m2, v.y), fmaxf(m1, v.x));
+                m1 = fminf(m1, v.x);
+            }
+            // certain "no match": d1 >= m1 - eps >= r^2 (m2' + eps) >= fl(r^2 d2) (rounding margin 1e-6)
+            const bool no_match = (double)m1 - eps >= r2 * ((double)m2 + eps) * (1.0 + 1e-6);
+            if (!no_match) thr = (float)(((double)m2 + 2.0 * eps) * (1.0 + 1e-6));
+            if (!(thr == thr)) thr = kInf;  // NaN guard: collect everything
+        }
+        g.rowthr[sp.rbase + i] = thr;
+    }
+    const uint32_t nb_pad = (pm.nb + kTile - 1) / kTile * kTile;
+    for (uint32_t j = threadIdx.x; j < nb_pad; j += blockDim.x) {
+        float thr = -kInf;
+        if (j < pm.nb && !unsafe) {
+            const float c1 = ord2f(g.colmin[sp.cbase + j]);
+            thr = (float)(((double)c1 + 2.0 * eps) * (1.0 + 1e-6));
+            if (!(thr == thr)) thr = kInf;
+        }
+        g.colthr[sp.cbase + j] = thr;
+    }
+}
+
+// ------------------------------------------------------------- finalize
+
+SLM_DEV void sl_enqueue(const SlArgs &g, uint32_t pair, uint32_t kind, uint32_t i, uint32_t j) {
+    const uint32_t s = atomicAdd(&g.ctl[kCtlQueueLen], 1u);
+    if (s < g.queue_cap) {
+        SlQueue e;
+        e.pair = pair;
+        e.kind = kind;
+        e.i = i;
+        e.j = j;
+        g.queue[s] = e;
+    } else {
+        atomicCAS(g.ctl + 1, 0u, (uint32_t)DERR_BAD_ITEM);
+    }
+    atomicAdd(&g.ctl[kind == 0 ? kCtlQueueRows : kCtlQueueCols], 1u);
+}
+
+// Exact column check: is row i the lowest-index argmin of column j among
+// the listed rows (all rows outside the list are provably farther)?
+SLM_DEV bool exact_col_winner(const float *A, const float *bj, const uint32_t *rows, uint32_t n, uint32_t i) {
+    float best = __int_as_float(0x7f800000);
+    uint32_t arg = 0xffffffffu;
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t r = rows[k];
+        const float d = sq_dist_spec(A + (size_t)r * kDesc, bj);
+        if (d < best || (d == best && r < arg)) {
+            best = d;
+            arg = r;
+        }
+    }
+    return arg == i;
+}
+
+__global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
+    const uint32_t p = blockIdx.x;
+    const PairMeta pm = g.pairs[p];
+    const SlPair sp = g.spairs[p];
+    const float kInf = __int_as_float(0x7f800000);
+    const float eps = sp.eps;
+    const double r2 = (double)g.ratio2;
+    const float *A = g.raw + (size_t)pm.a_row0 * kDesc;
+    const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
+    for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
+        const uint32_t ridx = sp.rbase + i;
+        uint32_t dec = kDecNone;
+        if (sp.unsafe) {
+            sl_enqueue(g, p, 0, i, 0);
+            dec = kDecPending;
+        } else if (g.rowthr[ridx] > -kInf) {
+            const uint32_t n = g.rowcnt[ridx];
+            if (n > kSlRowSlots) {
+                sl_enqueue(g, p, 0, i, 0);
+                dec = kDecPending;
+            } else {
+                const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
+                float a1 = kInf, a2 = kInf;
+                uint32_t j1 = 0xffffffffu;
+                for (uint32_t k = 0; k < n; ++k) {
+                    const uint2 e = S[k];
+                    const float v = __uint_as_float(e.y);
+                    if (v < a1 || (v == a1 && e.x < j1)) {
+                        a2 = a1;
+                        a1 = v;
+                        j1 = e.x;
+                    } else if (v < a2) {
+                        a2 = v;
+                    }
+                }
+                uint32_t cand = 0xffffffffu;
+                // S holds every column with d~ <= T, T >= (second smallest d~) + 2 eps,
+                // so the exact two smallest distances are rescored from S. With
+                // fewer than two finite entries the exact second best is infinite
+                // (matching.rs:205: no match).
+                const bool no_match = n < 2 || !(a2 < kInf) ||
+                                      (double)a1 - eps >= r2 * ((double)a2 + eps) * (1.0 + 1e-6);
+                const bool sure = !no_match && (double)a1 + eps < r2 * ((double)a2 - eps) * (1.0 - 1e-6) &&
+                                  (double)a2 - a1 > 2.0 * eps;
+                if (sure) {
+                    cand = j1;
+                } else if (!no_match) {
+                    // exact rescore of S (the reference's row update, matching.rs:182-187)
+                    float e1 = kInf, e2 = kInf;
+                    uint32_t ej = 0xffffffffu;
+                    float maxerr = 0.f;
+                    for (uint32_t k = 0; k < n; ++k) {
+                        const uint2 e = S[k];
+                        const float d = sq_dist_spec(A + (size_t)i * kDesc, B + (size_t)e.x * kDesc);
+                        maxerr = fmaxf(maxerr, fabsf(d - __uint_as_float(e.y)));
+                        if (d < e1 || (d == e1 && e.x < ej)) {
+                            e2 = e1;
+                            e1 = d;
+                            ej = e.x;
+                        } else if (d < e2) {
+                            e2 = d;
+                        }
+                    }
+                    atomicAdd(&g.ctl[kCtlRescored], 1u);
+                    if (maxerr == maxerr) atomicMax(&g.ctl[kCtlMaxErr], __float_as_uint(maxerr));
+                    if (ej != 0xffffffffu && e2 < kInf && !(e1 >= __fmul_rn(g.ratio2, e2))) cand = ej;
+                }
+                if (cand != 0xffffffffu) {
+                    if (!g.mutual) {
+                        dec = cand;
+                    } else {
+                        const uint32_t cidx = sp.cbase + cand;
+                        const uint32_t cn = g.colcnt[cidx];
+                        if (cn > kSlColSlots) {
+                            sl_enqueue(g, p, 1, i, cand);
+                            dec = kDecPending;
+                        } else {
+                            const uint32_t *C = g.colcand + (size_t)cidx * kSlColSlots;
+                            bool in = false;
+                            for (uint32_t k = 0; k < cn; ++k) in |= C[k] == i;
+                            if (in) {
+                                if (cn == 1) {
+                                    dec = cand;
+                                } else {
+                                    atomicAdd(&g.ctl[kCtlColRescored], 1u);
+                                    if (exact_col_winner(A, B + (size_t)cand * kDesc, C, cn, i)) dec = cand;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        g.rowdec[ridx] = dec;
+    }
+}
+
+// ------------------------------------------------------------- recompute
+
+// One warp per queued entry: exact scans in the reference's order and
+// tie rules (rows: matching.rs:182-187; columns: :188-203).
+__global__ void __launch_bounds__(256) sl_recompute_kernel(SlArgs g) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t qn = min(g.ctl[kCtlQueueLen], g.queue_cap);
+    const float kInf = __int_as_float(0x7f800000);
+    for (uint32_t e = gw; e < qn; e += nw) {
+        const SlQueue qe = g.queue[e];
+        const PairMeta pm = g.pairs[qe.pair];
+        const SlPair sp = g.spairs[qe.pair];
+        const float *A = g.raw + (size_t)pm.a_row0 * kDesc;
+        const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
+        uint32_t dec = kDecNone;
+        uint32_t col = qe.j;
+        bool check_col = qe.kind == 1;
+        if (qe.kind == 0) {
+            float d1 = kInf, d2 = kInf;
+            uint32_t j1 = 0xffffffffu;
+            for (uint32_t j = lane; j < pm.nb; j += 32) {
+                const float d = sq_dist_spec(A + (size_t)qe.i * kDesc, B + (size_t)j * kDesc);
+                if (d < d1) {
+                    d2 = d1;
+                    d1 = d;
+                    j1 = j;
+                } else if (d < d2) {
+                    d2 = d;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float o1 = __shfl_xor_sync(0xffffffffu, d1, o);
+                const float o2 = __shfl_xor_sync(0xffffffffu, d2, o);
+                const uint32_t oj = __shfl_xor_sync(0xffffffffu, j1, o);
+                const float n2 = fminf(fminf(d2, o2), fmaxf(d1, o1));
+                if (o1 < d1 || (o1 == d1 && oj < j1)) {
+                    d1 = o1;
+                    j1 = oj;
+                }
+                d2 = n2;
+            }
+            if (j1 != 0xffffffffu && d2 < kInf && !(d1 >= __fmul_rn(g.ratio2, d2))) {
+                if (g.mutual) {
+                    check_col = true;
+                    col = j1;
+                } else {
+                    dec = j1;
+                }
+            }
+        }
+        if (check_col) {
+            float bd = kInf;
+            uint32_t bi = 0xffffffffu;
+            for (uint32_t r = lane; r < pm.na; r += 32) {
+                const float d = sq_dist_spec(A + (size_t)r * kDesc, B + (size_t)col * kDesc);
+                if (d < bd) {
+                    bd = d;
+                    bi = r;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+                const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (od < bd || (od == bd && oi < bi)) {
+                    bd = od;
+                    bi = oi;
+                }
+            }
+            dec = bi == qe.i ? col : kDecNone;
+        }
+        if (lane == 0) g.rowdec[sp.rbase + qe.i] = dec;
+    }
+}
+
+// -------------------------------------------------------------- compact
+
+__global__ void __launch_bounds__(256) sl_compact_kernel(SlArgs g) {
+    __shared__ uint32_t warp_tot[8];
+    const uint32_t p = blockIdx.x;
+    const PairMeta pm = g.pairs[p];
+    const SlPair sp = g.spairs[p];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t base = 0;
+    for (uint32_t row0 = 0; row0 < pm.na; row0 += 256) {
+        const uint32_t i = row0 + tid;
+        uint32_t dec = kDecNone;
+        if (i < pm.na) dec = g.rowdec[sp.rbase + i];
+        if (dec == kDecPending) {
+            atomicCAS(g.ctl + 1, 0u, (uint32_t)DERR_BAD_ITEM);
+            dec = kDecNone;
+        }
+        const uint32_t flag = dec != kDecNone;
+        const uint32_t ballot = __ballot_sync(0xffffffffu, flag);
+        const uint32_t wpre = __popc(ballot & ((1u << lane) - 1u));
+        if (lane == 0) warp_tot[wid] = __popc(ballot);
+        __syncthreads();
+        uint32_t off = 0, tot = 0;
+        for (int w = 0; w < 8; ++w) {
+            off += (w < wid) ? warp_tot[w] : 0;
+            tot += warp_tot[w];
+        }
+        if (flag) g.slots[pm.slot_off + base + off + wpre] = make_uint2(i, dec);
+        base += tot;
+        __syncthreads();
+    }
+    if (tid == 0) g.counts[p] = base;
+}
+
+// ---------------------------------------------------------------- launch
+
+cudaError_t init_shortlist_kernels() {
+    cudaError_t e;
+    e = cudaFuncSetAttribute(sl_pass_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sl_smem_bytes<false>());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(sl_pass_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sl_smem_bytes<false>());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(sl_pass_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sl_smem_bytes<true>());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(sl_pass_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sl_smem_bytes<true>());
+}
+
+int shortlist_kernel_count() { return 6; }
+
+void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s) {
+    const int grid = (int)(a.n_items < (uint32_t)sms ? a.n_items : (uint32_t)sms);
+    if (a.fp8) {
+        if (grid) sl_pass_kernel<1, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+    } else {
+        if (grid) sl_pass_kernel<1, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
+    }
+    if (a.npairs) sl_mid_kernel<<<a.npairs, 256, 0, s>>>(a);
+    if (a.fp8) {
+        if (grid) sl_pass_kernel<2, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+    } else {
+        if (grid) sl_pass_kernel<2, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
+    }
+    if (a.npairs) sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
+    sl_recompute_kernel<<<2 * sms, 256, 0, s>>>(a);
+    if (a.npairs) sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
+}
+
+}  // namespace slm

@@ -19,6 +19,7 @@
 
 #include "slm.h"
 #include "slm_internal.h"
+#include "slm_shortlist.h"
 
 using namespace slm;
 
@@ -144,6 +145,11 @@ struct slm_store {
     std::vector<uint32_t> row0, n;
     uint64_t rows_used = 0;
     uint64_t version = 0;   // bumps when views are added or cleared
+    // Low-precision operand images for the shortlist path, rebuilt lazily
+    // when the views change (lowp_version != version) or the format changes.
+    int lowp_fp8 = -1;
+    uint64_t lowp_version = ~0ull;
+    DevBuf optiles, norms, qscale, vstats;
 };
 
 // ---------------------------------------------------------------------- plan
@@ -162,10 +168,18 @@ struct slm_plan {
     std::vector<uint64_t> slot_off;  // np + 1
     uint64_t n_parts = 0, n_cols = 0, n_slots = 0, distances = 0;
     DevBuf d_meta, d_items, d_parts, d_colbest, d_slots, d_counts, d_ctl, d_offsets, d_dense;
+    // shortlist path
+    std::vector<SlItem> sitems;
+    std::vector<SlPair> spairs;
+    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0;
+    DevBuf d_sitems, d_spairs, d_rowpart, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt, d_colcand,
+        d_rowdec, d_queue, d_dump;
+    bool dump = false;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel
     uint64_t kernels = 0;                      // kernels per launch
+    void *graph_optiles = nullptr;             // store buffer the captured graph reads
     bool launched = false;
     ~slm_plan() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -177,6 +191,7 @@ struct slm_plan {
 
 // Dense compaction of per-pair slots (device) into out + offsets.
 namespace slm {
+void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s);
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s);
 void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
                    uint32_t np, uint2 *dense, uint64_t cap, cudaStream_t s);
@@ -223,6 +238,86 @@ void plan_items(slm_plan *p) {
     });
 }
 
+// Shortlist plan: items of up to two 128-row a tiles against a range of
+// 128-column b tiles; per-row and per-column arrays padded to 128 entries per
+// pair so that every bulk copy starts on a 512-byte boundary.
+slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
+    slm_ctx *c = p->ctx;
+    uint64_t supers = 0;
+    for (uint32_t k = 0; k < p->np; ++k)
+        if (p->meta[k].nb) supers += (p->meta[k].na + 2 * kTile - 1) / (2 * kTile);
+    const uint64_t want = (uint64_t)std::max(1, c->sms) * (p->tune.items_per_sm ? p->tune.items_per_sm : 3);
+    uint32_t split = 1;
+    if (supers && supers < want) split = (uint32_t)((want + supers - 1) / supers);
+    p->sitems.clear();
+    p->spairs.assign(p->np, SlPair{});
+    uint64_t rb = 0, cb = 0, part = 0;
+    for (uint32_t k = 0; k < p->np; ++k) {
+        const PairMeta &m = p->meta[k];
+        SlPair &sp = p->spairs[k];
+        sp.rbase = (uint32_t)rb;
+        sp.cbase = (uint32_t)cb;
+        sp.view_a = pairs[k].i;
+        sp.view_b = pairs[k].j;
+        const uint32_t rt_n = (m.na + kTile - 1) / kTile, ct_n = (m.nb + kTile - 1) / kTile;
+        const uint32_t chunks = std::max(1u, std::min(split, ct_n));
+        sp.nchunk = chunks;
+        sp.part_base = (uint32_t)part;
+        if (m.na && m.nb) {
+            const uint32_t ns = (rt_n + 1) / 2;
+            for (uint32_t s2 = 0; s2 < ns; ++s2)
+                for (uint32_t ch = 0; ch < chunks; ++ch) {
+                    SlItem it{};
+                    it.pair = k;
+                    it.rt0 = 2 * s2;
+                    it.nat = std::min(2u, rt_n - 2 * s2);
+                    it.ct0 = (uint32_t)((uint64_t)ct_n * ch / chunks);
+                    it.ct1 = (uint32_t)((uint64_t)ct_n * (ch + 1) / chunks);
+                    it.part = (uint32_t)(part + s2 * chunks + ch);
+                    if (it.ct1 > it.ct0) p->sitems.push_back(it);
+                }
+            part += (uint64_t)ns * chunks;
+        }
+        rb += pad_rows(m.na);
+        cb += pad_rows(m.nb);
+    }
+    if (rb >= (1ull << 32) || cb >= (1ull << 32)) return fail(SLM_CAPACITY, "batch too large for one plan");
+    std::stable_sort(p->sitems.begin(), p->sitems.end(), [](const SlItem &x, const SlItem &y) {
+        return (uint64_t)(x.ct1 - x.ct0) * x.nat > (uint64_t)(y.ct1 - y.ct0) * y.nat;
+    });
+    p->rows_pad = rb + 2 * kTile;
+    p->cols_pad = cb + kTile;
+    p->sl_parts = std::max<uint64_t>(part, 1);
+    p->queue_cap = std::max<uint64_t>(p->n_slots, 1) + 64;
+    SLM_TRY(p->d_sitems.ensure(c, sizeof(SlItem) * std::max<size_t>(1, p->sitems.size())));
+    SLM_TRY(p->d_spairs.ensure(c, sizeof(SlPair) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_rowpart.ensure(c, sizeof(float2) * 256 * p->sl_parts));
+    SLM_TRY(p->d_colmin.ensure(c, sizeof(uint32_t) * p->cols_pad));
+    SLM_TRY(p->d_rowthr.ensure(c, sizeof(float) * p->rows_pad));
+    SLM_TRY(p->d_colthr.ensure(c, sizeof(float) * p->cols_pad));
+    SLM_TRY(p->d_rowcnt.ensure(c, sizeof(uint32_t) * p->rows_pad));
+    SLM_TRY(p->d_rowcand.ensure(c, sizeof(uint2) * kSlRowSlots * p->rows_pad));
+    SLM_TRY(p->d_colcnt.ensure(c, sizeof(uint32_t) * p->cols_pad));
+    SLM_TRY(p->d_colcand.ensure(c, sizeof(uint32_t) * kSlColSlots * p->cols_pad));
+    SLM_TRY(p->d_rowdec.ensure(c, sizeof(uint32_t) * p->rows_pad));
+    SLM_TRY(p->d_queue.ensure(c, sizeof(SlQueue) * p->queue_cap));
+    if (p->dump && p->np) SLM_TRY(p->d_dump.ensure(c, sizeof(float) * std::max<uint64_t>(1, (uint64_t)p->meta[0].na * p->meta[0].nb)));
+    SLM_TRY(p->d_meta.ensure(c, sizeof(PairMeta) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_slots.ensure(c, sizeof(uint2) * std::max<uint64_t>(1, p->n_slots)));
+    SLM_TRY(p->d_counts.ensure(c, sizeof(uint32_t) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_ctl.ensure(c, 64));
+    SLM_TRY(p->d_offsets.ensure(c, sizeof(uint64_t) * (p->np + 1) * 2));
+    SLM_TRY(p->d_dense.ensure(c, sizeof(uint2) * std::max<uint64_t>(1, p->n_slots)));
+    cudaStream_t s = p->stream;
+    SLM_CU(cudaMemcpyAsync(p->d_meta.p, p->meta.data(), sizeof(PairMeta) * p->np, cudaMemcpyHostToDevice, s));
+    SLM_CU(cudaMemcpyAsync(p->d_offsets.as<uint64_t>() + (p->np + 1), p->slot_off.data(),
+                           sizeof(uint64_t) * (p->np + 1), cudaMemcpyHostToDevice, s));
+    SLM_CU(cudaMemcpyAsync(p->d_spairs.p, p->spairs.data(), sizeof(SlPair) * p->np, cudaMemcpyHostToDevice, s));
+    SLM_CU(cudaMemcpyAsync(p->d_sitems.p, p->sitems.data(), sizeof(SlItem) * p->sitems.size(),
+                           cudaMemcpyHostToDevice, s));
+    return SLM_OK;
+}
+
 slm_status plan_build(slm_plan *p, const slm_pair *pairs) {
     slm_store *st = p->st;
     p->meta.resize(p->np);
@@ -248,6 +343,7 @@ slm_status plan_build(slm_plan *p, const slm_pair *pairs) {
     p->n_cols = col;
     p->n_slots = slot;
     p->distances = dist;
+    if (p->prec != SLM_PREC_FP32) return plan_build_shortlist(p, pairs);
     plan_items(p);
     slm_ctx *c = p->ctx;
     SLM_TRY(p->d_meta.ensure(c, sizeof(PairMeta) * std::max<size_t>(1, p->np)));
@@ -272,6 +368,51 @@ slm_status plan_build(slm_plan *p, const slm_pair *pairs) {
 slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
     uint32_t *ctl = p->d_ctl.as<uint32_t>();  // [0] work counter, [1] error word, [2..] shortlist counters
     SLM_CU(cudaMemsetAsync(ctl, 0, 64, s));
+    if (p->prec != SLM_PREC_FP32) {
+        slm_store *st = p->st;
+        launch_fill_u32(p->d_colmin.as<uint32_t>(), p->cols_pad, 0xff800000u, s);  // encodes +inf
+        SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, sizeof(uint32_t) * p->rows_pad, s));
+        SLM_CU(cudaMemsetAsync(p->d_colcnt.p, 0, sizeof(uint32_t) * p->cols_pad, s));
+        SlArgs a{};
+        a.optiles = st->optiles.as<uint8_t>();
+        a.norms = st->norms.as<float>();
+        a.raw = st->raw.as<float>();
+        a.qscale = p->prec == SLM_PREC_FP8 ? st->qscale.as<float>() : nullptr;
+        a.vstats = st->vstats.as<ViewStat>();
+        a.pairs = p->d_meta.as<PairMeta>();
+        a.spairs = p->d_spairs.as<SlPair>();
+        a.npairs = p->np;
+        a.items = p->d_sitems.as<SlItem>();
+        a.n_items = (uint32_t)p->sitems.size();
+        a.rowpart = p->d_rowpart.as<float2>();
+        a.colmin = p->d_colmin.as<uint32_t>();
+        a.rowthr = p->d_rowthr.as<float>();
+        a.colthr = p->d_colthr.as<float>();
+        a.rowcnt = p->d_rowcnt.as<uint32_t>();
+        a.rowcand = p->d_rowcand.as<uint2>();
+        a.colcnt = p->d_colcnt.as<uint32_t>();
+        a.colcand = p->d_colcand.as<uint32_t>();
+        a.rowdec = p->d_rowdec.as<uint32_t>();
+        a.queue = p->d_queue.as<SlQueue>();
+        a.queue_cap = (uint32_t)p->queue_cap;
+        a.ctl = ctl;
+        a.ratio2 = p->ratio * p->ratio;
+        a.mutual = p->mutual;
+        a.fp8 = p->prec == SLM_PREC_FP8;
+        a.dump = p->dump ? p->d_dump.as<float>() : nullptr;
+        a.slots = p->d_slots.as<uint2>();
+        a.counts = p->d_counts.as<uint32_t>();
+        SLM_CU(cudaEventRecordWithFlags(p->ev0, s, cudaEventRecordExternal));
+        launch_shortlist(a, p->ctx->sms, s);
+        SLM_CU(cudaEventRecordWithFlags(p->ev1, s, cudaEventRecordExternal));
+        p->kernels = 1 + (uint64_t)shortlist_kernel_count() + 2;
+        uint64_t *offsets = p->d_offsets.as<uint64_t>();
+        launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
+        launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
+                      p->d_dense.as<uint2>(), p->n_slots, s);
+        SLM_CU(cudaGetLastError());
+        return SLM_OK;
+    }
     if (p->mutual) launch_fill_u64(p->d_colbest.as<unsigned long long>(), p->n_cols, ~0ull, s);
     const float ratio2 = p->ratio * p->ratio;
     {
@@ -408,6 +549,16 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
     st->distances = p->distances;
     st->matches = matches;
     st->kernel_launches = p->kernels;
+    if (p->prec != SLM_PREC_FP32 && p->launched) {
+        uint32_t w[16];
+        SLM_CU(cudaMemcpy(w, p->d_ctl.p, sizeof(w), cudaMemcpyDeviceToHost));
+        st->rows_rescored = w[kCtlRescored];
+        st->rows_recomputed = w[kCtlQueueRows];
+        st->cols_recomputed = (uint64_t)w[kCtlQueueCols] + w[kCtlColRescored];
+        float e;
+        std::memcpy(&e, &w[kCtlMaxErr], sizeof(e));
+        st->max_abs_err = e;
+    }
     if (p->launched && p->ev0 && p->ev1) {
         float ms = 0;
         if (cudaEventElapsedTime(&ms, p->ev0, p->ev1) == cudaSuccess) st->kernel_ms = ms;
@@ -442,6 +593,7 @@ extern "C" slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out) {
     SLM_CU(cudaSetDevice(dev));
     {
         cudaError_t ke = init_exact_kernels();
+        if (ke == cudaSuccess) ke = init_shortlist_kernels();
         if (ke != cudaSuccess) {
             cudaGetLastError();
             return fail(SLM_NO_DEVICE, std::string("kernels do not load on this device: ") + cudaGetErrorString(ke));
@@ -548,6 +700,28 @@ extern "C" uint32_t slm_store_num_views(slm_store *st) { return st ? (uint32_t)s
 
 namespace {
 
+// Build (or rebuild) the store's low-precision operand images.
+slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
+    if (st->lowp_version == st->version && st->lowp_fp8 == (int)fp8) return SLM_OK;
+    slm_ctx *c = st->ctx;
+    const uint64_t tiles = std::max<uint64_t>(st->max_rows / kTile, 1);
+    const size_t tb = fp8 ? kFp8TileBytes : kBf16TileBytes;
+    SLM_TRY(st->optiles.ensure(c, tiles * tb));
+    SLM_TRY(st->norms.ensure(c, tiles * kTile * sizeof(float)));
+    if (fp8) SLM_TRY(st->qscale.ensure(c, tiles * kTile * sizeof(float)));
+    const size_t nv = std::max<size_t>(st->row0.size(), 1);
+    SLM_TRY(st->vstats.ensure(c, nv * sizeof(ViewStat)));
+    SLM_CU(cudaMemsetAsync(st->vstats.p, 0, nv * sizeof(ViewStat), s));
+    for (size_t v = 0; v < st->row0.size(); ++v)
+        launch_pack_lowp(st->raw.as<float>(), st->row0[v], st->n[v], (uint32_t)v, fp8 ? 1 : 0,
+                         st->optiles.as<uint8_t>(), st->norms.as<float>(), st->qscale.as<float>(),
+                         st->vstats.as<ViewStat>(), s);
+    SLM_CU(cudaGetLastError());
+    st->lowp_version = st->version;
+    st->lowp_fp8 = fp8 ? 1 : 0;
+    return SLM_OK;
+}
+
 slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                      int mutual, slm_precision prec, const slm_tune *tune, cudaStream_t stream) {
     p->ctx = c;
@@ -568,10 +742,22 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
         p->graph = nullptr;
     }
     p->launched = false;
+    p->dump = p->tune.variant == 2 && prec != SLM_PREC_FP32;
+    if (prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
     return plan_build(p, pairs);
 }
 
 slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
+    if (p->prec != SLM_PREC_FP32) {
+        const uint64_t v = p->st->lowp_version;
+        SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
+        // a rebuilt operand image may live in new buffers: capture again
+        if (v != p->st->lowp_version && p->exec && p->st->optiles.p != p->graph_optiles) {
+            cudaGraphExecDestroy(p->exec);
+            p->exec = nullptr;
+        }
+        p->graph_optiles = p->st->optiles.p;
+    }
     if (!p->ev0) SLM_CU(cudaEventCreate(&p->ev0));
     if (!p->ev1) SLM_CU(cudaEventCreate(&p->ev1));
     if (use_graph) {
@@ -871,4 +1057,14 @@ extern "C" slm_status slm_scheduled_pairs(const uint64_t *views, uint32_t nv, co
             }),
             v.end());
     return emit_pairs(v, out, cap, n_out);
+}
+
+extern "C" slm_status slm_plan_debug_dump(slm_plan *p, float *out, uint64_t cap) {
+    if (!p || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (!p->dump || !p->np) return fail(SLM_INVALID_ARG, "plan was not created with the dump variant");
+    const uint64_t n = (uint64_t)p->meta[0].na * p->meta[0].nb;
+    if (n > cap) return fail(SLM_CAPACITY, "need " + std::to_string(n) + " floats");
+    SLM_CU(cudaStreamSynchronize(p->stream));
+    if (n) SLM_CU(cudaMemcpy(out, p->d_dump.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return SLM_OK;
 }

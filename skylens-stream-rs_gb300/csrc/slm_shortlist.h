@@ -1,0 +1,124 @@
+// slm_shortlist.h — the low-precision shortlist path (BF16 / FP8 tcgen05).
+//
+// ratio_match's decision (crates/core/src/matching.rs:167-215) depends only on
+// a few distances per row: the two smallest, and, for the mutual check, the
+// smallest in the chosen column. The shortlist path finds them with tensor-core
+// distances d~ = |a|^2 + |b|^2 - 2 a.b whose error against the exact f32
+// distance d is bounded per image pair by eps (see shortlist_eps), then
+// settles every decision the bound cannot certify with exact spec-order FP32
+// arithmetic, so the match list is the reference's bit for bit.
+//
+//   pass 1  (tcgen05)  per row: m1 = min d~ and m2' = second smallest of the
+//                      per-32-column minima (an upper bound of the second
+//                      smallest d~); per column: c1 = min d~.
+//   mid                per row: threshold T = m2' + 2 eps, or "certain no
+//                      match" when m1 - eps >= r^2 (m2' + eps); per column:
+//                      threshold c1 + 2 eps.
+//   pass 2  (tcgen05)  recomputes d~ and appends (j, d~) with d~ <= T to the
+//                      row's candidate list S, and i with d~ <= c1 + 2 eps to
+//                      the column's list C.
+//   finalize           per row, from S: certain outcomes from the bounds, else
+//                      an exact rescore of S; the mutual check from C (a row
+//                      outside C loses, a sole member wins, else exact rescore
+//                      of C). Lists that overflowed go to the queue.
+//   recompute          exact FP32 row / column scans for queued rows.
+#pragma once
+#include <cstdint>
+
+#include "slm_internal.h"
+
+namespace slm {
+
+constexpr int kSlRowSlots = 16;    // S capacity per row
+constexpr int kSlColSlots = 8;     // C capacity per column
+constexpr int kSlStages = 4;       // b-tile ring depth
+constexpr int kSlThreads = 320;    // producer, MMA, 8 epilogue warps
+
+// Operand tile sizes per 128 descriptors.
+constexpr uint32_t kBf16TileBytes = 128 * 128 * 2;  // 32 KiB, 128B-swizzled, K-major
+constexpr uint32_t kFp8TileBytes = 128 * 128;       // 16 KiB
+
+// Per view, from the pack kernel: float bits of non-negative maxima
+// (atomicMax on the bit pattern orders them), and a non-finite flag.
+struct ViewStat {
+    uint32_t nmax;   // max |a|
+    uint32_t rho;    // max |a - q(a)| (q: the low-precision rounding, scale removed)
+    uint32_t nqmax;  // max |q(a)|
+    uint32_t bad;    // nonzero: some component is not finite
+};
+
+// Work item: rows [rt0*128, rt0*128 + nat*128) of a pair (nat 1 or 2 tiles)
+// against column tiles [ct0, ct1) of b.
+struct SlItem {
+    uint32_t pair, rt0, nat, ct0, ct1, part;
+    uint32_t pad[2];
+};
+
+// Per-pair extras of the shortlist path.
+struct SlPair {
+    uint32_t rbase;    // first entry in per-row arrays (multiple of 128)
+    uint32_t cbase;    // first entry in per-column arrays (multiple of 128)
+    uint32_t part_base, nchunk;  // pass-1 row partials: (part_base + (rt0/2)*nchunk + c) * 256 + r
+    uint32_t view_a, view_b;
+    float eps;         // written by the mid kernel
+    uint32_t unsafe;   // written by the mid kernel: settle every row exactly
+};
+
+// Row decision codes (per pair row).
+constexpr uint32_t kDecNone = 0xffffffffu;
+constexpr uint32_t kDecPending = 0xfffffffeu;
+
+// Queue entry for the recompute kernel.
+struct SlQueue {
+    uint32_t pair, kind, i, j;  // kind 0: exact row scan; 1: exact column check of (i, j)
+};
+
+// Counters in the plan's control block (u32 words after work/error).
+enum : int { kCtlRescored = 2, kCtlQueueRows = 3, kCtlQueueCols = 4, kCtlMaxErr = 5, kCtlQueueLen = 6,
+             kCtlColRescored = 7 };
+
+struct SlArgs {
+    const uint8_t *optiles;      // operand tiles by store row / 128
+    const float *norms;          // squared f32 norms by store row
+    const float *raw;            // row-major f32 descriptors by store row
+    const float *qscale;         // FP8: per-row inverse scale (nullptr for BF16)
+    const ViewStat *vstats;
+    const PairMeta *pairs;
+    SlPair *spairs;
+    uint32_t npairs;
+    const SlItem *items;
+    uint32_t n_items;
+    float2 *rowpart;             // pass 1
+    uint32_t *colmin;            // pass 1: order-preserving encoding of c1
+    float *rowthr;               // mid -> pass 2
+    float *colthr;               // mid -> pass 2
+    uint32_t *rowcnt;            // pass 2
+    uint2 *rowcand;              // (j, bits(d~))
+    uint32_t *colcnt;
+    uint32_t *colcand;           // i
+    uint32_t *rowdec;            // finalize / recompute
+    SlQueue *queue;
+    uint32_t queue_cap;
+    uint32_t *ctl;               // [1] error word, counters at kCtl*
+    float ratio2;
+    int mutual;
+    int fp8;
+    float *dump;                 // debug: d~ of pair 0, [na][nb] (nullptr: off)
+    uint2 *slots;
+    uint32_t *counts;
+};
+
+// Store-side builders.
+void launch_pack_lowp(const float *raw, uint32_t row0, uint32_t n, uint32_t view, int fp8, uint8_t *optiles,
+                      float *norms, float *qscale, ViewStat *vstats, cudaStream_t s);
+
+// Kernel image / attribute set-up (outside stream capture).
+cudaError_t init_shortlist_kernels();
+
+// The pipeline of one shortlist launch (after counters are cleared).
+void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s);
+
+// Number of kernels launch_shortlist enqueues.
+int shortlist_kernel_count();
+
+}  // namespace slm

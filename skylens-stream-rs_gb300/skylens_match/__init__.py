@@ -6,6 +6,9 @@ kernels in libslm; this package is its Python host interface.
 """
 from ._lib import SlmError, load, library_path
 from .buildlib import build
+
+# Precisions libslm implements (all bit-exact against the reference).
+BUILT_PRECISIONS = ("fp32", "bf16", "fp8")
 from .matching import (CAM_FRONT, CAM_LEFT, CAM_RIGHT, PAIR_CROSS, PAIR_POW2_MAX, PAIR_TEMPORAL, USIZE_MAX,
                        BatchPlan, DescriptorStore, Matcher, PairSchedule, candidate_pairs, default_matcher,
                        match_pairs, ratio_match, scheduled_pairs)

@@ -83,6 +83,7 @@ SIGNATURES = {
     "slm_plan_device_results": (c_int, [ctypes.c_void_p, P(ctypes.c_void_p), P(ctypes.c_void_p),
                                         P(ctypes.c_void_p)]),
     "slm_plan_bytes": (c_u64, [ctypes.c_void_p]),
+    "slm_plan_debug_dump": (c_int, [ctypes.c_void_p, P(c_f32), c_u64]),
     "slm_match_batch": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int,
                                 P(SlmPair), c_u64, P(c_u64), P(SlmStats)]),
 }

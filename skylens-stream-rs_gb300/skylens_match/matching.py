@@ -235,6 +235,13 @@ class BatchPlan:
     def nbytes(self) -> int:
         return int(self._L.slm_plan_bytes(self._h))
 
+    def debug_dump(self, na: int, nb: int) -> np.ndarray:
+        """Tensor-core distance estimates of the first pair (plans made with variant=2)."""
+        out = np.empty((na, nb), np.float32)
+        check(self._L.slm_plan_debug_dump(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), out.size),
+              "slm_plan_debug_dump")
+        return out
+
     def close(self) -> None:
         if self._h:
             self._L.slm_plan_destroy(self._h)

@@ -1,6 +1,9 @@
-"""GPU: the plain FP32 kernel against the oracle and the reference's tests.
+"""GPU: every precision (plain FP32, BF16 and FP8 shortlists) against the
+oracle and the reference's tests.
 
-Every comparison is exact equality of match lists (bit-exact integer output).
+Every comparison is exact equality of match lists (bit-exact integer output):
+the shortlist paths settle every decision their error bound cannot certify
+with exact FP32 arithmetic, so they too must equal the reference.
 """
 import threading
 
@@ -13,19 +16,23 @@ import skylens_match as sm
 from skylens_match import synth
 
 pytestmark = pytest.mark.gpu
-PREC = "fp32"
 
 
-def rm_of(matcher, prec=PREC):
+@pytest.fixture(params=["fp32", "bf16", "fp8"])
+def prec(request):
+    return request.param
+
+
+def rm_of(matcher, prec):
     return lambda a, b, ratio, mutual: matcher.ratio_match(a, b, ratio, mutual, prec)
 
 
 @pytest.mark.parametrize("case", refcases.ALL, ids=lambda f: f.__name__)
-def test_reference_case(matcher, case):
-    case(rm_of(matcher))
+def test_reference_case(matcher, case, prec):
+    case(rm_of(matcher, prec))
 
 
-def check(matcher, a, b, ratio=0.8, mutual=True, prec=PREC, threads=8):
+def check(matcher, a, b, ratio=0.8, mutual=True, prec="fp32", threads=8):
     got = matcher.ratio_match_np(a, b, ratio, mutual, prec)
     ref = O.ratio_match_np(a, b, ratio, mutual, threads=threads)
     assert got.shape == ref.shape and np.array_equal(got, ref), (
@@ -34,39 +41,39 @@ def check(matcher, a, b, ratio=0.8, mutual=True, prec=PREC, threads=8):
     return got
 
 
-def test_pair_800(matcher):
+def test_pair_800(matcher, prec):
     a, b = synth.pair_800(0)
     for mutual in (True, False):
-        check(matcher, a, b, 0.8, mutual)
+        check(matcher, a, b, 0.8, mutual, prec)
 
 
-def test_pair_8192_full_size(matcher):
+def test_pair_8192_full_size(matcher, prec):
     a, b = synth.pair_large(8192, 0.5, 0.05, seed=2)
-    m = check(matcher, a, b, 0.8, True, threads=16)
+    m = check(matcher, a, b, 0.8, True, prec, threads=16)
     assert len(m) > 1000
 
 
 @pytest.mark.parametrize("na,nb", [(1, 2), (2, 1), (1, 1), (63, 64), (64, 63), (65, 129), (127, 128), (128, 127),
                                    (129, 257), (255, 1), (257, 300), (1000, 3), (3, 1000), (600, 900)])
-def test_ragged_sizes(matcher, na, nb):
+def test_ragged_sizes(matcher, na, nb, prec):
     rng = np.random.Generator(np.random.PCG64(na * 1000 + nb))
     a = synth.sift_like(rng, na)
     k = min(na, nb) // 2
     b = np.concatenate([synth.noisy_copy(rng, a[:k], 0.03), synth.sift_like(rng, nb - k)])
     for ratio in (0.8, 1.0, 0.0, 1.5):
         for mutual in (True, False):
-            check(matcher, a, b, ratio, mutual)
+            check(matcher, a, b, ratio, mutual, prec)
 
 
-def test_empty_inputs(matcher):
+def test_empty_inputs(matcher, prec):
     a, _ = O.match_fixture(9, 10, 0)
     e = np.zeros((0, 128), np.float32)
-    assert matcher.ratio_match(a, e, 0.8, True) == []
-    assert matcher.ratio_match(e, a, 0.8, True) == []
-    assert matcher.ratio_match(e, e, 0.8, False) == []
+    assert matcher.ratio_match(a, e, 0.8, True, prec) == []
+    assert matcher.ratio_match(e, a, 0.8, True, prec) == []
+    assert matcher.ratio_match(e, e, 0.8, False, prec) == []
 
 
-def test_exact_duplicates_and_ties(matcher):
+def test_exact_duplicates_and_ties(matcher, prec):
     """Duplicate rows of b tie at the row minimum (d1 == d2: no match); duplicate
     rows of a tie at a column minimum (the lower i wins), across tile borders."""
     rng = np.random.Generator(np.random.PCG64(7))
@@ -78,11 +85,11 @@ def test_exact_duplicates_and_ties(matcher):
     a[260] = a[5]
     a[299] = a[129]
     for mutual in (True, False):
-        check(matcher, a, b, 0.8, mutual)
-        check(matcher, b, a, 0.8, mutual)
+        check(matcher, a, b, 0.8, mutual, prec)
+        check(matcher, b, a, 0.8, mutual, prec)
 
 
-def test_nan_and_unnormalised_inputs(matcher):
+def test_nan_and_unnormalised_inputs(matcher, prec):
     rng = np.random.Generator(np.random.PCG64(8))
     a = synth.sift_like(rng, 200) * 3.0
     b = np.concatenate([synth.noisy_copy(rng, a[:100] / 3.0, 0.03), synth.sift_like(rng, 150)]) * 0.5
@@ -91,10 +98,10 @@ def test_nan_and_unnormalised_inputs(matcher):
     b[12] = np.inf
     a[20] = 0.0
     for mutual in (True, False):
-        check(matcher, a.astype(np.float32), b.astype(np.float32), 0.8, mutual)
+        check(matcher, a.astype(np.float32), b.astype(np.float32), 0.8, mutual, prec)
 
 
-def test_concurrent_callers(matcher):
+def test_concurrent_callers(matcher, prec):
     """ratio_match is called from many rayon workers at once (pipeline.rs:487-492)."""
     z = synth.zone(positions=6, n_range=(200, 700), seed=11)
     pairs = [tuple(map(int, p)) for p in z.pairs[:24]]
@@ -104,7 +111,7 @@ def test_concurrent_callers(matcher):
     def worker(chunk):
         try:
             for p in chunk:
-                got[p] = matcher.ratio_match_np(z.view(p[0]), z.view(p[1]), 0.8, True, PREC)
+                got[p] = matcher.ratio_match_np(z.view(p[0]), z.view(p[1]), 0.8, True, prec)
         except Exception as e:  # surfaced below
             errs.append(e)
 
@@ -134,18 +141,18 @@ def zone_check(matcher, z, prec, pairs=None, threads=16):
     return stats
 
 
-def test_small_zone_batch(matcher):
+def test_small_zone_batch(matcher, prec):
     z = synth.zone(positions=10, n_range=(100, 900), seed=5)
-    zone_check(matcher, z, PREC)
+    zone_check(matcher, z, prec)
 
 
-def test_batch_with_repeated_and_reversed_pairs(matcher):
+def test_batch_with_repeated_and_reversed_pairs(matcher, prec):
     z = synth.zone(positions=4, n_range=(50, 400), seed=6)
     pairs = np.array([[0, 1], [1, 0], [0, 1], [2, 2], [3, 5], [5, 3]], np.uint32)
-    zone_check(matcher, z, PREC, pairs)
+    zone_check(matcher, z, prec, pairs)
 
 
-def test_device_entry_point(matcher):
+def test_device_entry_point(matcher, prec):
     torch = pytest.importorskip("torch")
     a, b = synth.pair_800(1)
     da = torch.from_numpy(a).cuda()
@@ -153,7 +160,7 @@ def test_device_entry_point(matcher):
     out = torch.zeros((800, 2), dtype=torch.int32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()  # inputs are ready before the library stream reads them
-    matcher.ratio_match_device(da.data_ptr(), 800, db.data_ptr(), 800, 0.8, True, PREC, out.data_ptr(), 800,
+    matcher.ratio_match_device(da.data_ptr(), 800, db.data_ptr(), 800, 0.8, True, prec, out.data_ptr(), 800,
                                cnt.data_ptr())
     torch.cuda.ExternalStream(matcher.stream).synchronize()
     n = int(cnt.item())
