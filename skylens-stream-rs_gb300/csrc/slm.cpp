@@ -49,6 +49,16 @@ slm_status fail(slm_status s, const std::string &msg) {
 
 uint64_t pad_rows(uint64_t n) { return (n + kTile - 1) / kTile * kTile; }
 
+// Timing events: under stream capture they must become event-record nodes
+// (cudaEventRecordExternal); outside capture the flag is not allowed.
+cudaError_t record_event(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t r = cudaStreamIsCapturing(s, &cs);
+    if (r != cudaSuccess) return r;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal)
+                                               : cudaEventRecord(e, s);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ context
@@ -402,9 +412,9 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.dump = p->dump ? p->d_dump.as<float>() : nullptr;
         a.slots = p->d_slots.as<uint2>();
         a.counts = p->d_counts.as<uint32_t>();
-        SLM_CU(cudaEventRecordWithFlags(p->ev0, s, cudaEventRecordExternal));
+        SLM_CU(record_event(p->ev0, s));
         launch_shortlist(a, p->ctx->sms, s);
-        SLM_CU(cudaEventRecordWithFlags(p->ev1, s, cudaEventRecordExternal));
+        SLM_CU(record_event(p->ev1, s));
         p->kernels = 1 + (uint64_t)shortlist_kernel_count() + 2;
         uint64_t *offsets = p->d_offsets.as<uint64_t>();
         launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
@@ -428,9 +438,9 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.mutual = p->mutual;
         a.x2 = p->tune.variant == 1 ? 0 : 1;
         // External records so that the events become timing nodes under graph capture.
-        SLM_CU(cudaEventRecordWithFlags(p->ev0, s, cudaEventRecordExternal));
+        SLM_CU(record_event(p->ev0, s));
         if (a.n_items) launch_exact(a, std::min<int>(p->ctx->sms, (int)a.n_items), s);
-        SLM_CU(cudaEventRecordWithFlags(p->ev1, s, cudaEventRecordExternal));
+        SLM_CU(record_event(p->ev1, s));
         p->kernels = (p->mutual ? 1 : 0) + (a.n_items ? 1 : 0) + (p->np ? 1 : 0) + 1 + (p->np ? 1 : 0);
         FinalizeArgs f{};
         f.pairs = p->d_meta.as<PairMeta>();
