@@ -158,7 +158,10 @@ SLM_DEV void tile_distances(const float *__restrict__ sa, const float *__restric
 #pragma unroll
             for (int c = 0; c < 8; ++c) d[r][c] = s[r][c];
     } else {
-        // Packed pairs of columns (c, c+1): {a_r, a_r} - {b_c, b_c+1}.
+        // Packed pairs of columns (c, c+1): {a_r, a_r} - {b_c, b_c+1}. A packed
+        // multiply followed by a packed add is contracted to a packed FMA by the
+        // code generator (measured: 25 % of distances off by an ulp), so the
+        // squares are scalar IEEE multiplies.
         u64 s[8][4];
 #pragma unroll
         for (int r = 0; r < 8; ++r)
@@ -182,8 +185,10 @@ SLM_DEV void tile_distances(const float *__restrict__ sa, const float *__restric
                     const u64 ar = f2_pack(av[r], av[r]);
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
+                        // packed sub and add, scalar multiplies: the compiler must not
+                        // see a packed multiply feeding a packed add (it would fuse them)
                         const u64 t = f2_sub(ar, bv[c]);
-                        const u64 tt = f2_mul(t, t);
+                        const u64 tt = f2_pack(__fmul_rn(f2_lo(t), f2_lo(t)), __fmul_rn(f2_hi(t), f2_hi(t)));
                         acc[r][c] = (c16 == 0) ? tt : f2_add(acc[r][c], tt);
                     }
                 }

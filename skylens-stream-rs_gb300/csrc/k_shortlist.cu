@@ -408,6 +408,8 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_empty);
             float m1 = kInf, m2 = kInf;
+            const bool own_row = sp.nchunk == 1;
+            uint32_t ncand = 0;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
                 if (!sl_wait(&S.b_full[st], sph, abort_flag, err) || !sl_wait(&S.t_full[tb], tph, abort_flag, err)) {
@@ -479,13 +481,13 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 const float cm = min32(d);
                                 if (cm <= thr_i) {
                                     const uint32_t ridx = sp.rbase + i;
+                                    uint2 *dst = g.rowcand + (size_t)ridx * kSlRowSlots;
 #pragma unroll
                                     for (int k = 0; k < 32; ++k) {
                                         if (d[k] <= thr_i) {
-                                            const uint32_t s = atomicAdd(&g.rowcnt[ridx], 1u);
-                                            if (s < kSlRowSlots)
-                                                g.rowcand[(size_t)ridx * kSlRowSlots + s] =
-                                                    make_uint2(j0 + k, __float_as_uint(d[k]));
+                                            // one item owns the whole row unless its columns are split
+                                            const uint32_t s = own_row ? ncand++ : atomicAdd(&g.rowcnt[ridx], 1u);
+                                            if (s < kSlRowSlots) dst[s] = make_uint2(j0 + k, __float_as_uint(d[k]));
                                         }
                                     }
                                 }
@@ -504,13 +506,8 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 const float xm = min32(x);
                                 if (xm <= 0.f) {
 #pragma unroll
-                                    for (int k = 0; k < 32; ++k) {
-                                        if (x[k] <= 0.f) {
-                                            const uint32_t cidx = sp.cbase + j0 + k;
-                                            const uint32_t s = atomicAdd(&g.colcnt[cidx], 1u);
-                                            if (s < kSlColSlots) g.colcand[(size_t)cidx * kSlColSlots + s] = i;
-                                        }
-                                    }
+                                    for (int k = 0; k < 32; ++k)
+                                        if (x[k] <= 0.f) atomicAdd(&g.colcnt[sp.cbase + j0 + k], 1u);  // no return: a reduction
                                 }
                             }
                         }
@@ -546,6 +543,8 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             if (!ok) break;
             if constexpr (PASS == 1) {
                 if (active) g.rowpart[(size_t)item.part * 256 + r] = make_float2(m1, m2);
+            } else {
+                if (own_row && rvalid && thr_i > -kInf) g.rowcnt[sp.rbase + i] = ncand;
             }
         }
     }
@@ -621,37 +620,39 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
 
 // ------------------------------------------------------------- finalize
 
-SLM_DEV void sl_enqueue(const SlArgs &g, uint32_t pair, uint32_t kind, uint32_t i, uint32_t j) {
-    const uint32_t s = atomicAdd(&g.ctl[kCtlQueueLen], 1u);
-    if (s < g.queue_cap) {
+SLM_DEV void sl_push(SlQueue *q, uint32_t *len, uint32_t cap, uint32_t *err, uint32_t pair, uint32_t kind, uint32_t i,
+                     uint32_t j) {
+    const uint32_t s = atomicAdd(len, 1u);
+    if (s < cap) {
         SlQueue e;
         e.pair = pair;
         e.kind = kind;
         e.i = i;
         e.j = j;
-        g.queue[s] = e;
+        q[s] = e;
     } else {
-        atomicCAS(g.ctl + 1, 0u, (uint32_t)DERR_BAD_ITEM);
+        atomicCAS(err, 0u, (uint32_t)DERR_BAD_ITEM);
     }
+}
+
+SLM_DEV void push_scan(const SlArgs &g, uint32_t pair, uint32_t kind, uint32_t i, uint32_t j) {
+    sl_push(g.queue, &g.ctl[kCtlScanLen], g.queue_cap, g.ctl + 1, pair, kind, i, j);
     atomicAdd(&g.ctl[kind == 0 ? kCtlQueueRows : kCtlQueueCols], 1u);
 }
 
-// Exact column check: is row i the lowest-index argmin of column j among
-// the listed rows (all rows outside the list are provably farther)?
-SLM_DEV bool exact_col_winner(const float *A, const float *bj, const uint32_t *rows, uint32_t n, uint32_t i) {
-    float best = __int_as_float(0x7f800000);
-    uint32_t arg = 0xffffffffu;
-    for (uint32_t k = 0; k < n; ++k) {
-        const uint32_t r = rows[k];
-        const float d = sq_dist_spec(A + (size_t)r * kDesc, bj);
-        if (d < best || (d == best && r < arg)) {
-            best = d;
-            arg = r;
-        }
-    }
-    return arg == i;
+// Mutual check of a candidate (i, j) from the column window counts: a row
+// whose d~ lies above the window (c1 + 2 eps) is provably not the column's
+// nearest; the only row inside it provably is. Returns the decision or
+// kDecPending after queueing an exact column check.
+SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &sp, uint32_t i, uint32_t j, float dij) {
+    const uint32_t cidx = sp.cbase + j;
+    if (!(dij <= g.colthr[cidx])) return kDecNone;
+    if (g.colcnt[cidx] == 1) return j;
+    push_scan(g, p, 1, i, j);
+    return kDecPending;
 }
 
+// One thread per row: decide from the bounds, or queue exact work.
 __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
     const uint32_t p = blockIdx.x;
     const PairMeta pm = g.pairs[p];
@@ -659,18 +660,16 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
     const float kInf = __int_as_float(0x7f800000);
     const float eps = sp.eps;
     const double r2 = (double)g.ratio2;
-    const float *A = g.raw + (size_t)pm.a_row0 * kDesc;
-    const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
     for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
         const uint32_t ridx = sp.rbase + i;
         uint32_t dec = kDecNone;
         if (sp.unsafe) {
-            sl_enqueue(g, p, 0, i, 0);
+            push_scan(g, p, 0, i, 0);
             dec = kDecPending;
         } else if (g.rowthr[ridx] > -kInf) {
             const uint32_t n = g.rowcnt[ridx];
             if (n > kSlRowSlots) {
-                sl_enqueue(g, p, 0, i, 0);
+                push_scan(g, p, 0, i, 0);
                 dec = kDecPending;
             } else {
                 const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
@@ -687,61 +686,19 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
                         a2 = v;
                     }
                 }
-                uint32_t cand = 0xffffffffu;
                 // S holds every column with d~ <= T, T >= (second smallest d~) + 2 eps,
-                // so the exact two smallest distances are rescored from S. With
-                // fewer than two finite entries the exact second best is infinite
+                // so the exact two smallest distances are among S. With fewer than
+                // two finite entries the exact second best is infinite
                 // (matching.rs:205: no match).
                 const bool no_match = n < 2 || !(a2 < kInf) ||
                                       (double)a1 - eps >= r2 * ((double)a2 + eps) * (1.0 + 1e-6);
                 const bool sure = !no_match && (double)a1 + eps < r2 * ((double)a2 - eps) * (1.0 - 1e-6) &&
                                   (double)a2 - a1 > 2.0 * eps;
                 if (sure) {
-                    cand = j1;
+                    dec = g.mutual ? mutual_from_counts(g, p, sp, i, j1, a1) : j1;
                 } else if (!no_match) {
-                    // exact rescore of S (the reference's row update, matching.rs:182-187)
-                    float e1 = kInf, e2 = kInf;
-                    uint32_t ej = 0xffffffffu;
-                    float maxerr = 0.f;
-                    for (uint32_t k = 0; k < n; ++k) {
-                        const uint2 e = S[k];
-                        const float d = sq_dist_spec(A + (size_t)i * kDesc, B + (size_t)e.x * kDesc);
-                        maxerr = fmaxf(maxerr, fabsf(d - __uint_as_float(e.y)));
-                        if (d < e1 || (d == e1 && e.x < ej)) {
-                            e2 = e1;
-                            e1 = d;
-                            ej = e.x;
-                        } else if (d < e2) {
-                            e2 = d;
-                        }
-                    }
-                    atomicAdd(&g.ctl[kCtlRescored], 1u);
-                    if (maxerr == maxerr) atomicMax(&g.ctl[kCtlMaxErr], __float_as_uint(maxerr));
-                    if (ej != 0xffffffffu && e2 < kInf && !(e1 >= __fmul_rn(g.ratio2, e2))) cand = ej;
-                }
-                if (cand != 0xffffffffu) {
-                    if (!g.mutual) {
-                        dec = cand;
-                    } else {
-                        const uint32_t cidx = sp.cbase + cand;
-                        const uint32_t cn = g.colcnt[cidx];
-                        if (cn > kSlColSlots) {
-                            sl_enqueue(g, p, 1, i, cand);
-                            dec = kDecPending;
-                        } else {
-                            const uint32_t *C = g.colcand + (size_t)cidx * kSlColSlots;
-                            bool in = false;
-                            for (uint32_t k = 0; k < cn; ++k) in |= C[k] == i;
-                            if (in) {
-                                if (cn == 1) {
-                                    dec = cand;
-                                } else {
-                                    atomicAdd(&g.ctl[kCtlColRescored], 1u);
-                                    if (exact_col_winner(A, B + (size_t)cand * kDesc, C, cn, i)) dec = cand;
-                                }
-                            }
-                        }
-                    }
+                    sl_push(g.rqueue, &g.ctl[kCtlRescoreLen], g.queue_cap, g.ctl + 1, p, 2, i, 0);
+                    dec = kDecPending;
                 }
             }
         }
@@ -749,79 +706,199 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
     }
 }
 
-// ------------------------------------------------------------- recompute
+// ------------------------------------------------------------- exact work
 
-// One warp per queued entry: exact scans in the reference's order and
-// tie rules (rows: matching.rs:182-187; columns: :188-203).
-__global__ void __launch_bounds__(256) sl_recompute_kernel(SlArgs g) {
-    const uint32_t lane = threadIdx.x & 31;
+// Exact distance by 8 lanes: lane k of the group accumulates components
+// 8c+k for c = 0..15 (matching.rs:146-155), then the lane sums are added in
+// order 0..7. p and r may differ per group; the result is valid in all 8 lanes.
+SLM_DEV float dist8(const float *__restrict__ p, const float *__restrict__ r) {
+    const uint32_t lane = threadIdx.x & 31, k = lane & 7, base = lane & ~7u;
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+        const float t = __fsub_rn(p[8 * c + k], r[8 * c + k]);
+        acc = __fadd_rn(acc, __fmul_rn(t, t));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s = __fadd_rn(s, __shfl_sync(0xffffffffu, acc, base + q));
+    return s;
+}
+
+// One warp per row of the rescore queue: exact distances of S (4 at a time),
+// the reference's row rule (matching.rs:182-187, 204-206), then the mutual
+// check from the column window counts.
+__global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
+    const uint32_t lane = threadIdx.x & 31, grp = lane >> 3;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t qn = min(g.ctl[kCtlQueueLen], g.queue_cap);
+    const uint32_t qn = min(g.ctl[kCtlRescoreLen], g.queue_cap);
     const float kInf = __int_as_float(0x7f800000);
     for (uint32_t e = gw; e < qn; e += nw) {
+        const SlQueue qe = g.rqueue[e];
+        const PairMeta pm = g.pairs[qe.pair];
+        const SlPair sp = g.spairs[qe.pair];
+        const uint32_t ridx = sp.rbase + qe.i;
+        const uint32_t n = g.rowcnt[ridx];
+        const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
+        const float *a = g.raw + (size_t)(pm.a_row0 + qe.i) * kDesc;
+        const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
+        float e1 = kInf, e2 = kInf, ad = kInf, maxerr = 0.f;
+        uint32_t ej = 0xffffffffu;
+        for (uint32_t k0 = 0; k0 < n; k0 += 4) {
+            const uint32_t k = k0 + grp;
+            const uint2 ent = S[k < n ? k : k0];
+            const float d = dist8(a, B + (size_t)ent.x * kDesc);
+            // every lane merges the 4 results in slot order
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                const float dq = __shfl_sync(0xffffffffu, d, q * 8);
+                const uint2 eq = S[k0 + q < n ? k0 + q : k0];
+                if (k0 + q < n) {
+                    const float approx = __uint_as_float(eq.y);
+                    maxerr = fmaxf(maxerr, fabsf(dq - approx));
+                    if (dq < e1 || (dq == e1 && eq.x < ej)) {
+                        e2 = e1;
+                        e1 = dq;
+                        ej = eq.x;
+                        ad = approx;
+                    } else if (dq < e2) {
+                        e2 = dq;
+                    }
+                }
+            }
+        }
+        if (lane == 0) {
+            atomicAdd(&g.ctl[kCtlRescored], 1u);
+            if (maxerr == maxerr) atomicMax(&g.ctl[kCtlMaxErr], __float_as_uint(maxerr));
+            uint32_t dec = kDecNone;
+            if (ej != 0xffffffffu && e2 < kInf && !(e1 >= __fmul_rn(g.ratio2, e2)))
+                dec = g.mutual ? mutual_from_counts(g, qe.pair, sp, qe.i, ej, ad) : ej;
+            g.rowdec[ridx] = dec;
+        }
+    }
+}
+
+// Block-wide (d, index) minimum with the lowest index on ties; all threads
+// get the result.
+SLM_DEV void block_argmin(float &d, uint32_t &idx, float *sd, uint32_t *si) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, d, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (od < d || (od == d && oi < idx)) {
+            d = od;
+            idx = oi;
+        }
+    }
+    const int w = threadIdx.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        sd[w] = d;
+        si[w] = idx;
+    }
+    __syncthreads();
+    d = sd[0];
+    idx = si[0];
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        if (sd[q] < d || (sd[q] == d && si[q] < idx)) {
+            d = sd[q];
+            idx = si[q];
+        }
+}
+
+// One CTA per entry of the scan queue: exact full scans, 32 distances at a
+// time (8 lanes each).
+__global__ void __launch_bounds__(256) sl_scan_kernel(SlArgs g) {
+    __shared__ float sd[8], s2[8];
+    __shared__ uint32_t si[8];
+    const uint32_t lane = threadIdx.x & 31, grp = threadIdx.x >> 3;  // 32 groups of 8 lanes
+    const uint32_t qn = min(g.ctl[kCtlScanLen], g.queue_cap);
+    const float kInf = __int_as_float(0x7f800000);
+    for (uint32_t e = blockIdx.x; e < qn; e += gridDim.x) {
         const SlQueue qe = g.queue[e];
         const PairMeta pm = g.pairs[qe.pair];
         const SlPair sp = g.spairs[qe.pair];
         const float *A = g.raw + (size_t)pm.a_row0 * kDesc;
         const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
-        uint32_t dec = kDecNone;
-        uint32_t col = qe.j;
+        uint32_t dec = kDecNone, col = qe.j;
         bool check_col = qe.kind == 1;
         if (qe.kind == 0) {
             float d1 = kInf, d2 = kInf;
             uint32_t j1 = 0xffffffffu;
-            for (uint32_t j = lane; j < pm.nb; j += 32) {
-                const float d = sq_dist_spec(A + (size_t)qe.i * kDesc, B + (size_t)j * kDesc);
-                if (d < d1) {
-                    d2 = d1;
-                    d1 = d;
-                    j1 = j;
-                } else if (d < d2) {
-                    d2 = d;
+            for (uint32_t j0 = 0; j0 < pm.nb; j0 += 32) {
+                const uint32_t j = j0 + grp;
+                const float d = dist8(A + (size_t)qe.i * kDesc, B + (size_t)(j < pm.nb ? j : 0) * kDesc);
+                if (j < pm.nb) {
+                    if (d < d1) {
+                        d2 = d1;
+                        d1 = d;
+                        j1 = j;
+                    } else if (d < d2) {
+                        d2 = d;
+                    }
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                const float o1 = __shfl_xor_sync(0xffffffffu, d1, o);
-                const float o2 = __shfl_xor_sync(0xffffffffu, d2, o);
-                const uint32_t oj = __shfl_xor_sync(0xffffffffu, j1, o);
-                const float n2 = fminf(fminf(d2, o2), fmaxf(d1, o1));
-                if (o1 < d1 || (o1 == d1 && oj < j1)) {
-                    d1 = o1;
-                    j1 = oj;
+            // merge (d1, j1, d2) across the 32 groups (lanes within a group agree)
+            float m2 = d2;
+            float b1 = d1;
+            uint32_t bj = j1;
+#pragma unroll
+            for (int o = 8; o < 32; o <<= 1) {
+                const float o1 = __shfl_xor_sync(0xffffffffu, b1, o);
+                const float o2 = __shfl_xor_sync(0xffffffffu, m2, o);
+                const uint32_t oj = __shfl_xor_sync(0xffffffffu, bj, o);
+                const float n2 = fminf(fminf(m2, o2), fmaxf(b1, o1));
+                if (o1 < b1 || (o1 == b1 && oj < bj)) {
+                    b1 = o1;
+                    bj = oj;
                 }
-                d2 = n2;
+                m2 = n2;
             }
-            if (j1 != 0xffffffffu && d2 < kInf && !(d1 >= __fmul_rn(g.ratio2, d2))) {
+            const int w = threadIdx.x >> 5;
+            __syncthreads();
+            if (lane == 0) {
+                sd[w] = b1;
+                s2[w] = m2;
+                si[w] = bj;
+            }
+            __syncthreads();
+            b1 = sd[0];
+            m2 = s2[0];
+            bj = si[0];
+            for (int q = 1; q < 8; ++q) {
+                const float n2 = fminf(fminf(m2, s2[q]), fmaxf(b1, sd[q]));
+                if (sd[q] < b1 || (sd[q] == b1 && si[q] < bj)) {
+                    b1 = sd[q];
+                    bj = si[q];
+                }
+                m2 = n2;
+            }
+            if (bj != 0xffffffffu && m2 < kInf && !(b1 >= __fmul_rn(g.ratio2, m2))) {
                 if (g.mutual) {
                     check_col = true;
-                    col = j1;
+                    col = bj;
                 } else {
-                    dec = j1;
+                    dec = bj;
                 }
             }
         }
         if (check_col) {
             float bd = kInf;
             uint32_t bi = 0xffffffffu;
-            for (uint32_t r = lane; r < pm.na; r += 32) {
-                const float d = sq_dist_spec(A + (size_t)r * kDesc, B + (size_t)col * kDesc);
-                if (d < bd) {
+            for (uint32_t r0 = 0; r0 < pm.na; r0 += 32) {
+                const uint32_t r = r0 + grp;
+                const float d = dist8(A + (size_t)(r < pm.na ? r : 0) * kDesc, B + (size_t)col * kDesc);
+                if (r < pm.na && (d < bd || (d == bd && r < bi))) {
                     bd = d;
                     bi = r;
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                const float od = __shfl_xor_sync(0xffffffffu, bd, o);
-                const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (od < bd || (od == bd && oi < bi)) {
-                    bd = od;
-                    bi = oi;
-                }
-            }
+            block_argmin(bd, bi, sd, si);
             dec = bi == qe.i ? col : kDecNone;
         }
-        if (lane == 0) g.rowdec[sp.rbase + qe.i] = dec;
+        if (threadIdx.x == 0) g.rowdec[sp.rbase + qe.i] = dec;
+        __syncthreads();
     }
 }
 
@@ -876,7 +953,7 @@ cudaError_t init_shortlist_kernels() {
                                 (int)sl_smem_bytes<true>());
 }
 
-int shortlist_kernel_count() { return 6; }
+int shortlist_kernel_count() { return 7; }
 
 void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s) {
     const int grid = (int)(a.n_items < (uint32_t)sms ? a.n_items : (uint32_t)sms);
@@ -892,7 +969,8 @@ void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s) {
         if (grid) sl_pass_kernel<2, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
     }
     if (a.npairs) sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
-    sl_recompute_kernel<<<2 * sms, 256, 0, s>>>(a);
+    sl_rescore_kernel<<<2 * sms, 256, 0, s>>>(a);
+    sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
     if (a.npairs) sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
 }
 

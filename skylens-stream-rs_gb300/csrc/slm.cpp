@@ -182,8 +182,8 @@ struct slm_plan {
     std::vector<SlItem> sitems;
     std::vector<SlPair> spairs;
     uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0;
-    DevBuf d_sitems, d_spairs, d_rowpart, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt, d_colcand,
-        d_rowdec, d_queue, d_dump;
+    DevBuf d_sitems, d_spairs, d_rowpart, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
+        d_rowdec, d_queue, d_rqueue, d_dump;
     bool dump = false;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -308,9 +308,9 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     SLM_TRY(p->d_rowcnt.ensure(c, sizeof(uint32_t) * p->rows_pad));
     SLM_TRY(p->d_rowcand.ensure(c, sizeof(uint2) * kSlRowSlots * p->rows_pad));
     SLM_TRY(p->d_colcnt.ensure(c, sizeof(uint32_t) * p->cols_pad));
-    SLM_TRY(p->d_colcand.ensure(c, sizeof(uint32_t) * kSlColSlots * p->cols_pad));
     SLM_TRY(p->d_rowdec.ensure(c, sizeof(uint32_t) * p->rows_pad));
     SLM_TRY(p->d_queue.ensure(c, sizeof(SlQueue) * p->queue_cap));
+    SLM_TRY(p->d_rqueue.ensure(c, sizeof(SlQueue) * p->queue_cap));
     if (p->dump && p->np) SLM_TRY(p->d_dump.ensure(c, sizeof(float) * std::max<uint64_t>(1, (uint64_t)p->meta[0].na * p->meta[0].nb)));
     SLM_TRY(p->d_meta.ensure(c, sizeof(PairMeta) * std::max<size_t>(1, p->np)));
     SLM_TRY(p->d_slots.ensure(c, sizeof(uint2) * std::max<uint64_t>(1, p->n_slots)));
@@ -401,9 +401,9 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.rowcnt = p->d_rowcnt.as<uint32_t>();
         a.rowcand = p->d_rowcand.as<uint2>();
         a.colcnt = p->d_colcnt.as<uint32_t>();
-        a.colcand = p->d_colcand.as<uint32_t>();
         a.rowdec = p->d_rowdec.as<uint32_t>();
         a.queue = p->d_queue.as<SlQueue>();
+        a.rqueue = p->d_rqueue.as<SlQueue>();
         a.queue_cap = (uint32_t)p->queue_cap;
         a.ctl = ctl;
         a.ratio2 = p->ratio * p->ratio;
@@ -564,7 +564,7 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
         SLM_CU(cudaMemcpy(w, p->d_ctl.p, sizeof(w), cudaMemcpyDeviceToHost));
         st->rows_rescored = w[kCtlRescored];
         st->rows_recomputed = w[kCtlQueueRows];
-        st->cols_recomputed = (uint64_t)w[kCtlQueueCols] + w[kCtlColRescored];
+        st->cols_recomputed = w[kCtlQueueCols];
         float e;
         std::memcpy(&e, &w[kCtlMaxErr], sizeof(e));
         st->max_abs_err = e;

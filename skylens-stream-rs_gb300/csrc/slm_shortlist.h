@@ -14,14 +14,16 @@
 //   mid                per row: threshold T = m2' + 2 eps, or "certain no
 //                      match" when m1 - eps >= r^2 (m2' + eps); per column:
 //                      threshold c1 + 2 eps.
-//   pass 2  (tcgen05)  recomputes d~ and appends (j, d~) with d~ <= T to the
-//                      row's candidate list S, and i with d~ <= c1 + 2 eps to
-//                      the column's list C.
-//   finalize           per row, from S: certain outcomes from the bounds, else
-//                      an exact rescore of S; the mutual check from C (a row
-//                      outside C loses, a sole member wins, else exact rescore
-//                      of C). Lists that overflowed go to the queue.
-//   recompute          exact FP32 row / column scans for queued rows.
+//   pass 2  (tcgen05)  recomputes d~; appends (j, d~) with d~ <= T to the row's
+//                      candidate list S and counts, per column, the rows with
+//                      d~ <= c1 + 2 eps (|C|).
+//   finalize           per row, from S: certain outcomes from the bounds; the
+//                      mutual check from |C| (a row above the column window
+//                      loses, the only row inside it wins). Everything else is
+//                      queued: rows to rescore exactly, rows to rescan, columns
+//                      to rescan.
+//   rescore            one warp per queued row: exact distances of S.
+//   scan               one CTA per queued row or column: exact full scans.
 #pragma once
 #include <cstdint>
 
@@ -30,7 +32,6 @@
 namespace slm {
 
 constexpr int kSlRowSlots = 16;    // S capacity per row
-constexpr int kSlColSlots = 8;     // C capacity per column
 constexpr int kSlStages = 4;       // b-tile ring depth
 constexpr int kSlThreads = 320;    // producer, MMA, 8 epilogue warps
 
@@ -68,14 +69,16 @@ struct SlPair {
 constexpr uint32_t kDecNone = 0xffffffffu;
 constexpr uint32_t kDecPending = 0xfffffffeu;
 
-// Queue entry for the recompute kernel.
+// Queue entries: the scan queue holds kind 0 (exact row scan of row i) and
+// kind 1 (exact column check: is row i the argmin of column j); the rescore
+// queue holds rows i whose S is rescored exactly.
 struct SlQueue {
-    uint32_t pair, kind, i, j;  // kind 0: exact row scan; 1: exact column check of (i, j)
+    uint32_t pair, kind, i, j;
 };
 
 // Counters in the plan's control block (u32 words after work/error).
-enum : int { kCtlRescored = 2, kCtlQueueRows = 3, kCtlQueueCols = 4, kCtlMaxErr = 5, kCtlQueueLen = 6,
-             kCtlColRescored = 7 };
+enum : int { kCtlRescored = 2, kCtlQueueRows = 3, kCtlQueueCols = 4, kCtlMaxErr = 5, kCtlScanLen = 6,
+             kCtlRescoreLen = 7 };
 
 struct SlArgs {
     const uint8_t *optiles;      // operand tiles by store row / 128
@@ -94,11 +97,11 @@ struct SlArgs {
     float *colthr;               // mid -> pass 2
     uint32_t *rowcnt;            // pass 2
     uint2 *rowcand;              // (j, bits(d~))
-    uint32_t *colcnt;
-    uint32_t *colcand;           // i
-    uint32_t *rowdec;            // finalize / recompute
-    SlQueue *queue;
-    uint32_t queue_cap;
+    uint32_t *colcnt;            // |C| per column
+    uint32_t *rowdec;            // finalize / rescore / scan
+    SlQueue *queue;              // scan queue
+    SlQueue *rqueue;             // rescore queue
+    uint32_t queue_cap;          // capacity of each queue
     uint32_t *ctl;               // [1] error word, counters at kCtl*
     float ratio2;
     int mutual;

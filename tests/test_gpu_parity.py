@@ -167,3 +167,40 @@ def test_device_entry_point(matcher, prec):
     ref = O.ratio_match_np(a, b, 0.8, True, threads=4)
     assert n == len(ref)
     assert np.array_equal(out[:n].cpu().numpy().astype(np.uint32), ref)
+
+
+def plan_rm(matcher, prec, variant):
+    """ratio_match through a one-pair batch plan (lets a test pick the kernel variant)."""
+    def rm(a, b, ratio, mutual):
+        a = np.ascontiguousarray(a, np.float32).reshape(-1, 128)
+        b = np.ascontiguousarray(b, np.float32).reshape(-1, 128)
+        st = matcher.store(len(a) + len(b), 2)
+        st.add_view(a)
+        st.add_view(b)
+        p = st.plan([(0, 1)], ratio, mutual, prec, variant=variant)
+        p.launch()
+        got = p.per_pair()[0]
+        p.close()
+        st.close()
+        return [tuple(x) for x in got.tolist()]
+    return rm
+
+
+@pytest.mark.parametrize("case", refcases.ALL, ids=lambda f: f.__name__)
+@pytest.mark.parametrize("variant", [1, 3], ids=["fp32-scalar", "fp32-packed"])
+def test_reference_case_fp32_variants(matcher, case, variant):
+    case(plan_rm(matcher, "fp32", variant))
+
+
+@pytest.mark.parametrize("variant", [1, 3], ids=["fp32-scalar", "fp32-packed"])
+def test_zone_batch_fp32_variants(matcher, variant):
+    z = synth.zone(positions=8, n_range=(100, 1200), seed=9)
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    st.add_views_packed(z.desc, z.offsets, z.counts)
+    plan = st.plan(z.pairs, 0.8, True, "fp32", variant=variant)
+    plan.launch()
+    per = plan.per_pair()
+    for k, (u, v) in enumerate(z.pairs):
+        assert np.array_equal(per[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16)), k
+    plan.close()
+    st.close()
