@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
-    ap.add_argument("--x2", action="store_true", help="FP32 kernel with packed f32x2 arithmetic (experimental)")
+    ap.add_argument("--scalar", action="store_true", help="FP32 kernel with all-scalar arithmetic")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -213,7 +213,7 @@ def main():
     ext = torch.cuda.ExternalStream(m.stream)
     store = m.store(n_rows, len(z.counts))
     store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
-    variant = 3 if args.x2 else 0
+    variant = 1 if args.scalar else 0
     plan = store.plan(z.pairs, 0.8, True, prec, variant=variant)
     plan_fp32 = plan if prec == "fp32" else store.plan(z.pairs, 0.8, True, "fp32", variant=variant)
 

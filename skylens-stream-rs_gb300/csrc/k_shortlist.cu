@@ -69,6 +69,16 @@ SLM_DEV float min32(const float (&d)[32]) {
     return fminf(min3f(x, y, z), fminf(m[9], m[10]));
 }
 
+// Minimum of 32 values plus the minima of its four groups of 8, so that a
+// rare hit below a threshold scans 8 values instead of 32.
+SLM_DEV float min32g(const float (&d)[32], float (&gm)[4]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        gm[q] = fminf(min3f(d[8 * q], d[8 * q + 1], d[8 * q + 2]),
+                      min3f(d[8 * q + 3], d[8 * q + 4], min3f(d[8 * q + 5], d[8 * q + 6], d[8 * q + 7])));
+    return fminf(min3f(gm[0], gm[1], gm[2]), gm[3]);
+}
+
 // Exact reference distance (matching.rs:146-155): lane k = components 8c+k.
 SLM_DEV float sq_dist_spec(const float *__restrict__ p, const float *__restrict__ r) {
     float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -478,16 +488,22 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                             }
                         } else {
                             if (thr_i > -kInf) {
-                                const float cm = min32(d);
+                                float gm[4];
+                                const float cm = min32g(d, gm);
                                 if (cm <= thr_i) {
                                     const uint32_t ridx = sp.rbase + i;
                                     uint2 *dst = g.rowcand + (size_t)ridx * kSlRowSlots;
 #pragma unroll
-                                    for (int k = 0; k < 32; ++k) {
-                                        if (d[k] <= thr_i) {
-                                            // one item owns the whole row unless its columns are split
-                                            const uint32_t s = own_row ? ncand++ : atomicAdd(&g.rowcnt[ridx], 1u);
-                                            if (s < kSlRowSlots) dst[s] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                    for (int q = 0; q < 4; ++q) {
+                                        if (gm[q] <= thr_i) {
+#pragma unroll
+                                            for (int k = 8 * q; k < 8 * q + 8; ++k) {
+                                                if (d[k] <= thr_i) {
+                                                    // one item owns the whole row unless its columns are split
+                                                    const uint32_t s = own_row ? ncand++ : atomicAdd(&g.rowcnt[ridx], 1u);
+                                                    if (s < kSlRowSlots) dst[s] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                }
+                                            }
                                         }
                                     }
                                 }
@@ -503,11 +519,17 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                     x[4 * k4 + 2] = d[4 * k4 + 2] - tt.z;
                                     x[4 * k4 + 3] = d[4 * k4 + 3] - tt.w;
                                 }
-                                const float xm = min32(x);
+                                float gm[4];
+                                const float xm = min32g(x, gm);
                                 if (xm <= 0.f) {
 #pragma unroll
-                                    for (int k = 0; k < 32; ++k)
-                                        if (x[k] <= 0.f) atomicAdd(&g.colcnt[sp.cbase + j0 + k], 1u);  // no return: a reduction
+                                    for (int q = 0; q < 4; ++q) {
+                                        if (gm[q] <= 0.f) {
+#pragma unroll
+                                            for (int k = 8 * q; k < 8 * q + 8; ++k)
+                                                if (x[k] <= 0.f) atomicAdd(&g.colcnt[sp.cbase + j0 + k], 1u);  // reduction
+                                        }
+                                    }
                                 }
                             }
                         }

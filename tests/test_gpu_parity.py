@@ -187,12 +187,12 @@ def plan_rm(matcher, prec, variant):
 
 
 @pytest.mark.parametrize("case", refcases.ALL, ids=lambda f: f.__name__)
-@pytest.mark.parametrize("variant", [1, 3], ids=["fp32-scalar", "fp32-packed"])
+@pytest.mark.parametrize("variant", [1, 0], ids=["fp32-scalar", "fp32-packed"])
 def test_reference_case_fp32_variants(matcher, case, variant):
     case(plan_rm(matcher, "fp32", variant))
 
 
-@pytest.mark.parametrize("variant", [1, 3], ids=["fp32-scalar", "fp32-packed"])
+@pytest.mark.parametrize("variant", [1, 0], ids=["fp32-scalar", "fp32-packed"])
 def test_zone_batch_fp32_variants(matcher, variant):
     z = synth.zone(positions=8, n_range=(100, 1200), seed=9)
     st = matcher.store(int(z.counts.sum()), len(z.counts))
