@@ -1,0 +1,156 @@
+//! Safe wrapper over libslm with the reference's signatures:
+//!
+//! * `ratio_match(a, b, ratio, mutual) -> Vec<(usize, usize)>`
+//!   (skylens_core::matching::ratio_match, crates/core/src/matching.rs:167)
+//! * `candidate_pairs(views, temporal, cross, pow2_max)` (matching.rs:18)
+//! * `match_pairs(descs, pairs, ratio, mutual)`: the matching half of
+//!   pipeline.rs:485-493 as one GPU batch.
+//!
+//! The one deviation from the reference: it cannot fail on the CPU, this can
+//! fail on the GPU; a non-OK status panics with libslm's message (there is no
+//! CPU fallback). The process-wide context is thread-safe, so the function may
+//! be called from rayon workers as the reference is.
+use skylens_match_sys as sys;
+use std::ffi::CStr;
+use std::sync::OnceLock;
+
+/// Anything that carries a 128-float descriptor (skylens_core's `Feature`
+/// implements it with `fn desc(&self) -> &[f32; 128] { &self.desc }`).
+pub trait Descriptor {
+    fn desc(&self) -> &[f32; 128];
+}
+
+/// Which kernel family computes the distances (all give identical results).
+#[derive(Clone, Copy, Debug, PartialEq, Eq)]
+pub enum Precision {
+    Fp32,
+    Bf16,
+    Fp8,
+}
+
+impl Precision {
+    fn raw(self) -> sys::SlmPrecision {
+        match self {
+            Precision::Fp32 => sys::SLM_PREC_FP32,
+            Precision::Bf16 => sys::SLM_PREC_BF16,
+            Precision::Fp8 => sys::SLM_PREC_FP8,
+        }
+    }
+}
+
+struct Ctx(*mut sys::slm_ctx);
+// libslm contexts are safe to share across threads (include/slm.h).
+unsafe impl Send for Ctx {}
+unsafe impl Sync for Ctx {}
+
+fn check(st: sys::SlmStatus, what: &str) {
+    if st != sys::SLM_OK {
+        let msg = unsafe { CStr::from_ptr(sys::slm_last_error()) }.to_string_lossy().into_owned();
+        let name = unsafe { CStr::from_ptr(sys::slm_status_str(st)) }.to_string_lossy().into_owned();
+        panic!("{what}: {name}: {msg}");
+    }
+}
+
+fn ctx() -> *mut sys::slm_ctx {
+    static CTX: OnceLock<Ctx> = OnceLock::new();
+    CTX.get_or_init(|| {
+        let opts = sys::slm_opts { device: 0, stream: std::ptr::null_mut(), hbm_budget: 0 };
+        let mut h = std::ptr::null_mut();
+        check(unsafe { sys::slm_ctx_create(&opts, &mut h) }, "slm_ctx_create");
+        Ctx(h)
+    })
+    .0
+}
+
+fn pack<D: Descriptor>(v: &[D]) -> Vec<f32> {
+    let mut out = Vec::with_capacity(v.len() * 128);
+    for d in v {
+        out.extend_from_slice(d.desc());
+    }
+    out
+}
+
+/// Drop-in for `skylens_core::matching::ratio_match` (BF16 shortlist, exact).
+pub fn ratio_match<D: Descriptor>(a: &[D], b: &[D], ratio: f32, mutual: bool) -> Vec<(usize, usize)> {
+    ratio_match_with(a, b, ratio, mutual, Precision::Bf16)
+}
+
+pub fn ratio_match_with<D: Descriptor>(a: &[D], b: &[D], ratio: f32, mutual: bool, p: Precision)
+                                       -> Vec<(usize, usize)> {
+    let (fa, fb) = (pack(a), pack(b));
+    let mut out = vec![sys::slm_pair::default(); a.len().max(1)];
+    let mut n = 0u32;
+    check(
+        unsafe {
+            sys::slm_ratio_match(ctx(), fa.as_ptr(), a.len() as u32, fb.as_ptr(), b.len() as u32, ratio,
+                                 mutual as i32, p.raw(), out.as_mut_ptr(), out.len() as u32, &mut n,
+                                 std::ptr::null_mut())
+        },
+        "slm_ratio_match",
+    );
+    out.truncate(n as usize);
+    out.into_iter().map(|p| (p.i as usize, p.j as usize)).collect()
+}
+
+/// `candidate_pairs` (matching.rs:18-40), computed by libslm's host code.
+pub fn candidate_pairs(views: &[(usize, usize)], temporal: usize, cross: usize, pow2_max: usize)
+                       -> Vec<(usize, usize)> {
+    let flat: Vec<u64> = views.iter().flat_map(|&(c, p)| [c as u64, p as u64]).collect();
+    let mut n = 0u64;
+    let st = unsafe {
+        sys::slm_candidate_pairs(flat.as_ptr(), views.len() as u32, temporal as u64, cross as u64,
+                                 pow2_max as u64, std::ptr::null_mut(), 0, &mut n)
+    };
+    if st != sys::SLM_CAPACITY && st != sys::SLM_OK {
+        check(st, "slm_candidate_pairs");
+    }
+    let mut out = vec![sys::slm_pair::default(); n as usize];
+    check(
+        unsafe {
+            sys::slm_candidate_pairs(flat.as_ptr(), views.len() as u32, temporal as u64, cross as u64,
+                                     pow2_max as u64, out.as_mut_ptr(), n, &mut n)
+        },
+        "slm_candidate_pairs",
+    );
+    out.into_iter().map(|p| (p.i as usize, p.j as usize)).collect()
+}
+
+/// The matching half of `pipeline::match_pairs` (pipeline.rs:485-493): every
+/// pair's `ratio_match(fa, fb, ratio, mutual)` in one GPU batch. `views[v]` are
+/// the features of view v; returns one match list per pair, in pair order.
+pub fn match_pairs<D: Descriptor>(views: &[&[D]], pairs: &[(usize, usize)], ratio: f32, mutual: bool)
+                                  -> Vec<Vec<(usize, usize)>> {
+    let c = ctx();
+    let total: usize = views.iter().map(|v| v.len()).sum();
+    let mut store = std::ptr::null_mut();
+    check(unsafe { sys::slm_store_create(c, total as u64, views.len() as u32, &mut store) }, "slm_store_create");
+    let mut desc = Vec::with_capacity(total * 128);
+    let (mut offsets, mut counts) = (Vec::new(), Vec::new());
+    for v in views {
+        offsets.push((desc.len() / 128) as u64);
+        counts.push(v.len() as u32);
+        desc.extend(pack(v));
+    }
+    let mut ids = vec![0u32; views.len()];
+    check(
+        unsafe {
+            sys::slm_store_add_views(store, desc.as_ptr(), offsets.as_ptr(), counts.as_ptr(), views.len() as u32,
+                                     ids.as_mut_ptr())
+        },
+        "slm_store_add_views",
+    );
+    let raw: Vec<sys::slm_pair> =
+        pairs.iter().map(|&(i, j)| sys::slm_pair { i: ids[i], j: ids[j] }).collect();
+    let cap: usize = pairs.iter().map(|&(i, _)| views[i].len()).sum::<usize>().max(1);
+    let mut out = vec![sys::slm_pair::default(); cap];
+    let mut off = vec![0u64; pairs.len() + 1];
+    let st = unsafe {
+        sys::slm_match_batch(c, store, raw.as_ptr(), raw.len() as u32, ratio, mutual as i32, sys::SLM_PREC_BF16,
+                             out.as_mut_ptr(), cap as u64, off.as_mut_ptr(), std::ptr::null_mut())
+    };
+    unsafe { sys::slm_store_destroy(store) };
+    check(st, "slm_match_batch");
+    (0..pairs.len())
+        .map(|k| out[off[k] as usize..off[k + 1] as usize].iter().map(|p| (p.i as usize, p.j as usize)).collect())
+        .collect()
+}
