@@ -111,6 +111,24 @@ slm_status slm_ratio_match_device(slm_ctx *ctx, const float *d_a, uint32_t na, c
                                   float ratio, int mutual, slm_precision prec, slm_pair *d_out, uint32_t cap,
                                   uint32_t *d_count);
 
+/* The same exact FP32 match without any device allocation. No counterpart in
+ * the reference. For callers that cannot call cudaMalloc: an application whose
+ * framework owns all device memory through its own pool, or a latency-critical
+ * loop where an allocation (which may synchronise the device) would stall other
+ * streams. No context is needed: work goes to `stream` (a cudaStream_t; NULL is
+ * the legacy default stream) on the current device. Scratch comes from one
+ * fixed device array inside the library (about 5 MiB, held by every device
+ * that loads the library until exit), which limits na and nb to
+ * SLM_NOALLOC_MAX_DESCS each; larger sizes return SLM_INVALID_ARG. d_a and d_b
+ * must be 16-byte aligned. The first call on a device sets that device up
+ * (make it before any stream capture). Calls share the array: calls that
+ * overlap on the GPU race. *d_count receives the match count (0xffffffff if a
+ * bounded device wait gave up); at most cap pairs are written to d_out. */
+#define SLM_NOALLOC_MAX_DESCS 4096
+slm_status slm_ratio_match_device_noalloc(const float *d_a, uint32_t na, const float *d_b, uint32_t nb, float ratio,
+                                          int mutual, slm_pair *d_out, uint32_t cap, uint32_t *d_count,
+                                          void *stream);
+
 /* ---------------------------------------------------- pair generators */
 
 /* candidate_pairs (matching.rs:18-40). views: 2*nv uint64 (camera, position).

@@ -144,6 +144,8 @@ extern "C" const char *slm_status_str(slm_status s) {
 
 extern "C" const char *slm_last_error(void) { return g_last_error.c_str(); }
 
+void slm::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
 // --------------------------------------------------------------------- store
 
 struct slm_store {

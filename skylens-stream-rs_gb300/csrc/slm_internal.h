@@ -77,5 +77,7 @@ void launch_exact(const ExactArgs &a, int grid, cudaStream_t s);
 cudaError_t init_exact_kernels();
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s);
 void launch_fill_u64(unsigned long long *p, uint64_t n, unsigned long long v, cudaStream_t s);
+// Sets the message slm_last_error() returns on this host thread.
+void set_last_error(const char *msg);
 
 }  // namespace slm

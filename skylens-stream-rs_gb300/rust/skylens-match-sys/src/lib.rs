@@ -95,6 +95,11 @@ extern "C" {
     pub fn slm_ratio_match_device(ctx: *mut slm_ctx, d_a: *const f32, na: u32, d_b: *const f32, nb: u32,
                                   ratio: f32, mutual: c_int, prec: SlmPrecision, d_out: *mut slm_pair, cap: u32,
                                   d_count: *mut u32) -> SlmStatus;
+    /// No counterpart in the reference: for callers that cannot allocate device
+    /// memory; na, nb <= 4096, overlapping calls race (include/slm.h).
+    pub fn slm_ratio_match_device_noalloc(d_a: *const f32, na: u32, d_b: *const f32, nb: u32, ratio: f32,
+                                          mutual: c_int, d_out: *mut slm_pair, cap: u32, d_count: *mut u32,
+                                          stream: *mut c_void) -> SlmStatus;
     pub fn slm_candidate_pairs(views: *const u64, nv: u32, temporal: u64, cross: u64, pow2_max: u64,
                                out: *mut slm_pair, cap: u64, n_out: *mut u64) -> SlmStatus;
     pub fn slm_pair_schedule_default() -> slm_pair_schedule;

@@ -65,6 +65,8 @@ SIGNATURES = {
                                 P(SlmPair), c_u32, P(c_u32), P(SlmStats)]),
     "slm_ratio_match_device": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, ctypes.c_void_p, c_u32, c_f32,
                                        c_int, c_int, ctypes.c_void_p, c_u32, ctypes.c_void_p]),
+    "slm_ratio_match_device_noalloc": (c_int, [ctypes.c_void_p, c_u32, ctypes.c_void_p, c_u32, c_f32, c_int,
+                                               ctypes.c_void_p, c_u32, ctypes.c_void_p, ctypes.c_void_p]),
     "slm_candidate_pairs": (c_int, [P(c_u64), c_u32, c_u64, c_u64, c_u64, P(SlmPair), c_u64, P(c_u64)]),
     "slm_pair_schedule_default": (SlmPairSchedule, []),
     "slm_pair_schedule_spec": (SlmPairSchedule, []),

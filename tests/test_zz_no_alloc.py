@@ -1,0 +1,73 @@
+"""GPU: slm_ratio_match_device_noalloc, the entry point that allocates nothing.
+
+It exists for callers that cannot call cudaMalloc (a framework that owns all
+device memory through its own pool, or a latency-critical loop where an
+allocation would stall other streams). Its scratch is one fixed device array
+in the library, so this checks that two calls in a row (the second smaller than
+the first, so the array still holds the first call's data) return exactly what
+the allocating entry point slm_ratio_match_device returns, and that sizes past
+the array's limit are refused. This file sorts last so a failure here comes
+after every other test has run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import skylens_match as sm
+from skylens_match import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+MAX_DESCS = 4096
+
+
+def _pair(seed, na, nb):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = synth.sift_like(rng, na)
+    k = min(na, nb) // 2
+    b = np.concatenate([synth.noisy_copy(rng, a[rng.permutation(na)[:k]], 0.05), synth.sift_like(rng, nb - k)])
+    return a, np.ascontiguousarray(b[rng.permutation(nb)])
+
+
+def test_noalloc_equals_allocating_entry_point_twice():
+    torch = pytest.importorskip("torch")
+    L = sm.load()
+    m = sm.Matcher()
+    stream = torch.cuda.ExternalStream(m.stream)
+    for seed, na, nb in [(1, 4096, 3900), (2, 700, 1300)]:
+        a, b = _pair(seed, na, nb)
+        da = torch.from_numpy(a).cuda()
+        db = torch.from_numpy(b).cuda()
+        ref_out = torch.zeros((na, 2), dtype=torch.int32, device="cuda")
+        ref_cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        out = torch.full((na, 2), -1, dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        m.ratio_match_device(da.data_ptr(), na, db.data_ptr(), nb, 0.8, True, "fp32", ref_out.data_ptr(), na,
+                             ref_cnt.data_ptr())
+        st = L.slm_ratio_match_device_noalloc(ctypes.c_void_p(da.data_ptr()), na, ctypes.c_void_p(db.data_ptr()), nb,
+                                              ctypes.c_float(0.8), 1, ctypes.c_void_p(out.data_ptr()), na,
+                                              ctypes.c_void_p(cnt.data_ptr()), ctypes.c_void_p(m.stream))
+        _lib.check(st, "slm_ratio_match_device_noalloc")
+        stream.synchronize()
+        n_ref, n = int(ref_cnt.item()), int(cnt.item())
+        assert n == n_ref
+        got = out[:n].cpu().numpy().astype(np.uint32)
+        assert np.array_equal(got, ref_out[:n_ref].cpu().numpy().astype(np.uint32))
+        assert np.array_equal(got, O.ratio_match_np(a, b, 0.8, True, threads=8))
+    m.close()
+
+
+def test_noalloc_refuses_sizes_beyond_its_array():
+    torch = pytest.importorskip("torch")
+    L = sm.load()
+    a = torch.zeros((MAX_DESCS + 1, 128), dtype=torch.float32, device="cuda")
+    out = torch.zeros((MAX_DESCS + 1, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = L.slm_ratio_match_device_noalloc(ctypes.c_void_p(a.data_ptr()), MAX_DESCS + 1, ctypes.c_void_p(a.data_ptr()),
+                                          16, ctypes.c_float(0.8), 1, ctypes.c_void_p(out.data_ptr()),
+                                          MAX_DESCS + 1, ctypes.c_void_p(cnt.data_ptr()), None)
+    assert st == _lib.SLM_INVALID_ARG
+    assert b"at most 4096" in L.slm_last_error()
