@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--scalar", action="store_true", help="FP32 kernel with all-scalar arithmetic")
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--serve", action="store_true", help="serving workload (Poisson view arrivals)")
+    ap.add_argument("--rates", default="10,50,200", help="serving arrival rates, views/s")
+    ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
     return ap.parse_args()
 
 
@@ -183,10 +186,124 @@ def run_reference(args):
     return 0
 
 
+def run_serve(args):
+    """Serving: zones of 48 positions x 3 cameras, n ~ log-uniform[500, 4000],
+    views arriving as a Poisson process; each view is matched against its
+    candidate_pairs partners already on the device."""
+    import oracle as O
+    from skylens_match import serve
+    z = serve.serving_zone(48, seed=args.seed + 2)
+    reqs = serve.zone_requests(z)
+    out = {"metric": "serving: image pairs/s and p50/p99 request latency (view arrival -> match lists on host)",
+           "config": {"workload": "serve_zone144", "views": len(z.counts), "pairs": int(len(z.pairs)),
+                      "n": "log-uniform [500, 4000]", "arrivals": "Poisson"}, "runs": []}
+    check = {}
+    for prec in ("bf16", "fp32"):
+        for rate in [float(r) for r in args.rates.split(",")]:
+            srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
+            res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate))
+            st = srv.stats()
+            srv.close()
+            npairs = sum(len(p) for _, p in reqs)
+            # bit-exactness against the oracle on a sample of requests
+            mism = 0
+            for k in range(0, len(reqs), 9):
+                v, pairs = reqs[k]
+                for (u, _), got in zip(pairs, res[k]):
+                    key = (u, v)
+                    if key not in check:
+                        check[key] = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=os.cpu_count() or 1)
+                    mism += not np.array_equal(got, check[key])
+            out["runs"].append({"precision": prec, "rate_views_per_s": rate, "p50_ms": float(np.percentile(lats, 50)),
+                                "p99_ms": float(np.percentile(lats, 99)), "mean_ms": float(lats.mean()),
+                                "pairs_per_s": npairs / wall, "wall_s": wall, "batches": st["batches"],
+                                "max_batch_requests": st["max_batch_requests"], "max_inflight": st["max_inflight"],
+                                "bit_exact_sample_mismatches": int(mism)})
+            print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
+    print(json.dumps(out), flush=True)
+    if args.json_out:
+        open(args.json_out, "w").write(json.dumps(out) + "\n")
+    return 0
+
+
+def run_pairs(args):
+    """Single-pair configurations: 800 x 800, 8192 x 8192 (BF16 vs FP32), and
+    32768 x 32768 (FP8 E4M3 shortlist); bit-exactness against the oracle,
+    distance-estimate error against FP64, rows settled exactly."""
+    import torch
+
+    import oracle as O
+    import skylens_match as sm
+    from skylens_match import synth
+    m = sm.Matcher()
+    ext = torch.cuda.ExternalStream(m.stream)
+    cases = [("pair800", synth.pair_800(0)), ("pair8192", synth.pair_large(8192, 0.5, 0.05, seed=2)),
+             ("pair32768", synth.pair_fp8(32768, seed=4))]
+    out = []
+    for name, (a, b) in cases:
+        ref = O.ratio_match_np(a, b, 0.8, True, threads=os.cpu_count() or 1)
+        st = m.store(len(a) + len(b), 2)
+        st.add_view(a)
+        st.add_view(b)
+        row = {"config": name, "na": len(a), "nb": len(b), "distances": len(a) * len(b), "precisions": {}}
+        for prec in ("fp32", "bf16", "fp8"):
+            if name == "pair32768" and prec == "fp32" and args.steps < 2:
+                continue
+            plan = st.plan([(0, 1)], 0.8, True, prec)
+            plan.launch()
+            got, _ = plan.results()
+            times = []
+            for _ in range(max(1, args.steps)):
+                with torch.cuda.stream(ext):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                plan.launch()
+                with torch.cuda.stream(ext):
+                    e1.record()
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            plan.results()
+            s = plan.stats
+            ms = float(np.median(times))
+            row["precisions"][prec] = {"ms": ms, "distances_per_s": len(a) * len(b) / (ms / 1e3),
+                                       "bit_exact": bool(np.array_equal(got, ref)), "matches": int(len(got)),
+                                       "rows_rescored_frac": s["rows_rescored"] / len(a),
+                                       "rows_recomputed_frac": s["rows_recomputed"] / len(a),
+                                       "cols_recomputed": s["cols_recomputed"],
+                                       "max_err_rescored_vs_f32": s["max_abs_err"]}
+            plan.close()
+        # distance-estimate error against FP64 on a 1024 x 1024 block of the pair
+        sub_a, sub_b = a[:1024], b[:1024]
+        d64 = O.dist_matrix_f64(sub_a, sub_b)
+        st2 = m.store(2048, 2)
+        st2.add_view(sub_a)
+        st2.add_view(sub_b)
+        for prec in ("bf16", "fp8"):
+            p = st2.plan([(0, 1)], 0.8, True, prec, variant=2)
+            p.launch()
+            p.results()
+            dt = p.debug_dump(1024, 1024)
+            row["precisions"][prec]["max_abs_err_vs_fp64_1024x1024"] = float(np.abs(dt - d64).max())
+            p.close()
+        st2.close()
+        st.close()
+        print(json.dumps(row), flush=True)
+        out.append(row)
+    if args.json_out:
+        open(args.json_out, "w").write("\n".join(json.dumps(r) for r in out) + "\n")
+    m.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
+    if args.pairs:
+        return run_pairs(args)
     import torch
 
     import oracle as O

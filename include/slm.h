@@ -213,6 +213,59 @@ slm_status slm_match_batch(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, u
                            int mutual, slm_precision prec, slm_pair *out, uint64_t cap, uint64_t *offsets,
                            slm_stats *stats);
 
+/* ------------------------------------------------------------- serving */
+
+/* A serving engine for views that stream in (a new zone filling up): each
+ * submission adds one view to a device-resident store and asks for its
+ * ratio_match against partners already submitted, as the pipeline's
+ * match_pairs (pipeline.rs:485-493) does for a whole region. A worker thread
+ * batches pending submissions every tick and admits a batch when one of
+ * `slots` streams is free and the batch fits that slot's share of the HBM
+ * budget; admitted batches run concurrently on their streams, so requests
+ * that arrive while others are on the GPU start as soon as a slot frees.
+ * A request's results do not depend on what it was batched with. */
+typedef struct slm_server slm_server;
+
+typedef struct {
+    int device;
+    uint64_t hbm_budget;      /* bytes for store + batches; 0: 80 % of free HBM */
+    uint64_t max_descs;       /* store capacity (descriptors) */
+    uint32_t max_views;       /* store capacity (views) */
+    uint32_t slots;           /* concurrent batches (streams); 0: 3 */
+    uint32_t max_batch_pairs; /* image pairs per batch; 0: 4096 */
+    uint32_t tick_us;         /* batching tick; 0: 200 us */
+    float ratio;              /* Lowe ratio (0.8 in the pipeline) */
+    int mutual;
+    slm_precision prec;
+} slm_server_opts;
+
+/* Placeholder for the submitted view itself in a submission's pair list. */
+#define SLM_SELF 0xffffffffu
+
+typedef struct {
+    uint64_t submitted, completed, batches, pairs, matches;
+    uint64_t max_batch_requests; /* most requests seen in one batch */
+    uint64_t max_inflight;       /* most batches on the GPU at once */
+    uint64_t bytes_in_use;
+} slm_server_stats;
+
+slm_status slm_server_create(const slm_server_opts *opts, slm_server **out);
+/* Waits for work in flight, then frees everything. */
+slm_status slm_server_destroy(slm_server *srv);
+/* Queue one view (n x 128 floats, copied before returning) and the image
+ * pairs to match once it is on the device: pairs[k] = (a, b) of view ids
+ * where one side is SLM_SELF (this view) and the other an id returned by an
+ * earlier submission. Returns the view's id and a ticket. */
+slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs, uint32_t np,
+                             uint32_t *view_id, uint64_t *ticket);
+/* Wait up to timeout_ms (0: poll) for a ticket. SLM_TIMEOUT if not done yet.
+ * On completion copies pair k's matches to out[offsets[k] .. offsets[k+1])
+ * (offsets has np+1 entries) and the request's latency (submit -> results on
+ * the host) to *latency_ms; the ticket is then released. */
+slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t timeout_ms, slm_pair *out, uint64_t cap,
+                           uint64_t *offsets, double *latency_ms);
+slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st);
+
 #ifdef __cplusplus
 }
 #endif

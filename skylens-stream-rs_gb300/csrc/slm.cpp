@@ -161,6 +161,8 @@ struct slm_store {
     // when the views change (lowp_version != version) or the format changes.
     int lowp_fp8 = -1;
     uint64_t lowp_version = ~0ull;
+    uint64_t epoch = 0, lowp_epoch = ~0ull;  // epoch bumps on clear
+    size_t lowp_views = 0;                   // views whose images are built
     DevBuf optiles, norms, qscale, vstats;
 };
 
@@ -703,6 +705,7 @@ extern "C" slm_status slm_store_clear(slm_store *st) {
     st->n.clear();
     st->rows_used = 0;
     st->version++;
+    st->epoch++;
     return SLM_OK;
 }
 
@@ -712,25 +715,32 @@ extern "C" uint32_t slm_store_num_views(slm_store *st) { return st ? (uint32_t)s
 
 namespace {
 
-// Build (or rebuild) the store's low-precision operand images.
+// Build the store's low-precision operand images: only the views appended
+// since the last build, unless the store was cleared or the format changed.
 slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
     if (st->lowp_version == st->version && st->lowp_fp8 == (int)fp8) return SLM_OK;
     slm_ctx *c = st->ctx;
     const uint64_t tiles = std::max<uint64_t>(st->max_rows / kTile, 1);
     const size_t tb = fp8 ? kFp8TileBytes : kBf16TileBytes;
+    const bool fresh = st->lowp_fp8 != (int)fp8 || st->lowp_epoch != st->epoch;
+    size_t first = fresh ? 0 : st->lowp_views;
     SLM_TRY(st->optiles.ensure(c, tiles * tb));
     SLM_TRY(st->norms.ensure(c, tiles * kTile * sizeof(float)));
     if (fp8) SLM_TRY(st->qscale.ensure(c, tiles * kTile * sizeof(float)));
-    const size_t nv = std::max<size_t>(st->row0.size(), 1);
+    const size_t nv = std::max<size_t>({st->row0.size(), (size_t)st->max_views, 1});
+    if (st->vstats.bytes < nv * sizeof(ViewStat)) first = 0;  // grows: statistics are rebuilt
     SLM_TRY(st->vstats.ensure(c, nv * sizeof(ViewStat)));
-    SLM_CU(cudaMemsetAsync(st->vstats.p, 0, nv * sizeof(ViewStat), s));
-    for (size_t v = 0; v < st->row0.size(); ++v)
+    if (first < st->row0.size())
+        SLM_CU(cudaMemsetAsync(st->vstats.as<ViewStat>() + first, 0, (st->row0.size() - first) * sizeof(ViewStat), s));
+    for (size_t v = first; v < st->row0.size(); ++v)
         launch_pack_lowp(st->raw.as<float>(), st->row0[v], st->n[v], (uint32_t)v, fp8 ? 1 : 0,
                          st->optiles.as<uint8_t>(), st->norms.as<float>(), st->qscale.as<float>(),
                          st->vstats.as<ViewStat>(), s);
     SLM_CU(cudaGetLastError());
     st->lowp_version = st->version;
     st->lowp_fp8 = fp8 ? 1 : 0;
+    st->lowp_epoch = st->epoch;
+    st->lowp_views = st->row0.size();
     return SLM_OK;
 }
 
@@ -1078,5 +1088,344 @@ extern "C" slm_status slm_plan_debug_dump(slm_plan *p, float *out, uint64_t cap)
     if (n > cap) return fail(SLM_CAPACITY, "need " + std::to_string(n) + " floats");
     SLM_CU(cudaStreamSynchronize(p->stream));
     if (n) SLM_CU(cudaMemcpy(out, p->d_dump.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return SLM_OK;
+}
+
+// ----------------------------------------------------------------- serving
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct ServeRequest {
+    uint64_t ticket = 0;
+    uint32_t view = 0;
+    std::vector<float> desc;         // host copy until uploaded
+    std::vector<slm_pair> pairs;     // SLM_SELF resolved to `view`
+    std::vector<slm_pair> matches;   // results, pair order
+    std::vector<uint64_t> offsets;   // np + 1
+    Clock::time_point t_submit, t_done;
+    bool uploaded = false, done = false;
+    slm_status status = SLM_OK;
+    std::string error;
+};
+
+struct ServeSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    slm_plan plan;
+    std::vector<ServeRequest *> reqs;
+    bool busy = false;
+};
+
+}  // namespace
+
+struct slm_server {
+    slm_ctx *ctx = nullptr;
+    slm_store *store = nullptr;
+    slm_server_opts opts{};
+    std::vector<ServeSlot *> slots;
+    cudaEvent_t upload_done = nullptr;  // last store upload
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<ServeRequest *> pending;
+    std::unordered_map<uint64_t, ServeRequest *> reqs;
+    uint64_t next_ticket = 1;
+    uint32_t next_view = 0;
+    uint64_t slot_budget = 0;
+    bool stop = false;
+    slm_server_stats stats{};
+};
+
+namespace {
+
+// Scratch a batch needs (matches plan_build_shortlist's and plan_build's
+// allocations; used for admission).
+uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, slm_precision prec) {
+    uint64_t rows = 0, cols = 0, na = 0, items = 0;
+    for (const slm_pair &p : pairs) {
+        const uint64_t a = p.i < st->n.size() ? st->n[p.i] : 0, b = p.j < st->n.size() ? st->n[p.j] : 0;
+        rows += pad_rows(a);
+        cols += pad_rows(b);
+        na += a;
+        items += (pad_rows(a) / kTile + 1) * 4;
+    }
+    uint64_t bytes = 64 + pairs.size() * (sizeof(PairMeta) + 16 + 8) + na * 16 + cols * 8;
+    if (prec == SLM_PREC_FP32)
+        bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
+    else
+        bytes += rows * (4 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 8;
+    return bytes + bytes / 4;  // DevBuf growth slack
+}
+
+void serve_fail_request(ServeRequest *r, slm_status s) {
+    r->status = s;
+    r->error = g_last_error;
+    r->done = true;
+    r->t_done = Clock::now();
+}
+
+// Worker: collect finished batches, then admit pending requests into free slots.
+void serve_loop(slm_server *srv) {
+    cudaSetDevice(srv->ctx->device);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    while (true) {
+        // Sleep one tick (completions are polled every tick) unless a new
+        // request can start right away.
+        srv->cv_work.wait_for(lk, std::chrono::microseconds(srv->opts.tick_us), [&] {
+            if (srv->stop) return true;
+            if (srv->pending.empty()) return false;
+            for (ServeSlot *s : srv->slots)
+                if (!s->busy) return true;
+            return false;
+        });
+        if (srv->stop) {
+            bool busy = false;
+            for (ServeSlot *s : srv->slots) busy |= s->busy;
+            if (!busy && srv->pending.empty()) break;
+        }
+        // 1. completions
+        for (ServeSlot *s : srv->slots) {
+            if (!s->busy || cudaEventQuery(s->done) != cudaSuccess) continue;
+            cudaGetLastError();
+            const uint32_t np = s->plan.np;
+            std::vector<uint64_t> off(np + 1);
+            std::vector<slm_pair> out(std::max<uint64_t>(s->plan.n_slots, 1));
+            slm_stats st{};
+            const slm_status rs = slm_plan_results(&s->plan, out.data(), out.size(), off.data(), &st);
+            uint32_t k = 0;
+            for (ServeRequest *r : s->reqs) {
+                if (rs != SLM_OK) {
+                    serve_fail_request(r, rs);
+                    k += (uint32_t)r->pairs.size();
+                    continue;
+                }
+                r->offsets.assign(1, 0);
+                for (size_t q = 0; q < r->pairs.size(); ++q, ++k) {
+                    r->matches.insert(r->matches.end(), out.begin() + off[k], out.begin() + off[k + 1]);
+                    r->offsets.push_back(r->matches.size());
+                }
+                r->done = true;
+                r->t_done = Clock::now();
+                srv->stats.completed++;
+                srv->stats.matches += r->matches.size();
+            }
+            s->reqs.clear();
+            s->busy = false;
+        }
+        srv->cv_done.notify_all();
+        // 2. admission: FIFO into each free slot while the batch fits
+        for (ServeSlot *s : srv->slots) {
+            if (s->busy || srv->pending.empty()) continue;
+            std::vector<ServeRequest *> take;
+            std::vector<slm_pair> pairs;
+            // upload views of requests about to be admitted (ordered on the store's stream)
+            while (!srv->pending.empty()) {
+                ServeRequest *r = srv->pending.front();
+                if (!take.empty() && pairs.size() + r->pairs.size() > srv->opts.max_batch_pairs) break;
+                if (!r->uploaded) {
+                    uint32_t id = 0;
+                    const slm_status us = store_append(srv->store, r->desc.data(), (uint32_t)(r->desc.size() / kDesc),
+                                                       false, srv->ctx->stream, &id);
+                    if (us != SLM_OK) {
+                        srv->pending.pop_front();
+                        serve_fail_request(r, us);
+                        continue;
+                    }
+                    r->uploaded = true;
+                    std::vector<float>().swap(r->desc);
+                }
+                std::vector<slm_pair> trial = pairs;
+                trial.insert(trial.end(), r->pairs.begin(), r->pairs.end());
+                if (!take.empty() && batch_bytes(srv->store, trial, srv->opts.prec) > srv->slot_budget) break;
+                pairs.swap(trial);
+                take.push_back(r);
+                srv->pending.pop_front();
+            }
+            if (take.empty()) continue;
+            // Low-precision images of the new views, on the upload stream, so
+            // every slot that waits for the upload also sees them.
+            if (srv->opts.prec != SLM_PREC_FP32) {
+                const slm_status ls = store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream);
+                if (ls != SLM_OK) {
+                    for (ServeRequest *r : take) serve_fail_request(r, ls);
+                    srv->cv_done.notify_all();
+                    continue;
+                }
+            }
+            cudaEventRecord(srv->upload_done, srv->ctx->stream);
+            cudaStreamWaitEvent(s->stream, srv->upload_done, 0);
+            slm_tune t{};
+            t.use_graph = 2;
+            slm_status ps = plan_init(&s->plan, srv->ctx, srv->store, pairs.data(), (uint32_t)pairs.size(),
+                                      srv->opts.ratio, srv->opts.mutual, srv->opts.prec, &t, s->stream);
+            if (ps == SLM_OK) ps = plan_launch_on(&s->plan, s->stream, false);
+            if (ps == SLM_OK && cudaEventRecord(s->done, s->stream) != cudaSuccess)
+                ps = fail(SLM_CUDA_ERROR, "cudaEventRecord");
+            if (ps != SLM_OK) {
+                for (ServeRequest *r : take) serve_fail_request(r, ps);
+                srv->cv_done.notify_all();
+                continue;
+            }
+            s->reqs = take;
+            s->busy = true;
+            srv->stats.batches++;
+            srv->stats.pairs += pairs.size();
+            srv->stats.max_batch_requests = std::max<uint64_t>(srv->stats.max_batch_requests, take.size());
+            uint64_t inflight = 0;
+            for (ServeSlot *q : srv->slots) inflight += q->busy;
+            srv->stats.max_inflight = std::max(srv->stats.max_inflight, inflight);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server **out) {
+    if (!opts || !out) return fail(SLM_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (opts->prec != SLM_PREC_FP32 && opts->prec != SLM_PREC_BF16 && opts->prec != SLM_PREC_FP8)
+        return fail(SLM_INVALID_ARG, "unknown precision");
+    SLM_TRY(validate_ratio(opts->ratio));
+    auto *srv = new (std::nothrow) slm_server();
+    if (!srv) return fail(SLM_OOM, "host allocation failed");
+    srv->opts = *opts;
+    if (!srv->opts.slots) srv->opts.slots = 3;
+    if (!srv->opts.max_batch_pairs) srv->opts.max_batch_pairs = 4096;
+    if (!srv->opts.tick_us) srv->opts.tick_us = 200;
+    slm_opts co{};
+    co.device = opts->device;
+    co.hbm_budget = opts->hbm_budget;
+    slm_status s = slm_ctx_create(&co, &srv->ctx);
+    if (s == SLM_OK && !opts->hbm_budget) srv->ctx->budget = srv->ctx->budget / 5 * 4;
+    if (s == SLM_OK) s = slm_store_create(srv->ctx, opts->max_descs, opts->max_views, &srv->store);
+    if (s == SLM_OK && cudaEventCreateWithFlags(&srv->upload_done, cudaEventDisableTiming) != cudaSuccess)
+        s = fail(SLM_CUDA_ERROR, "cudaEventCreate");
+    for (uint32_t k = 0; s == SLM_OK && k < srv->opts.slots; ++k) {
+        auto *sl = new ServeSlot();
+        srv->slots.push_back(sl);
+        if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess)
+            s = fail(SLM_CUDA_ERROR, "stream/event creation failed");
+        sl->plan.ctx = srv->ctx;
+    }
+    if (s != SLM_OK) {
+        std::string keep = g_last_error;
+        slm_server_destroy(srv);
+        g_last_error = keep;
+        return s;
+    }
+    const uint64_t used = srv->ctx->used.load();
+    const uint64_t left = srv->ctx->budget > used ? srv->ctx->budget - used : 0;
+    srv->slot_budget = left / srv->opts.slots;
+    srv->worker = std::thread(serve_loop, srv);
+    *out = srv;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_server_destroy(slm_server *srv) {
+    if (!srv) return SLM_OK;
+    if (srv->worker.joinable()) {
+        {
+            std::lock_guard<std::mutex> g(srv->mu);
+            srv->stop = true;
+        }
+        srv->cv_work.notify_all();
+        srv->worker.join();
+    }
+    if (srv->ctx) cudaSetDevice(srv->ctx->device);
+    for (ServeSlot *s : srv->slots) {
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        if (s->plan.ev0) {
+            cudaEventDestroy(s->plan.ev0);
+            s->plan.ev0 = nullptr;
+        }
+        if (s->plan.ev1) {
+            cudaEventDestroy(s->plan.ev1);
+            s->plan.ev1 = nullptr;
+        }
+        if (s->done) cudaEventDestroy(s->done);
+        if (s->stream) cudaStreamDestroy(s->stream);
+        delete s;
+    }
+    for (auto &kv : srv->reqs) delete kv.second;
+    if (srv->upload_done) cudaEventDestroy(srv->upload_done);
+    if (srv->store) slm_store_destroy(srv->store);
+    if (srv->ctx) slm_ctx_destroy(srv->ctx);
+    delete srv;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs,
+                                        uint32_t np, uint32_t *view_id, uint64_t *ticket) {
+    if (!srv || (n && !desc) || (np && !pairs) || !ticket) return fail(SLM_INVALID_ARG, "NULL argument");
+    auto *r = new (std::nothrow) ServeRequest();
+    if (!r) return fail(SLM_OOM, "host allocation failed");
+    r->desc.assign(desc, desc + (size_t)n * kDesc);
+    r->t_submit = Clock::now();
+    std::lock_guard<std::mutex> g(srv->mu);
+    if (srv->next_view >= srv->opts.max_views) {
+        delete r;
+        return fail(SLM_CAPACITY, "server store is full (max_views)");
+    }
+    r->view = srv->next_view;
+    for (uint32_t k = 0; k < np; ++k) {
+        slm_pair p = pairs[k];
+        if (p.i == SLM_SELF) p.i = r->view;
+        if (p.j == SLM_SELF) p.j = r->view;
+        if (p.i > r->view || p.j > r->view) {
+            delete r;
+            return fail(SLM_INVALID_ARG, "pair names a view not yet submitted");
+        }
+        r->pairs.push_back(p);
+    }
+    srv->next_view++;
+    r->ticket = srv->next_ticket++;
+    srv->reqs[r->ticket] = r;
+    srv->pending.push_back(r);
+    srv->stats.submitted++;
+    if (view_id) *view_id = r->view;
+    *ticket = r->ticket;
+    srv->cv_work.notify_all();
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t timeout_ms, slm_pair *out,
+                                      uint64_t cap, uint64_t *offsets, double *latency_ms) {
+    if (!srv || (cap && !out) || !offsets) return fail(SLM_INVALID_ARG, "NULL argument");
+    std::unique_lock<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return fail(SLM_INVALID_ARG, "unknown ticket");
+    ServeRequest *r = it->second;
+    if (!srv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return r->done; }))
+        return fail(SLM_TIMEOUT, "request not finished");
+    if (r->status != SLM_OK) {
+        const slm_status s = r->status;
+        g_last_error = r->error;
+        srv->reqs.erase(it);
+        delete r;
+        return s;
+    }
+    if (r->matches.size() > cap) return fail(SLM_CAPACITY, "need " + std::to_string(r->matches.size()) + " pairs");
+    std::copy(r->offsets.begin(), r->offsets.end(), offsets);
+    std::copy(r->matches.begin(), r->matches.end(), out);
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    srv->reqs.erase(it);
+    delete r;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st) {
+    if (!srv || !st) return fail(SLM_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(srv->mu);
+    *st = srv->stats;
+    st->bytes_in_use = srv->ctx->used.load();
     return SLM_OK;
 }

@@ -44,6 +44,21 @@ class SlmTune(ctypes.Structure):
     _fields_ = [("items_per_sm", c_u32), ("shortlist_k", c_u32), ("use_graph", c_u32), ("variant", c_u32)]
 
 
+class SlmServerOpts(ctypes.Structure):
+    _fields_ = [("device", c_int), ("hbm_budget", c_u64), ("max_descs", c_u64), ("max_views", c_u32),
+                ("slots", c_u32), ("max_batch_pairs", c_u32), ("tick_us", c_u32), ("ratio", c_f32),
+                ("mutual", c_int), ("prec", c_int)]
+
+
+class SlmServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_u64), ("completed", c_u64), ("batches", c_u64), ("pairs", c_u64),
+                ("matches", c_u64), ("max_batch_requests", c_u64), ("max_inflight", c_u64),
+                ("bytes_in_use", c_u64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SlmError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str):
         self.status = status
@@ -86,6 +101,12 @@ SIGNATURES = {
                                         P(ctypes.c_void_p)]),
     "slm_plan_bytes": (c_u64, [ctypes.c_void_p]),
     "slm_plan_debug_dump": (c_int, [ctypes.c_void_p, P(c_f32), c_u64]),
+    "slm_server_create": (c_int, [P(SlmServerOpts), P(ctypes.c_void_p)]),
+    "slm_server_destroy": (c_int, [ctypes.c_void_p]),
+    "slm_server_submit": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, P(SlmPair), c_u32, P(c_u32), P(c_u64)]),
+    "slm_server_wait": (c_int, [ctypes.c_void_p, c_u64, c_u32, P(SlmPair), c_u64, P(c_u64),
+                                P(ctypes.c_double)]),
+    "slm_server_stats_get": (c_int, [ctypes.c_void_p, P(SlmServerStats)]),
     "slm_match_batch": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int,
                                 P(SlmPair), c_u64, P(c_u64), P(SlmStats)]),
 }

@@ -1,0 +1,42 @@
+"""GPU: the serving engine (continuous batching over streaming views).
+
+Each request's match lists must be the same when it runs alone (one slot, one
+request at a time) and when it is batched with others and overlaps other
+batches on the device (three slots, a burst of requests, small batches), and
+must equal the oracle's ratio_match for every pair.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from skylens_match import serve, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp32"])
+def test_serving_results_same_alone_and_in_the_mix(prec):
+    z = synth.zone(positions=7, n_range=(150, 900), seed=21)
+    reqs = serve.zone_requests(z)
+    total = int(z.counts.sum())
+
+    alone = serve.Server(total, len(z.counts), prec, slots=1, max_batch_pairs=4096)
+    res_alone = []
+    for v, pairs in reqs:
+        _, t = alone.submit(z.view(v), pairs)
+        res_alone.append(alone.wait(t, cap=int(z.counts[v]) * max(1, len(pairs)))[0])
+    st_alone = alone.stats()
+    alone.close()
+
+    mix = serve.Server(total, len(z.counts), prec, slots=3, max_batch_pairs=6)
+    res_mix, lats, wall = serve.stream_zone(mix, z, rate=None)
+    st_mix = mix.stats()
+    mix.close()
+
+    assert st_alone["max_batch_requests"] == 1
+    assert st_mix["batches"] > 1 and st_mix["max_inflight"] >= 2, st_mix
+    for (v, pairs), ra, rm in zip(reqs, res_alone, res_mix):
+        assert len(ra) == len(rm) == len(pairs)
+        for (u, _), a_k, m_k in zip(pairs, ra, rm):
+            assert np.array_equal(a_k, m_k), (u, v)
+            assert np.array_equal(a_k, O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=8)), (u, v)
