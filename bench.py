@@ -271,18 +271,20 @@ def run_pairs(args):
                                        "cols_recomputed": s["cols_recomputed"],
                                        "max_err_rescored_vs_f32": s["max_abs_err"]}
             plan.close()
-        # distance-estimate error against FP64 on a 1024 x 1024 block of the pair
-        sub_a, sub_b = a[:1024], b[:1024]
+        # distance-estimate error against FP64 on a block of up to 1024 x 1024
+        nsub = min(1024, len(a), len(b))
+        sub_a, sub_b = a[:nsub], b[:nsub]
         d64 = O.dist_matrix_f64(sub_a, sub_b)
-        st2 = m.store(2048, 2)
+        st2 = m.store(2 * nsub, 2)
         st2.add_view(sub_a)
         st2.add_view(sub_b)
         for prec in ("bf16", "fp8"):
             p = st2.plan([(0, 1)], 0.8, True, prec, variant=2)
             p.launch()
             p.results()
-            dt = p.debug_dump(1024, 1024)
-            row["precisions"][prec]["max_abs_err_vs_fp64_1024x1024"] = float(np.abs(dt - d64).max())
+            dt = p.debug_dump(nsub, nsub)
+            row["precisions"][prec]["max_abs_err_vs_fp64"] = float(np.abs(dt - d64).max())
+            row["precisions"][prec]["err_block"] = f"{nsub}x{nsub}"
             p.close()
         st2.close()
         st.close()
