@@ -69,6 +69,61 @@ SLM_DEV float min32(const float (&d)[32]) {
     return fminf(min3f(x, y, z), fminf(m[9], m[10]));
 }
 
+typedef unsigned long long u64x;
+SLM_DEV u64x f2_pack(float lo, float hi) {
+    u64x d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+SLM_DEV float f2_lo(u64x v) { return __uint_as_float(static_cast<uint32_t>(v)); }
+SLM_DEV float f2_hi(u64x v) { return __uint_as_float(static_cast<uint32_t>(v >> 32)); }
+SLM_DEV u64x f2_add(u64x a, u64x b) {
+    u64x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Approximate-path arithmetic: one rounding, covered by the error bound.
+SLM_DEV u64x f2_fma(u64x a, u64x b, u64x c) {
+    u64x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// 32 lanes x 16 consecutive 32-bit TMEM columns (asynchronous until the wait).
+SLM_DEV void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+// Waits for this thread's TMEM loads; the registers are operands so no use
+// of them can be scheduled before the wait.
+SLM_DEV void tmem_wait_ld16(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+                   "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                   "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+}
+
+// Minimum of 16 values, and with the minima of its two groups of 8.
+SLM_DEV float min16(const float (&d)[16]) {
+    const float a = min3f(d[0], d[1], d[2]), b = min3f(d[3], d[4], d[5]), c = min3f(d[6], d[7], d[8]);
+    const float e = min3f(d[9], d[10], d[11]), f = min3f(d[12], d[13], d[14]);
+    return fminf(min3f(a, b, c), min3f(e, f, d[15]));
+}
+SLM_DEV float min16g(const float (&d)[16], float (&gm)[2]) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+        gm[q] = fminf(min3f(d[8 * q], d[8 * q + 1], d[8 * q + 2]),
+                      min3f(d[8 * q + 3], d[8 * q + 4], min3f(d[8 * q + 5], d[8 * q + 6], d[8 * q + 7])));
+    return fminf(gm[0], gm[1]);
+}
+
 // Minimum of 32 values plus the minima of its four groups of 8, so that a
 // rare hit below a threshold scans 8 values instead of 32.
 SLM_DEV float min32g(const float (&d)[32], float (&gm)[4]) {
@@ -251,7 +306,8 @@ struct SlSmem {
     float anorm[256];
     float athr[256];
     float ascale[256];
-    float colpart[2][8][128];
+    float colpart[2][8][128];  // [tile parity][(a tile, lane quarter)][column]
+    float2 rowx[256];          // pass 1: the second column half's row state
     uint64_t a_full, a_empty;
     uint64_t b_full[kSlStages], b_empty[kSlStages];
     uint64_t t_full[2], t_empty[2];
@@ -296,16 +352,16 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
 
     if (threadIdx.x == 0) {
         mbar_init(&S.a_full, 1);
-        mbar_init(&S.a_empty, 1 + 8);
+        mbar_init(&S.a_empty, 1 + kSlEpWarps);
         for (int s = 0; s < kSlStages; ++s) {
             mbar_init(&S.b_full[s], 1);
-            mbar_init(&S.b_empty[s], 1 + 8);
+            mbar_init(&S.b_empty[s], 1 + kSlEpWarps);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&S.t_full[b], 1);
-            mbar_init(&S.t_empty[b], 8);
+            mbar_init(&S.t_empty[b], kSlEpWarps);
         }
-        mbar_init(&S.ep_bar, 8);
+        mbar_init(&S.ep_bar, kSlEpWarps);
         S.abort_flag = 0;
         fence_mbar_init();
     }
@@ -397,9 +453,15 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
         }
     } else {
         // ---------------------------------------------------------- epilogue
-        const int ep = warp - 2;            // 0..7
-        const int at = ep >> 2;             // which a tile
-        const int q = warp & 3;             // TMEM lane quarter this warp may access
+        // 16 warps. Warp w reads TMEM lane quarter q = w % 4 (the only quarter
+        // it may access) of a tile `at`, columns [h*64, h*64 + 64) of every
+        // 128-column b tile; one thread per row, 16 columns per tcgen05.ld,
+        // the next load issued before the current chunk is reduced.
+        const int ep = warp - 2;                 // 0..15
+        const int q = warp & 3;
+        const int at = (ep >> 2) & 1;
+        const int h = ep >> 3;
+        const int combo = at * 4 + q;
         const int r = at * 128 + q * 32 + lane;  // row within the item
         const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0, eph = 0;
@@ -419,6 +481,8 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             if (lane == 0) mbar_arrive(&S.a_empty);
             float m1 = kInf, m2 = kInf;
             const bool own_row = sp.nchunk == 1;
+            const uint32_t ridx = sp.rbase + i;
+            uint2 *cand = g.rowcand + (size_t)ridx * kSlRowSlots + h * kSlHalfSlots;
             uint32_t ncand = 0;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
@@ -429,56 +493,64 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                 tc_fence_after();
                 if (active) {
                     const bool any_invalid_row = __any_sync(0xffffffffu, !rvalid);
-#pragma unroll 1
+                    const uint32_t tcol = tmem + lane_addr + (tb * 2 + at) * 128 + h * 64;
+                    uint32_t v[2][16];
+                    tmem_ld16(tcol, v[0]);
+#pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        uint32_t v[32];
-                        tmem_ld32(tmem + lane_addr + (tb * 2 + at) * 128 + c * 32, v);
-                        tmem_wait_ld();
-                        const uint32_t j0 = t * kTile + c * 32;
-                        float d[32];
-                        const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][c * 32]);
+                        uint32_t (&vc)[16] = v[c & 1];
+                        tmem_wait_ld16(vc);
+                        if (c + 1 < 4) tmem_ld16(tcol + (c + 1) * 16, v[(c + 1) & 1]);
+                        const uint32_t cb = h * 64 + c * 16;   // column within the tile
+                        const uint32_t j0 = t * kTile + cb;    // column within the pair
+                        float d[16];
+                        const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][cb]);
                         if constexpr (FP8) {
-                            const float4 *bs4 = reinterpret_cast<const float4 *>(&S.bscale[st][c * 32]);
+                            const float4 *bs4 = reinterpret_cast<const float4 *>(&S.bscale[st][cb]);
                             const float m2sa = -2.f * sa_i;
 #pragma unroll
-                            for (int k4 = 0; k4 < 8; ++k4) {
+                            for (int k4 = 0; k4 < 4; ++k4) {
                                 const float4 nb = bn4[k4], sb = bs4[k4];
                                 const float nbv[4] = {nb.x, nb.y, nb.z, nb.w}, sbv[4] = {sb.x, sb.y, sb.z, sb.w};
 #pragma unroll
                                 for (int e = 0; e < 4; ++e)
-                                    d[4 * k4 + e] = fmaf(__uint_as_float(v[4 * k4 + e]), m2sa * sbv[e], na_i + nbv[e]);
+                                    d[4 * k4 + e] = fmaf(__uint_as_float(vc[4 * k4 + e]), m2sa * sbv[e], na_i + nbv[e]);
                             }
                         } else {
+                            const u64x na2 = f2_pack(na_i, na_i), m22 = f2_pack(-2.f, -2.f);
 #pragma unroll
-                            for (int k4 = 0; k4 < 8; ++k4) {
-                                const float4 nb = bn4[k4];
-                                const float nbv[4] = {nb.x, nb.y, nb.z, nb.w};
-#pragma unroll
-                                for (int e = 0; e < 4; ++e)
-                                    d[4 * k4 + e] = fmaf(__uint_as_float(v[4 * k4 + e]), -2.f, na_i + nbv[e]);
+                            for (int k4 = 0; k4 < 4; ++k4) {
+                                const ulonglong2 nb = *reinterpret_cast<const ulonglong2 *>(&bn4[k4]);
+                                const u64x w0 = f2_add(na2, nb.x), w1 = f2_add(na2, nb.y);
+                                const u64x d0 = f2_fma(f2_pack(__uint_as_float(vc[4 * k4]), __uint_as_float(vc[4 * k4 + 1])), m22, w0);
+                                const u64x d1 = f2_fma(f2_pack(__uint_as_float(vc[4 * k4 + 2]), __uint_as_float(vc[4 * k4 + 3])), m22, w1);
+                                d[4 * k4 + 0] = f2_lo(d0);
+                                d[4 * k4 + 1] = f2_hi(d0);
+                                d[4 * k4 + 2] = f2_lo(d1);
+                                d[4 * k4 + 3] = f2_hi(d1);
                             }
                         }
-                        if (j0 + 32 > pm.nb) {  // ragged last tile: padding columns never win
+                        if (j0 + 16 > pm.nb) {  // ragged last tile: padding columns never win
 #pragma unroll
-                            for (int k = 0; k < 32; ++k)
+                            for (int k = 0; k < 16; ++k)
                                 if (j0 + k >= pm.nb) d[k] = kInf;
                         }
                         if constexpr (PASS == 1) {
                             if (g.dump && item.pair == 0 && rvalid) {
 #pragma unroll
-                                for (int k = 0; k < 32; ++k)
+                                for (int k = 0; k < 16; ++k)
                                     if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = d[k];
                             }
-                            const float cm = min32(d);
+                            const float cm = min16(d);
                             m2 = fminf(m2, fmaxf(m1, cm));
                             m1 = fminf(m1, cm);
                             if (any_invalid_row) {
 #pragma unroll
-                                for (int k = 0; k < 32; ++k) d[k] = rvalid ? d[k] : kInf;
+                                for (int k = 0; k < 16; ++k) d[k] = rvalid ? d[k] : kInf;
                             }
-                            float4 *cp = reinterpret_cast<float4 *>(&S.colpart[tb][ep][c * 32]);
+                            float4 *cp = reinterpret_cast<float4 *>(&S.colpart[tb][combo][cb]);
 #pragma unroll
-                            for (int k4 = 0; k4 < 8; ++k4) {
+                            for (int k4 = 0; k4 < 4; ++k4) {
                                 float4 o;
                                 o.x = warp_min_f32(d[4 * k4 + 0]);
                                 o.y = warp_min_f32(d[4 * k4 + 1]);
@@ -488,20 +560,19 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                             }
                         } else {
                             if (thr_i > -kInf) {
-                                float gm[4];
-                                const float cm = min32g(d, gm);
+                                float gm[2];
+                                const float cm = min16g(d, gm);
                                 if (cm <= thr_i) {
-                                    const uint32_t ridx = sp.rbase + i;
-                                    uint2 *dst = g.rowcand + (size_t)ridx * kSlRowSlots;
 #pragma unroll
-                                    for (int q = 0; q < 4; ++q) {
-                                        if (gm[q] <= thr_i) {
+                                    for (int qq = 0; qq < 2; ++qq) {
+                                        if (gm[qq] <= thr_i) {
 #pragma unroll
-                                            for (int k = 8 * q; k < 8 * q + 8; ++k) {
+                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
                                                 if (d[k] <= thr_i) {
                                                     // one item owns the whole row unless its columns are split
-                                                    const uint32_t s = own_row ? ncand++ : atomicAdd(&g.rowcnt[ridx], 1u);
-                                                    if (s < kSlRowSlots) dst[s] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                    const uint32_t sl = own_row ? ncand++
+                                                                                : atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
+                                                    if (sl < kSlHalfSlots) cand[sl] = make_uint2(j0 + k, __float_as_uint(d[k]));
                                                 }
                                             }
                                         }
@@ -509,24 +580,24 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 }
                             }
                             if (rvalid) {
-                                const float4 *bt4 = reinterpret_cast<const float4 *>(&S.bthr[st][c * 32]);
-                                float x[32];
+                                const float4 *bt4 = reinterpret_cast<const float4 *>(&S.bthr[st][cb]);
+                                float x[16];
 #pragma unroll
-                                for (int k4 = 0; k4 < 8; ++k4) {
+                                for (int k4 = 0; k4 < 4; ++k4) {
                                     const float4 tt = bt4[k4];
                                     x[4 * k4 + 0] = d[4 * k4 + 0] - tt.x;
                                     x[4 * k4 + 1] = d[4 * k4 + 1] - tt.y;
                                     x[4 * k4 + 2] = d[4 * k4 + 2] - tt.z;
                                     x[4 * k4 + 3] = d[4 * k4 + 3] - tt.w;
                                 }
-                                float gm[4];
-                                const float xm = min32g(x, gm);
+                                float gm[2];
+                                const float xm = min16g(x, gm);
                                 if (xm <= 0.f) {
 #pragma unroll
-                                    for (int q = 0; q < 4; ++q) {
-                                        if (gm[q] <= 0.f) {
+                                    for (int qq = 0; qq < 2; ++qq) {
+                                        if (gm[qq] <= 0.f) {
 #pragma unroll
-                                            for (int k = 8 * q; k < 8 * q + 8; ++k)
+                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k)
                                                 if (x[k] <= 0.f) atomicAdd(&g.colcnt[sp.cbase + j0 + k], 1u);  // reduction
                                         }
                                     }
@@ -539,7 +610,7 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.t_empty[tb]);
                 if constexpr (PASS == 1) {
-                    // all 8 epilogue warps have stored their column partials of this tile
+                    // all 16 epilogue warps have stored their column partials of this tile
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&S.ep_bar);
                     if (!sl_wait(&S.ep_bar, eph, abort_flag, err)) {
@@ -547,11 +618,11 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                         break;
                     }
                     eph ^= 1;
-                    const int e = threadIdx.x - 64;
+                    const int e = threadIdx.x - 64;  // 0..511
                     if (e < 128) {
                         float m = kInf;
-                        for (int w = 0; w < 8; ++w)
-                            if ((w >> 2) < (int)item.nat) m = fminf(m, S.colpart[tb][w][e]);
+                        for (int cmb = 0; cmb < 8; ++cmb)
+                            if ((cmb >> 2) < (int)item.nat) m = fminf(m, S.colpart[tb][cmb][e]);
                         const uint32_t j = t * kTile + e;
                         if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(m));
                     }
@@ -564,9 +635,20 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             }
             if (!ok) break;
             if constexpr (PASS == 1) {
-                if (active) g.rowpart[(size_t)item.part * 256 + r] = make_float2(m1, m2);
+                // merge the two column halves of each row, then store the partial
+                if (h == 1 && active) S.rowx[r] = make_float2(m1, m2);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.ep_bar);
+                if (!sl_wait(&S.ep_bar, eph, abort_flag, err)) break;
+                eph ^= 1;
+                if (h == 0 && active) {
+                    const float2 o = S.rowx[r];
+                    m2 = fminf(fminf(m2, o.y), fmaxf(m1, o.x));
+                    m1 = fminf(m1, o.x);
+                    g.rowpart[(size_t)item.part * 256 + r] = make_float2(m1, m2);
+                }
             } else {
-                if (own_row && rvalid && thr_i > -kInf) g.rowcnt[sp.rbase + i] = ncand;
+                if (own_row && rvalid && thr_i > -kInf) g.rowcnt[2 * ridx + h] = ncand;
             }
         }
     }
@@ -689,8 +771,9 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
             push_scan(g, p, 0, i, 0);
             dec = kDecPending;
         } else if (g.rowthr[ridx] > -kInf) {
-            const uint32_t n = g.rowcnt[ridx];
-            if (n > kSlRowSlots) {
+            const uint32_t n0 = g.rowcnt[2 * ridx], n1 = g.rowcnt[2 * ridx + 1];
+            const uint32_t n = n0 + n1;
+            if (n0 > kSlHalfSlots || n1 > kSlHalfSlots) {
                 push_scan(g, p, 0, i, 0);
                 dec = kDecPending;
             } else {
@@ -698,7 +781,7 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
                 float a1 = kInf, a2 = kInf;
                 uint32_t j1 = 0xffffffffu;
                 for (uint32_t k = 0; k < n; ++k) {
-                    const uint2 e = S[k];
+                    const uint2 e = S[k < n0 ? k : kSlHalfSlots + (k - n0)];
                     const float v = __uint_as_float(e.y);
                     if (v < a1 || (v == a1 && e.x < j1)) {
                         a2 = a1;
@@ -761,21 +844,23 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
         const PairMeta pm = g.pairs[qe.pair];
         const SlPair sp = g.spairs[qe.pair];
         const uint32_t ridx = sp.rbase + qe.i;
-        const uint32_t n = g.rowcnt[ridx];
+        const uint32_t n0 = g.rowcnt[2 * ridx], n = n0 + g.rowcnt[2 * ridx + 1];
         const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
+        // entry k of S: slots [0, n0) of the first half, then the second half
+        auto slot = [&](uint32_t k) { return k < n0 ? k : kSlHalfSlots + (k - n0); };
         const float *a = g.raw + (size_t)(pm.a_row0 + qe.i) * kDesc;
         const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
         float e1 = kInf, e2 = kInf, ad = kInf, maxerr = 0.f;
         uint32_t ej = 0xffffffffu;
         for (uint32_t k0 = 0; k0 < n; k0 += 4) {
             const uint32_t k = k0 + grp;
-            const uint2 ent = S[k < n ? k : k0];
+            const uint2 ent = S[slot(k < n ? k : k0)];
             const float d = dist8(a, B + (size_t)ent.x * kDesc);
             // every lane merges the 4 results in slot order
 #pragma unroll
             for (uint32_t q = 0; q < 4; ++q) {
                 const float dq = __shfl_sync(0xffffffffu, d, q * 8);
-                const uint2 eq = S[k0 + q < n ? k0 + q : k0];
+                const uint2 eq = S[slot(k0 + q < n ? k0 + q : k0)];
                 if (k0 + q < n) {
                     const float approx = __uint_as_float(eq.y);
                     maxerr = fmaxf(maxerr, fabsf(dq - approx));

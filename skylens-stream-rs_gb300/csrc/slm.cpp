@@ -309,7 +309,7 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     SLM_TRY(p->d_colmin.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowthr.ensure(c, sizeof(float) * p->rows_pad));
     SLM_TRY(p->d_colthr.ensure(c, sizeof(float) * p->cols_pad));
-    SLM_TRY(p->d_rowcnt.ensure(c, sizeof(uint32_t) * p->rows_pad));
+    SLM_TRY(p->d_rowcnt.ensure(c, 2 * sizeof(uint32_t) * p->rows_pad));
     SLM_TRY(p->d_rowcand.ensure(c, sizeof(uint2) * kSlRowSlots * p->rows_pad));
     SLM_TRY(p->d_colcnt.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowdec.ensure(c, sizeof(uint32_t) * p->rows_pad));
@@ -385,7 +385,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
     if (p->prec != SLM_PREC_FP32) {
         slm_store *st = p->st;
         launch_fill_u32(p->d_colmin.as<uint32_t>(), p->cols_pad, 0xff800000u, s);  // encodes +inf
-        SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, sizeof(uint32_t) * p->rows_pad, s));
+        SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, 2 * sizeof(uint32_t) * p->rows_pad, s));
         SLM_CU(cudaMemsetAsync(p->d_colcnt.p, 0, sizeof(uint32_t) * p->cols_pad, s));
         SlArgs a{};
         a.optiles = st->optiles.as<uint8_t>();
@@ -1161,7 +1161,7 @@ uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, sl
     if (prec == SLM_PREC_FP32)
         bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
     else
-        bytes += rows * (4 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 8;
+        bytes += rows * (5 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 8;
     return bytes + bytes / 4;  // DevBuf growth slack
 }
 

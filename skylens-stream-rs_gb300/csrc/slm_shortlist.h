@@ -31,9 +31,11 @@
 
 namespace slm {
 
-constexpr int kSlRowSlots = 16;    // S capacity per row
+constexpr int kSlHalfSlots = 16;   // S capacity per row and column half
+constexpr int kSlRowSlots = 2 * kSlHalfSlots;
 constexpr int kSlStages = 4;       // b-tile ring depth
-constexpr int kSlThreads = 320;    // producer, MMA, 8 epilogue warps
+constexpr int kSlEpWarps = 16;     // epilogue warps
+constexpr int kSlThreads = 32 * (2 + kSlEpWarps);  // producer, MMA, epilogue
 
 // Operand tile sizes per 128 descriptors.
 constexpr uint32_t kBf16TileBytes = 128 * 128 * 2;  // 32 KiB, 128B-swizzled, K-major
@@ -95,7 +97,7 @@ struct SlArgs {
     uint32_t *colmin;            // pass 1: order-preserving encoding of c1
     float *rowthr;               // mid -> pass 2
     float *colthr;               // mid -> pass 2
-    uint32_t *rowcnt;            // pass 2
+    uint32_t *rowcnt;            // pass 2: two counters per row (column halves)
     uint2 *rowcand;              // (j, bits(d~))
     uint32_t *colcnt;            // |C| per column
     uint32_t *rowdec;            // finalize / rescore / scan
