@@ -494,13 +494,9 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                 if (active) {
                     const bool any_invalid_row = __any_sync(0xffffffffu, !rvalid);
                     const uint32_t tcol = tmem + lane_addr + (tb * 2 + at) * 128 + h * 64;
-                    uint32_t v[2][16];
-                    tmem_ld16(tcol, v[0]);
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        uint32_t (&vc)[16] = v[c & 1];
-                        tmem_wait_ld16(vc);
-                        if (c + 1 < 4) tmem_ld16(tcol + (c + 1) * 16, v[(c + 1) & 1]);
+                    // chunks of 16 columns, two per iteration: loads double-buffered,
+                    // the body kept at two copies (instruction-cache footprint)
+                    auto chunk = [&](const uint32_t (&vc)[16], int c) {
                         const uint32_t cb = h * 64 + c * 16;   // column within the tile
                         const uint32_t j0 = t * kTile + cb;    // column within the pair
                         float d[16];
@@ -604,6 +600,17 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 }
                             }
                         }
+                    };
+                    uint32_t v0[16], v1[16];
+                    tmem_ld16(tcol, v0);
+#pragma unroll 1
+                    for (int c = 0; c < 4; c += 2) {
+                        tmem_wait_ld16(v0);
+                        tmem_ld16(tcol + (c + 1) * 16, v1);
+                        chunk(v0, c);
+                        tmem_wait_ld16(v1);
+                        if (c + 2 < 4) tmem_ld16(tcol + (c + 2) * 16, v0);
+                        chunk(v1, c + 1);
                     }
                 }
                 tc_fence_before();
