@@ -69,6 +69,7 @@ typedef struct {
     float kernel_ms;            /* device time of the main matching kernel, last launch */
     float max_abs_err;          /* max |approx - exact| seen on rescored pairs */
     uint64_t kernel_launches;   /* kernels one launch of the batch runs */
+    float pass_ms[2];           /* BF16/FP8: tensor-core passes 1 and 2; FP32: [0] = exact kernel */
 } slm_stats;
 
 typedef struct slm_ctx slm_ctx;

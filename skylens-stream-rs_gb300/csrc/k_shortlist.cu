@@ -1067,21 +1067,27 @@ cudaError_t init_shortlist_kernels() {
                                 (int)sl_smem_bytes<true>());
 }
 
-int shortlist_kernel_count() { return 7; }
-
-void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s) {
+void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
     const int grid = (int)(a.n_items < (uint32_t)sms ? a.n_items : (uint32_t)sms);
-    if (a.fp8) {
-        if (grid) sl_pass_kernel<1, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+    if (!grid) return;
+    if (pass == 1) {
+        if (a.fp8)
+            sl_pass_kernel<1, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+        else
+            sl_pass_kernel<1, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
     } else {
-        if (grid) sl_pass_kernel<1, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
+        if (a.fp8)
+            sl_pass_kernel<2, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+        else
+            sl_pass_kernel<2, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
     }
+}
+
+void launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
     if (a.npairs) sl_mid_kernel<<<a.npairs, 256, 0, s>>>(a);
-    if (a.fp8) {
-        if (grid) sl_pass_kernel<2, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
-    } else {
-        if (grid) sl_pass_kernel<2, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
-    }
+}
+
+void launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     if (a.npairs) sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
     sl_rescore_kernel<<<2 * sms, 256, 0, s>>>(a);
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);

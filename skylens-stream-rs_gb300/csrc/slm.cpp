@@ -191,7 +191,8 @@ struct slm_plan {
     bool dump = false;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel(s)
+    cudaEvent_t evp[3] = {nullptr, nullptr, nullptr};  // shortlist: after pass 1, mid, pass 2
     uint64_t kernels = 0;                      // kernels per launch
     void *graph_optiles = nullptr;             // store buffer the captured graph reads
     bool launched = false;
@@ -200,6 +201,8 @@ struct slm_plan {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (cudaEvent_t &e : evp)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -417,9 +420,15 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.slots = p->d_slots.as<uint2>();
         a.counts = p->d_counts.as<uint32_t>();
         SLM_CU(record_event(p->ev0, s));
-        launch_shortlist(a, p->ctx->sms, s);
+        launch_shortlist_pass(a, 1, p->ctx->sms, s);
+        SLM_CU(record_event(p->evp[0], s));
+        launch_shortlist_mid(a, s);
+        SLM_CU(record_event(p->evp[1], s));
+        launch_shortlist_pass(a, 2, p->ctx->sms, s);
+        SLM_CU(record_event(p->evp[2], s));
+        launch_shortlist_tail(a, p->ctx->sms, s);
         SLM_CU(record_event(p->ev1, s));
-        p->kernels = 1 + (uint64_t)shortlist_kernel_count() + 2;
+        p->kernels = 1 + 7 + 2;
         uint64_t *offsets = p->d_offsets.as<uint64_t>();
         launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
         launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
@@ -576,6 +585,12 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
     if (p->launched && p->ev0 && p->ev1) {
         float ms = 0;
         if (cudaEventElapsedTime(&ms, p->ev0, p->ev1) == cudaSuccess) st->kernel_ms = ms;
+        if (p->prec != SLM_PREC_FP32) {
+            if (cudaEventElapsedTime(&ms, p->ev0, p->evp[0]) == cudaSuccess) st->pass_ms[0] = ms;
+            if (cudaEventElapsedTime(&ms, p->evp[1], p->evp[2]) == cudaSuccess) st->pass_ms[1] = ms;
+        } else {
+            st->pass_ms[0] = st->kernel_ms;
+        }
         cudaGetLastError();
     }
     return SLM_OK;
@@ -782,6 +797,8 @@ slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
     }
     if (!p->ev0) SLM_CU(cudaEventCreate(&p->ev0));
     if (!p->ev1) SLM_CU(cudaEventCreate(&p->ev1));
+    for (cudaEvent_t &e : p->evp)
+        if (!e) SLM_CU(cudaEventCreate(&e));
     if (use_graph) {
         if (!p->exec) {
             SLM_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));

@@ -120,10 +120,11 @@ void launch_pack_lowp(const float *raw, uint32_t row0, uint32_t n, uint32_t view
 // Kernel image / attribute set-up (outside stream capture).
 cudaError_t init_shortlist_kernels();
 
-// The pipeline of one shortlist launch (after counters are cleared).
-void launch_shortlist(const SlArgs &a, int sms, cudaStream_t s);
+// The pipeline of one shortlist launch (after counters are cleared):
+// pass 1, mid, pass 2, then finalize / rescore / scan / compact.
+void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s);
+void launch_shortlist_mid(const SlArgs &a, cudaStream_t s);
+void launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s);
 
-// Number of kernels launch_shortlist enqueues.
-int shortlist_kernel_count();
 
 }  // namespace slm

@@ -37,6 +37,7 @@ pub struct slm_stats {
     pub kernel_ms: f32,
     pub max_abs_err: f32,
     pub kernel_launches: u64,
+    pub pass_ms: [f32; 2],
 }
 
 #[repr(C)]

@@ -25,10 +25,12 @@ class SlmPair(ctypes.Structure):
 class SlmStats(ctypes.Structure):
     _fields_ = [("pairs", c_u64), ("distances", c_u64), ("matches", c_u64), ("rows_recomputed", c_u64),
                 ("cols_recomputed", c_u64), ("rows_rescored", c_u64), ("kernel_ms", c_f32),
-                ("max_abs_err", c_f32), ("kernel_launches", c_u64)]
+                ("max_abs_err", c_f32), ("kernel_launches", c_u64), ("pass_ms", c_f32 * 2)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["pass_ms"] = list(d["pass_ms"])
+        return d
 
 
 class SlmOpts(ctypes.Structure):
