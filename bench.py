@@ -330,9 +330,15 @@ def main():
     ext = torch.cuda.ExternalStream(m.stream)
     store = m.store(n_rows, len(z.counts))
     store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
-    variant = 1 if args.scalar else 0
-    plan = store.plan(z.pairs, 0.8, True, prec, variant=variant)
-    plan_fp32 = plan if prec == "fp32" else store.plan(z.pairs, 0.8, True, "fp32", variant=variant)
+    # Both arms use settings chosen by the library's autotuner on this batch.
+    tuned = {}
+    for pr in ([prec] if prec == "fp32" else [prec, "fp32"]):
+        tuned[pr] = store.autotune(z.pairs, 0.8, True, pr)[0]
+    if args.scalar:
+        plan = store.plan(z.pairs, 0.8, True, prec, variant=1)
+    else:
+        plan = store.plan(z.pairs, 0.8, True, prec, autotune=True)
+    plan_fp32 = plan if prec == "fp32" else store.plan(z.pairs, 0.8, True, "fp32", autotune=True)
 
     # ---- correctness against the oracle on a sample of pairs
     plan.launch()
@@ -464,7 +470,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[prec],
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": prec, "views": len(z.counts), "pairs": int(len(z.pairs)),
+            "config": {"workload": WORKLOAD, "precision": prec, "tuned": tuned, "views": len(z.counts),
+                       "pairs": int(len(z.pairs)),
                        "distances": dist_n, "descriptors": n_rows, "ratio": 0.8, "mutual": True,
                        "l2": "flushed between steps (512 MiB write, outside the events)",
                        "parallelism": f"replicas{ws}"},

@@ -184,7 +184,18 @@ typedef struct {
                                (default), 1 all scalar; both IEEE, bit-exact.
                                BF16/FP8: 2 keeps the approximate distances of pair 0
                                for slm_plan_debug_dump (diagnostics) */
+    uint32_t row_tiles;     /* BF16/FP8: 128-row a tiles per work item, 1 or 2 (0: 2) */
+    uint32_t autotune;      /* 1: use the context's tuned setting for this batch shape
+                               (slm_autotune), tuning it first if none is cached */
 } slm_tune;
+
+/* Time a small grid of settings (row tiles per item, items per SM, FP32
+ * arithmetic variant) on this batch with CUDA events and return the fastest in
+ * *best (and its time in *best_ms). The result is cached in the context under
+ * the batch's shape (precision, mean rows per pair, pair count), which plans
+ * with slm_tune.autotune = 1 use. Launches the batch several times. */
+slm_status slm_autotune(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio, int mutual,
+                        slm_precision prec, slm_tune *best, float *best_ms);
 
 /* Plan the matching of np image pairs (view-id pairs in `pairs`, the
  * match_pairs loop of pipeline.rs:485-493) on a store. The plan owns its

@@ -652,7 +652,8 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                     const float2 o = S.rowx[r];
                     m2 = fminf(fminf(m2, o.y), fmaxf(m1, o.x));
                     m1 = fminf(m1, o.x);
-                    g.rowpart[(size_t)item.part * 256 + r] = make_float2(m1, m2);
+                    // slot = row within its 256-row group (items of one 128-row tile start mid-group)
+                    g.rowpart[(size_t)item.part * 256 + (i & 255u)] = make_float2(m1, m2);
                 }
             } else {
                 if (own_row && rvalid && thr_i > -kInf) g.rowcnt[2 * ridx + h] = ncand;

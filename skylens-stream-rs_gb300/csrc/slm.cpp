@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -75,6 +76,7 @@ struct slm_ctx {
     std::mutex mu;
     std::vector<Workspace *> idle;  // single-pair workspaces not in use
     std::vector<Workspace *> all;
+    std::map<uint64_t, slm_tune> tuned;  // autotuned settings by batch shape
 
     slm_status alloc(void **p, size_t bytes) {
         *p = nullptr;
@@ -281,13 +283,17 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
         sp.nchunk = chunks;
         sp.part_base = (uint32_t)part;
         if (m.na && m.nb) {
+            // row_tiles == 1: one 128-row a tile per item (M = 128 per CTA)
+            const uint32_t per = p->tune.row_tiles == 1 ? 1u : 2u;
             const uint32_t ns = (rt_n + 1) / 2;
             for (uint32_t s2 = 0; s2 < ns; ++s2)
+                for (uint32_t half = 0; half < 2 / per; ++half)
                 for (uint32_t ch = 0; ch < chunks; ++ch) {
                     SlItem it{};
                     it.pair = k;
-                    it.rt0 = 2 * s2;
-                    it.nat = std::min(2u, rt_n - 2 * s2);
+                    it.rt0 = 2 * s2 + half;
+                    if (it.rt0 >= rt_n) continue;
+                    it.nat = std::min(per, rt_n - it.rt0);
                     it.ct0 = (uint32_t)((uint64_t)ct_n * ch / chunks);
                     it.ct1 = (uint32_t)((uint64_t)ct_n * (ch + 1) / chunks);
                     it.part = (uint32_t)(part + s2 * chunks + ch);
@@ -823,6 +829,78 @@ slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
 
 }  // namespace
 
+namespace {
+
+uint64_t tune_key(const slm_store *st, const slm_pair *pairs, uint32_t np, int mutual, slm_precision prec) {
+    uint64_t rows = 0;
+    for (uint32_t k = 0; k < np; ++k) rows += pairs[k].i < st->n.size() ? st->n[pairs[k].i] : 0;
+    auto lg = [](uint64_t x) {
+        uint64_t b = 0;
+        while (x > 1) x >>= 1, ++b;
+        return b;
+    };
+    return ((uint64_t)prec << 16) | ((uint64_t)(mutual ? 1 : 0) << 15) | (lg(np ? rows / np : 0) << 8) | lg(np);
+}
+
+}  // namespace
+
+extern "C" slm_status slm_autotune(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
+                                   int mutual, slm_precision prec, slm_tune *best, float *best_ms) {
+    if (!c || !st || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
+    SLM_TRY(validate_ratio(ratio));
+    SLM_TRY(ctx_check_device(c));
+    std::vector<slm_tune> grid;
+    const uint32_t ips[3] = {2, 4, 8};
+    for (uint32_t a = 0; a < 2; ++a)
+        for (uint32_t ipsm : ips) {
+            slm_tune t{};
+            t.use_graph = 2;
+            t.items_per_sm = ipsm;
+            if (prec == SLM_PREC_FP32)
+                t.variant = a;  // 0 packed f32x2 sub/add, 1 scalar
+            else
+                t.row_tiles = a + 1;
+            grid.push_back(t);
+        }
+    std::unique_ptr<slm_plan> p(new (std::nothrow) slm_plan());
+    if (!p) return fail(SLM_OOM, "host allocation failed");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SLM_CU(cudaEventCreate(&e0));
+    SLM_CU(cudaEventCreate(&e1));
+    float best_t = 3.4e38f;
+    slm_tune best_tune = grid[0];
+    slm_status status = SLM_OK;
+    for (const slm_tune &t : grid) {
+        status = plan_init(p.get(), c, st, pairs, np, ratio, mutual, prec, &t, c->stream);
+        if (status != SLM_OK) break;
+        status = plan_launch_on(p.get(), c->stream, false);  // warm-up
+        float tmin = 3.4e38f;
+        for (int rep = 0; rep < 3 && status == SLM_OK; ++rep) {
+            cudaEventRecord(e0, c->stream);
+            status = plan_launch_on(p.get(), c->stream, false);
+            cudaEventRecord(e1, c->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) status = fail(SLM_CUDA_ERROR, "autotune timing");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tmin = std::min(tmin, ms);
+        }
+        if (status != SLM_OK) break;
+        SLM_TRY(check_status_word(p.get()));
+        if (tmin < best_t) best_t = tmin, best_tune = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != SLM_OK) return status;
+    best_tune.use_graph = 1;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        c->tuned[tune_key(st, pairs, np, mutual, prec)] = best_tune;
+    }
+    if (best) *best = best_tune;
+    if (best_ms) *best_ms = best_t;
+    return SLM_OK;
+}
+
 extern "C" slm_status slm_plan_create(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                                       int mutual, slm_precision prec, const slm_tune *tune, slm_plan **out) {
     if (!c || !st || !out || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
@@ -831,9 +909,22 @@ extern "C" slm_status slm_plan_create(slm_ctx *c, slm_store *st, const slm_pair 
     SLM_TRY(validate_ratio(ratio));
     *out = nullptr;
     SLM_TRY(ctx_check_device(c));
+    slm_tune t = tune ? *tune : slm_tune{};
+    if (t.autotune) {
+        const uint64_t key = tune_key(st, pairs, np, mutual, prec);
+        bool have = false;
+        {
+            std::lock_guard<std::mutex> g(c->mu);
+            auto it = c->tuned.find(key);
+            if (it != c->tuned.end()) have = true, t = it->second;
+        }
+        if (!have) SLM_TRY(slm_autotune(c, st, pairs, np, ratio, mutual, prec, &t, nullptr));
+        if (tune && tune->use_graph) t.use_graph = tune->use_graph;
+        t.autotune = 0;
+    }
     auto *p = new (std::nothrow) slm_plan();
     if (!p) return fail(SLM_OOM, "host allocation failed");
-    slm_status s = plan_init(p, c, st, pairs, np, ratio, mutual, prec, tune, c->stream);
+    slm_status s = plan_init(p, c, st, pairs, np, ratio, mutual, prec, &t, c->stream);
     if (s != SLM_OK) {
         std::string keep = g_last_error;
         delete p;

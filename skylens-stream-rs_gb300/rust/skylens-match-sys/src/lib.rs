@@ -68,6 +68,8 @@ pub struct slm_tune {
     pub shortlist_k: u32,
     pub use_graph: u32,
     pub variant: u32,
+    pub row_tiles: u32,
+    pub autotune: u32,
 }
 
 #[repr(C)]
@@ -122,6 +124,8 @@ extern "C" {
     pub fn slm_plan_results(p: *mut slm_plan, out: *mut slm_pair, cap: u64, offsets: *mut u64, st: *mut slm_stats)
                             -> SlmStatus;
     pub fn slm_plan_bytes(p: *mut slm_plan) -> u64;
+    pub fn slm_autotune(ctx: *mut slm_ctx, st: *mut slm_store, pairs: *const slm_pair, np: u32, ratio: f32,
+                        mutual: c_int, prec: SlmPrecision, best: *mut slm_tune, best_ms: *mut f32) -> SlmStatus;
     pub fn slm_match_batch(ctx: *mut slm_ctx, st: *mut slm_store, pairs: *const slm_pair, np: u32, ratio: f32,
                            mutual: c_int, prec: SlmPrecision, out: *mut slm_pair, cap: u64, offsets: *mut u64,
                            stats: *mut slm_stats) -> SlmStatus;

@@ -43,7 +43,11 @@ class SlmPairSchedule(ctypes.Structure):
 
 
 class SlmTune(ctypes.Structure):
-    _fields_ = [("items_per_sm", c_u32), ("shortlist_k", c_u32), ("use_graph", c_u32), ("variant", c_u32)]
+    _fields_ = [("items_per_sm", c_u32), ("shortlist_k", c_u32), ("use_graph", c_u32), ("variant", c_u32),
+                ("row_tiles", c_u32), ("autotune", c_u32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class SlmServerOpts(ctypes.Structure):
@@ -109,6 +113,8 @@ SIGNATURES = {
     "slm_server_wait": (c_int, [ctypes.c_void_p, c_u64, c_u32, P(SlmPair), c_u64, P(c_u64),
                                 P(ctypes.c_double)]),
     "slm_server_stats_get": (c_int, [ctypes.c_void_p, P(SlmServerStats)]),
+    "slm_autotune": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int, P(SlmTune),
+                             P(c_f32)]),
     "slm_match_batch": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int,
                                 P(SlmPair), c_u64, P(c_u64), P(SlmStats)]),
 }

@@ -187,22 +187,34 @@ class DescriptorStore:
             pass
 
     def plan(self, pairs, ratio: float = 0.8, mutual: bool = True, precision="fp32", *, items_per_sm: int = 0,
-             shortlist_k: int = 0, use_graph: int = 1, variant: int = 0) -> "BatchPlan":
-        return BatchPlan(self, pairs, ratio, mutual, precision, items_per_sm, shortlist_k, use_graph, variant)
+             shortlist_k: int = 0, use_graph: int = 1, variant: int = 0, row_tiles: int = 0,
+             autotune: bool = False) -> "BatchPlan":
+        return BatchPlan(self, pairs, ratio, mutual, precision, items_per_sm, shortlist_k, use_graph, variant,
+                         row_tiles, autotune)
+
+    def autotune(self, pairs, ratio: float = 0.8, mutual: bool = True, precision="bf16"):
+        """Time a grid of settings on this batch; returns (best setting dict, best ms)."""
+        pr = _pairs_array(pairs)
+        t = SlmTune()
+        ms = ctypes.c_float()
+        check(self._L.slm_autotune(self.m.handle, self._h, pr.ctypes.data_as(ctypes.POINTER(SlmPair)), len(pr),
+                                   ctypes.c_float(ratio), int(bool(mutual)), _prec(precision), ctypes.byref(t),
+                                   ctypes.byref(ms)), "slm_autotune")
+        return t.as_dict(), ms.value
 
 
 class BatchPlan:
     """A planned batch of image pairs (pipeline.rs:485-493), replayed as one CUDA graph."""
 
     def __init__(self, store: DescriptorStore, pairs, ratio, mutual, precision, items_per_sm=0, shortlist_k=0,
-                 use_graph=1, variant=0):
+                 use_graph=1, variant=0, row_tiles=0, autotune=False):
         self.store = store
         self._L = store._L
         pr = _pairs_array(pairs)
         self.np = len(pr)
         self.total_rows = int(sum(store.counts[int(u)] for u, _ in pr)) if len(pr) else 0
         self.distances = int(sum(store.counts[int(u)] * store.counts[int(v)] for u, v in pr)) if len(pr) else 0
-        tune = SlmTune(items_per_sm, shortlist_k, use_graph, variant)
+        tune = SlmTune(items_per_sm, shortlist_k, use_graph, variant, row_tiles, int(bool(autotune)))
         h = ctypes.c_void_p()
         check(self._L.slm_plan_create(store.m.handle, store.handle, pr.ctypes.data_as(ctypes.POINTER(SlmPair)),
                                       self.np, ctypes.c_float(ratio), int(bool(mutual)), _prec(precision),

@@ -204,3 +204,34 @@ def test_zone_batch_fp32_variants(matcher, variant):
         assert np.array_equal(per[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16)), k
     plan.close()
     st.close()
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8"])
+def test_zone_batch_one_row_tile_per_item(matcher, prec):
+    """Items of one 128-row tile (M = 128 per CTA) give the same lists."""
+    z = synth.zone(positions=8, n_range=(100, 1300), seed=13)
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    st.add_views_packed(z.desc, z.offsets, z.counts)
+    plan = st.plan(z.pairs, 0.8, True, prec, row_tiles=1)
+    plan.launch()
+    per = plan.per_pair()
+    for k, (u, v) in enumerate(z.pairs):
+        assert np.array_equal(per[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16)), k
+    plan.close()
+    st.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_autotuned_plan(matcher, prec):
+    z = synth.zone(positions=6, n_range=(200, 1000), seed=17)
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    st.add_views_packed(z.desc, z.offsets, z.counts)
+    best, ms = st.autotune(z.pairs, 0.8, True, prec)
+    assert ms > 0 and best["items_per_sm"] in (2, 4, 8)
+    plan = st.plan(z.pairs, 0.8, True, prec, autotune=True)
+    plan.launch()
+    per = plan.per_pair()
+    for k, (u, v) in enumerate(z.pairs):
+        assert np.array_equal(per[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16)), k
+    plan.close()
+    st.close()
