@@ -126,6 +126,20 @@ class Clocks:
                 "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
 
 
+def reduce_over_ranks(ms: float, units: int, dist, device=None):
+    """Whole-job rate over replicas: every rank timed its own zone; the job time
+    is the slowest rank's (MAX) and the work is the sum over ranks (SUM).
+    Returns (max ms, total units, units per second)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return ms, units, units / (ms / 1e3)
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(u.item()), float(u.item()) / (float(t.item()) / 1e3)
+
+
 def peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -391,11 +405,7 @@ def main():
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
     ms = float(np.mean(step_ms))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * len(z.pairs) / (ms / 1e3)
+    ms, _, value = reduce_over_ranks(ms, len(z.pairs), dist, device="cuda" if dist else None)
 
     fp32 = None
     if plan_fp32 is not plan:

@@ -60,6 +60,40 @@ __global__ void __launch_bounds__(256) pack_fp32_kernel(const float *__restrict_
     }
 }
 
+// Many views at once: one CTA per entry of a tile table
+// {first store row of the view, rows of the view, tile within the view, view}.
+__global__ void __launch_bounds__(256) pack_fp32_tiles_kernel(const uint4 *__restrict__ tab,
+                                                              const float *__restrict__ raw,
+                                                              float *__restrict__ tiled) {
+    const uint4 e = tab[blockIdx.x];
+    __shared__ float sm[32][kDesc + 1];
+    const float *src = raw + (size_t)e.x * kDesc;
+    float *dst = tiled + (size_t)(e.x / kTile + e.z) * kTileFloats;
+    for (int g = 0; g < 4; ++g) {
+        const uint32_t r0 = e.z * kTile + g * 32;
+        for (int q = threadIdx.x; q < 32 * 32; q += 256) {
+            const int r = q >> 5, c = q & 31;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + r < e.y) v = reinterpret_cast<const float4 *>(src + (size_t)(r0 + r) * kDesc)[c];
+            sm[r][4 * c + 0] = v.x;
+            sm[r][4 * c + 1] = v.y;
+            sm[r][4 * c + 2] = v.z;
+            sm[r][4 * c + 3] = v.w;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < 32 * kDesc; q += 256) {
+            const int slot = q >> 5, r = q & 31;
+            const int k = 8 * (slot & 15) + (slot >> 4);  // inverse of perm_slot
+            dst[slot * kTile + g * 32 + r] = sm[r][k];
+        }
+        __syncthreads();
+    }
+}
+
+void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw, float *tiled, cudaStream_t s) {
+    if (ntiles) pack_fp32_tiles_kernel<<<ntiles, 256, 0, s>>>(tab, raw, tiled);
+}
+
 void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0, cudaStream_t s) {
     const uint32_t tiles = (n + kTile - 1) / kTile;
     if (tiles) pack_fp32_kernel<<<tiles, 256, 0, s>>>(src, n, tiled, tile0);

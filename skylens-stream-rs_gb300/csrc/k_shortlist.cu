@@ -163,12 +163,13 @@ SLM_DEV float sq_dist_spec(const float *__restrict__ p, const float *__restrict_
 // image (K-major, 128B swizzle: 16-byte chunk c of row r at c ^ (r % 8)),
 // f32 squared norms, and the view's error statistics.
 template <bool FP8>
-__global__ void __launch_bounds__(128) pack_lowp_kernel(const float *__restrict__ raw, uint32_t row0, uint32_t n,
-                                                        uint32_t view, uint8_t *__restrict__ optiles,
-                                                        float *__restrict__ norms, float *__restrict__ qscale,
-                                                        ViewStat *__restrict__ vstats) {
+__global__ void __launch_bounds__(128) pack_lowp_kernel(const uint4 *__restrict__ tab, const float *__restrict__ raw,
+                                                        uint8_t *__restrict__ optiles, float *__restrict__ norms,
+                                                        float *__restrict__ qscale, ViewStat *__restrict__ vstats) {
+    const uint4 te = tab[blockIdx.x];  // {first store row of the view, rows, tile within the view, view}
+    const uint32_t row0 = te.x, n = te.y, view = te.w;
     const uint32_t r = threadIdx.x;
-    const uint32_t tile = blockIdx.x;
+    const uint32_t tile = te.z;
     const uint32_t row = tile * kTile + r;  // row within the view
     const bool valid = row < n;
     const float *src = raw + (size_t)(row0 + row) * kDesc;
@@ -265,14 +266,13 @@ __global__ void __launch_bounds__(128) pack_lowp_kernel(const float *__restrict_
     }
 }
 
-void launch_pack_lowp(const float *raw, uint32_t row0, uint32_t n, uint32_t view, int fp8, uint8_t *optiles,
-                      float *norms, float *qscale, ViewStat *vstats, cudaStream_t s) {
-    const uint32_t tiles = (n + kTile - 1) / kTile;
-    if (!tiles) return;
+void launch_pack_lowp(const uint4 *tab, uint32_t ntiles, const float *raw, int fp8, uint8_t *optiles, float *norms,
+                      float *qscale, ViewStat *vstats, cudaStream_t s) {
+    if (!ntiles) return;
     if (fp8)
-        pack_lowp_kernel<true><<<tiles, 128, 0, s>>>(raw, row0, n, view, optiles, norms, qscale, vstats);
+        pack_lowp_kernel<true><<<ntiles, 128, 0, s>>>(tab, raw, optiles, norms, qscale, vstats);
     else
-        pack_lowp_kernel<false><<<tiles, 128, 0, s>>>(raw, row0, n, view, optiles, norms, qscale, vstats);
+        pack_lowp_kernel<false><<<ntiles, 128, 0, s>>>(tab, raw, optiles, norms, qscale, vstats);
 }
 
 // ------------------------------------------------------------ tcgen05 pieces

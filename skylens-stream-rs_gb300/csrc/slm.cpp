@@ -165,6 +165,9 @@ struct slm_store {
     uint64_t lowp_version = ~0ull;
     uint64_t epoch = 0, lowp_epoch = ~0ull;  // epoch bumps on clear
     size_t lowp_views = 0;                   // views whose images are built
+    uint64_t fp32_epoch = ~0ull;             // FP32 tiles, built lazily the same way
+    size_t fp32_views = 0;
+    DevBuf tiletab;                          // {row0, n, tile, view} per tile to pack
     DevBuf optiles, norms, qscale, vstats;
 };
 
@@ -553,8 +556,6 @@ slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool devic
     if (n) {
         SLM_CU(cudaMemcpyAsync(raw, desc, (size_t)n * kDesc * sizeof(float),
                                device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-        launch_pack_fp32(raw, n, st->tiled.as<float>(), (uint32_t)(st->rows_used / kTile), s);
-        SLM_CU(cudaGetLastError());
     }
     if (id) *id = (uint32_t)st->row0.size();
     st->row0.push_back((uint32_t)st->rows_used);
@@ -736,6 +737,32 @@ extern "C" uint32_t slm_store_num_views(slm_store *st) { return st ? (uint32_t)s
 
 namespace {
 
+// Upload the tile table of views [first, end) and return its tile count.
+slm_status upload_tiletab(slm_store *st, size_t first, size_t end, cudaStream_t s, uint32_t *ntiles) {
+    std::vector<uint4> tab;
+    for (size_t v = first; v < end; ++v)
+        for (uint32_t t = 0; t < (st->n[v] + kTile - 1) / kTile; ++t)
+            tab.push_back(make_uint4(st->row0[v], st->n[v], t, (uint32_t)v));
+    *ntiles = (uint32_t)tab.size();
+    if (tab.empty()) return SLM_OK;
+    SLM_TRY(st->tiletab.ensure(st->ctx, tab.size() * sizeof(uint4)));
+    SLM_CU(cudaMemcpyAsync(st->tiletab.p, tab.data(), tab.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+    return SLM_OK;
+}
+
+// FP32 tiles of the views appended since the last build (one launch).
+slm_status store_sync_fp32(slm_store *st, cudaStream_t s) {
+    const size_t first = st->fp32_epoch == st->epoch ? st->fp32_views : 0;
+    if (first >= st->row0.size() && st->fp32_epoch == st->epoch) return SLM_OK;
+    uint32_t nt = 0;
+    SLM_TRY(upload_tiletab(st, first, st->row0.size(), s, &nt));
+    launch_pack_fp32_tiles(st->tiletab.as<uint4>(), nt, st->raw.as<float>(), st->tiled.as<float>(), s);
+    SLM_CU(cudaGetLastError());
+    st->fp32_epoch = st->epoch;
+    st->fp32_views = st->row0.size();
+    return SLM_OK;
+}
+
 // Build the store's low-precision operand images: only the views appended
 // since the last build, unless the store was cleared or the format changed.
 slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
@@ -753,10 +780,10 @@ slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
     SLM_TRY(st->vstats.ensure(c, nv * sizeof(ViewStat)));
     if (first < st->row0.size())
         SLM_CU(cudaMemsetAsync(st->vstats.as<ViewStat>() + first, 0, (st->row0.size() - first) * sizeof(ViewStat), s));
-    for (size_t v = first; v < st->row0.size(); ++v)
-        launch_pack_lowp(st->raw.as<float>(), st->row0[v], st->n[v], (uint32_t)v, fp8 ? 1 : 0,
-                         st->optiles.as<uint8_t>(), st->norms.as<float>(), st->qscale.as<float>(),
-                         st->vstats.as<ViewStat>(), s);
+    uint32_t nt = 0;
+    SLM_TRY(upload_tiletab(st, first, st->row0.size(), s, &nt));
+    launch_pack_lowp(st->tiletab.as<uint4>(), nt, st->raw.as<float>(), fp8 ? 1 : 0, st->optiles.as<uint8_t>(),
+                     st->norms.as<float>(), st->qscale.as<float>(), st->vstats.as<ViewStat>(), s);
     SLM_CU(cudaGetLastError());
     st->lowp_version = st->version;
     st->lowp_fp8 = fp8 ? 1 : 0;
@@ -786,11 +813,15 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
     }
     p->launched = false;
     p->dump = p->tune.variant == 2 && prec != SLM_PREC_FP32;
-    if (prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
+    if (prec != SLM_PREC_FP32)
+        SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
+    else
+        SLM_TRY(store_sync_fp32(st, stream));
     return plan_build(p, pairs);
 }
 
 slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
+    if (p->prec == SLM_PREC_FP32) SLM_TRY(store_sync_fp32(p->st, s));
     if (p->prec != SLM_PREC_FP32) {
         const uint64_t v = p->st->lowp_version;
         SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
@@ -1360,8 +1391,10 @@ void serve_loop(slm_server *srv) {
             if (take.empty()) continue;
             // Low-precision images of the new views, on the upload stream, so
             // every slot that waits for the upload also sees them.
-            if (srv->opts.prec != SLM_PREC_FP32) {
-                const slm_status ls = store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream);
+            {
+                const slm_status ls = srv->opts.prec != SLM_PREC_FP32
+                                          ? store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream)
+                                          : store_sync_fp32(srv->store, srv->ctx->stream);
                 if (ls != SLM_OK) {
                     for (ServeRequest *r : take) serve_fail_request(r, ls);
                     srv->cv_done.notify_all();

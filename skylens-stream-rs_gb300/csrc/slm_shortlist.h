@@ -113,9 +113,10 @@ struct SlArgs {
     uint32_t *counts;
 };
 
-// Store-side builders.
-void launch_pack_lowp(const float *raw, uint32_t row0, uint32_t n, uint32_t view, int fp8, uint8_t *optiles,
-                      float *norms, float *qscale, ViewStat *vstats, cudaStream_t s);
+// Store-side builder: one CTA per entry {first store row of the view, rows,
+// tile within the view, view} of the tile table.
+void launch_pack_lowp(const uint4 *tab, uint32_t ntiles, const float *raw, int fp8, uint8_t *optiles, float *norms,
+                      float *qscale, ViewStat *vstats, cudaStream_t s);
 
 // Kernel image / attribute set-up (outside stream capture).
 cudaError_t init_shortlist_kernels();
