@@ -462,8 +462,9 @@ def main():
         roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "T FP32 instr/s",
                 "frac": achieved / peak, "traffic": None, "kernel": "exact_kernel",
                 "peak_source": f"{sm_count} SMs x 128 lanes x {mhz:.0f} MHz (sampled)"}
-    prof = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(prof):
+    # DRAM bytes per launch of the dominant kernel from an ncu capture of this workload
+    prof = os.path.join(REPO, "profiles", "sl_pass_kernel_zone240_dram.json")
+    if os.path.exists(prof) and WORKLOAD == "zone240" and args.positions == 80:
         try:
             roof["traffic"] = json.load(open(prof)).get(roof["kernel"])
         except Exception:

@@ -321,13 +321,31 @@ constexpr size_t sl_smem_bytes() {
     return sizeof(SlSmem<FP8>) + 1024;  // slack for 1024-byte alignment
 }
 
+constexpr uint32_t kSuspendNs = 20000;  // suspend-time hint of one poll (20 us)
+
 // Bounded wait (about 2 s of wall time); on timeout raises the CTA abort flag
 // and records an error so every role leaves its loop.
+SLM_DEV bool sl_try_wait_hint(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+        : "memory");
+    return ok != 0;
+}
+
 SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_flag, uint32_t *err) {
     uint64_t t0 = 0;
     for (uint32_t it = 0;; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63) == 63) {
+        // the hint lets the hardware suspend the warp until the phase completes
+        // (or the hint expires) instead of re-issuing the poll
+        if (sl_try_wait_hint(bar, parity)) return true;
+        if ((it & 7) == 7) {
             if (*abort_flag) return false;
             const uint64_t now = globaltimer();
             if (t0 == 0) t0 = now;
