@@ -82,6 +82,11 @@ SLM_DEV u64x f2_add(u64x a, u64x b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+SLM_DEV u64x f2_sub(u64x a, u64x b) {
+    u64x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 // Approximate-path arithmetic: one rounding, covered by the error bound.
 SLM_DEV u64x f2_fma(u64x a, u64x b, u64x c) {
     u64x d;
@@ -108,6 +113,18 @@ SLM_DEV void tmem_wait_ld16(uint32_t (&r)[16]) {
                    "+r"(r[14]), "+r"(r[15])
                  :
                  : "memory");
+}
+
+// atomicAdd(p, 1) when pred holds, without a branch (no return value).
+SLM_DEV void red_add1_if(uint32_t *p, bool pred) {
+    asm volatile(
+        "{\n"
+        ".reg .pred q;\n"
+        "setp.ne.u32 q, %1, 0;\n"
+        "@q red.relaxed.gpu.global.add.u32 [%0], 1;\n"
+        "}\n" ::"l"(p),
+        "r"((uint32_t)pred)
+        : "memory");
 }
 
 // Minimum of 16 values, and with the minima of its two groups of 8.
@@ -321,31 +338,13 @@ constexpr size_t sl_smem_bytes() {
     return sizeof(SlSmem<FP8>) + 1024;  // slack for 1024-byte alignment
 }
 
-constexpr uint32_t kSuspendNs = 20000;  // suspend-time hint of one poll (20 us)
-
 // Bounded wait (about 2 s of wall time); on timeout raises the CTA abort flag
 // and records an error so every role leaves its loop.
-SLM_DEV bool sl_try_wait_hint(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n"
-        ".reg .pred p;\n"
-        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n"
-        "selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
-        : "memory");
-    return ok != 0;
-}
-
 SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_flag, uint32_t *err) {
     uint64_t t0 = 0;
     for (uint32_t it = 0;; ++it) {
-        // the hint lets the hardware suspend the warp until the phase completes
-        // (or the hint expires) instead of re-issuing the poll
-        if (sl_try_wait_hint(bar, parity)) return true;
-        if ((it & 7) == 7) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63) {
             if (*abort_flag) return false;
             const uint64_t now = globaltimer();
             if (t0 == 0) t0 = now;
@@ -358,7 +357,7 @@ SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_fl
     }
 }
 
-template <int PASS, bool FP8>
+template <int PASS, bool FP8, bool DUMP>
 __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
     extern __shared__ uint8_t sl_smem_raw[];
     const uint32_t pad = (1024u - (smem_u32(sl_smem_raw) & 1023u)) & 1023u;
@@ -550,7 +549,7 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 if (j0 + k >= pm.nb) d[k] = kInf;
                         }
                         if constexpr (PASS == 1) {
-                            if (g.dump && item.pair == 0 && rvalid) {
+                            if (DUMP && item.pair == 0 && rvalid) {
 #pragma unroll
                                 for (int k = 0; k < 16; ++k)
                                     if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = d[k];
@@ -573,20 +572,31 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 if (lane == 0) cp[k4] = o;
                             }
                         } else {
-                            if (thr_i > -kInf) {
+                            {
+                                // rows certain to have no match carry thr_i = -inf: no hit
                                 float gm[2];
                                 const float cm = min16g(d, gm);
                                 if (cm <= thr_i) {
 #pragma unroll
                                     for (int qq = 0; qq < 2; ++qq) {
                                         if (gm[qq] <= thr_i) {
+                                            if (own_row) {
+                                                // the item owns the whole row: predicated stores, running count
 #pragma unroll
-                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
-                                                if (d[k] <= thr_i) {
-                                                    // one item owns the whole row unless its columns are split
-                                                    const uint32_t sl = own_row ? ncand++
-                                                                                : atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
-                                                    if (sl < kSlHalfSlots) cand[sl] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
+                                                    const bool hit = d[k] <= thr_i;
+                                                    if (hit && ncand < kSlHalfSlots)
+                                                        cand[ncand] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                    ncand += hit ? 1u : 0u;
+                                                }
+                                            } else {
+#pragma unroll
+                                                for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
+                                                    if (d[k] <= thr_i) {
+                                                        const uint32_t sl = atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
+                                                        if (sl < kSlHalfSlots)
+                                                            cand[sl] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                    }
                                                 }
                                             }
                                         }
@@ -594,27 +604,28 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 }
                             }
                             if (rvalid) {
-                                const float4 *bt4 = reinterpret_cast<const float4 *>(&S.bthr[st][cb]);
+                                const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(&S.bthr[st][cb]);
                                 float x[16];
 #pragma unroll
                                 for (int k4 = 0; k4 < 4; ++k4) {
-                                    const float4 tt = bt4[k4];
-                                    x[4 * k4 + 0] = d[4 * k4 + 0] - tt.x;
-                                    x[4 * k4 + 1] = d[4 * k4 + 1] - tt.y;
-                                    x[4 * k4 + 2] = d[4 * k4 + 2] - tt.z;
-                                    x[4 * k4 + 3] = d[4 * k4 + 3] - tt.w;
+                                    const ulonglong2 tt = bt2[k4];
+                                    const u64x x0 = f2_sub(f2_pack(d[4 * k4], d[4 * k4 + 1]), tt.x);
+                                    const u64x x1 = f2_sub(f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]), tt.y);
+                                    x[4 * k4 + 0] = f2_lo(x0);
+                                    x[4 * k4 + 1] = f2_hi(x0);
+                                    x[4 * k4 + 2] = f2_lo(x1);
+                                    x[4 * k4 + 3] = f2_hi(x1);
                                 }
                                 float gm[2];
                                 const float xm = min16g(x, gm);
                                 if (xm <= 0.f) {
+                                    uint32_t *cc = g.colcnt + sp.cbase + j0;
 #pragma unroll
-                                    for (int qq = 0; qq < 2; ++qq) {
+                                    for (int qq = 0; qq < 2; ++qq)
                                         if (gm[qq] <= 0.f) {
 #pragma unroll
-                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k)
-                                                if (x[k] <= 0.f) atomicAdd(&g.colcnt[sp.cbase + j0 + k], 1u);  // reduction
+                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k) red_add1_if(cc + k, x[k] <= 0.f);
                                         }
-                                    }
                                 }
                             }
                         }
@@ -1072,33 +1083,33 @@ __global__ void __launch_bounds__(256) sl_compact_kernel(SlArgs g) {
 // ---------------------------------------------------------------- launch
 
 cudaError_t init_shortlist_kernels() {
-    cudaError_t e;
-    e = cudaFuncSetAttribute(sl_pass_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sl_smem_bytes<false>());
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(sl_pass_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sl_smem_bytes<false>());
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(sl_pass_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sl_smem_bytes<true>());
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(sl_pass_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sl_smem_bytes<true>());
+    const int sb = (int)sl_smem_bytes<false>(), s8 = (int)sl_smem_bytes<true>();
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(sl_pass_kernel<1, false, false>, at, sb);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(sl_pass_kernel<1, false, true>, at, sb);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(sl_pass_kernel<2, false, false>, at, sb);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(sl_pass_kernel<1, true, false>, at, s8);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(sl_pass_kernel<1, true, true>, at, s8);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(sl_pass_kernel<2, true, false>, at, s8);
+    return e;
 }
 
 void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
     const int grid = (int)(a.n_items < (uint32_t)sms ? a.n_items : (uint32_t)sms);
     if (!grid) return;
+    const size_t sb = sl_smem_bytes<false>(), s8 = sl_smem_bytes<true>();
     if (pass == 1) {
         if (a.fp8)
-            sl_pass_kernel<1, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+            a.dump ? sl_pass_kernel<1, true, true><<<grid, kSlThreads, s8, s>>>(a)
+                   : sl_pass_kernel<1, true, false><<<grid, kSlThreads, s8, s>>>(a);
         else
-            sl_pass_kernel<1, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
+            a.dump ? sl_pass_kernel<1, false, true><<<grid, kSlThreads, sb, s>>>(a)
+                   : sl_pass_kernel<1, false, false><<<grid, kSlThreads, sb, s>>>(a);
     } else {
         if (a.fp8)
-            sl_pass_kernel<2, true><<<grid, kSlThreads, sl_smem_bytes<true>(), s>>>(a);
+            sl_pass_kernel<2, true, false><<<grid, kSlThreads, s8, s>>>(a);
         else
-            sl_pass_kernel<2, false><<<grid, kSlThreads, sl_smem_bytes<false>(), s>>>(a);
+            sl_pass_kernel<2, false, false><<<grid, kSlThreads, sb, s>>>(a);
     }
 }
 
