@@ -124,7 +124,8 @@ _lib = None
 
 
 def library_path() -> str:
-    return _build.LIB
+    """libslm.so to load: $SLM_LIB_PATH if set (a build placed elsewhere), else the in-tree build."""
+    return os.environ.get("SLM_LIB_PATH") or _build.LIB
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -133,9 +134,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.LIB
+        path = library_path()
         if not os.path.exists(path):
-            if not build_if_missing:
+            if not build_if_missing or path != _build.LIB:
                 raise RuntimeError(f"libslm is not built: {path} missing")
             _build.build()
         L = ctypes.CDLL(path)
