@@ -63,13 +63,15 @@ typedef struct {
     uint64_t pairs;             /* image pairs matched */
     uint64_t distances;         /* sum over pairs of na*nb */
     uint64_t matches;           /* pairs written */
-    uint64_t rows_recomputed;   /* shortlist rows rescanned exactly */
-    uint64_t cols_recomputed;   /* mutual checks settled by an exact column scan */
+    uint64_t rows_recomputed;   /* shortlist rows settled by an exact scan (rows of routed pairs included) */
+    uint64_t cols_recomputed;   /* columns settled by an exact scan (columns of routed pairs included) */
     uint64_t rows_rescored;     /* rows whose shortlist was rescored exactly */
     float kernel_ms;            /* device time of the main matching kernel, last launch */
     float max_abs_err;          /* max |approx - exact| seen on rescored pairs */
     uint64_t kernel_launches;   /* kernels one launch of the batch runs */
     float pass_ms[2];           /* BF16/FP8: tensor-core passes 1 and 2; FP32: [0] = exact kernel */
+    uint64_t pairs_routed;      /* BF16/FP8: pairs whose error bound was too loose to certify
+                                   their rows, matched whole by the exact FP32 kernel */
 } slm_stats;
 
 typedef struct slm_ctx slm_ctx;

@@ -261,6 +261,9 @@ __global__ void __launch_bounds__(kThreads, 1) exact_kernel(ExactArgs g) {
     }
     for (int c = tid; c < 2 * kTile; c += kThreads) (&S.colred[0][0])[c] = ~0ull;
     __syncthreads();
+    // Items planned on the device (pairs routed from the shortlist path) come
+    // with their count in device memory, written by an earlier kernel.
+    const uint32_t n_items = g.n_items_dev ? min(*g.n_items_dev, g.n_items) : g.n_items;
 
     uint32_t a_phase = 0;
     uint32_t seq = 0;  // b tiles consumed by this CTA (selects ring slot and parity)
@@ -269,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1) exact_kernel(ExactArgs g) {
         if (tid == 0) S.item = atomicAdd(g.work, 1u);
         ok = __syncthreads_and(ok);
         const uint32_t it = S.item;
-        if (it >= g.n_items || !ok) break;
+        if (it >= n_items || !ok) break;
         const Item item = g.items[it];
         const PairMeta pm = g.pairs[item.pair];
         const float *atile = g.tiled + (size_t)(pm.a_row0 / kTile + item.rt) * kTileFloats;
@@ -430,15 +433,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs g) {
             const uint32_t rt = i / kTile;
             float d1 = __int_as_float(0x7f800000), d2 = __int_as_float(0x7f800000);
             uint32_t j1 = 0xffffffffu;
-            for (uint32_t c = 0; c < pm.nchunk; ++c) {
-                const RowPart p = g.parts[(size_t)(pm.part_base + rt * pm.nchunk + c) * kTile + (i % kTile)];
-                const float nd2 = fminf(fmaxf(d1, p.d1), fminf(d2, p.d2));
-                if (p.d1 < d1 || (p.d1 == d1 && p.j1 < j1)) {
-                    d1 = p.d1;
-                    j1 = p.j1;
-                }
-                d2 = nd2;
-            }
+            for (uint32_t c = 0; c < pm.nchunk; ++c)
+                merge_rowpart(g.parts[(size_t)(pm.part_base + rt * pm.nchunk + c) * kTile + (i % kTile)], d1, d2, j1);
             const bool d2_finite = d2 < __int_as_float(0x7f800000);
             if (j1 != 0xffffffffu && d2_finite && !(d1 >= __fmul_rn(g.ratio2, d2))) {
                 if (!g.mutual || static_cast<uint32_t>(g.colbest[pm.col_base + j1]) == i) {

@@ -5,7 +5,7 @@
 // by the per-pair error bound eps or settled with exact spec-order FP32
 // distances (matching.rs:146-155), so results equal the reference's.
 //
-// Tensor-core kernel (sl_pass_kernel, one persistent CTA per SM, 10 warps):
+// Tensor-core kernel (sl_pass_kernel, one persistent CTA per SM, 18 warps):
 //   warp 0      TMA producer: per item the a tiles (1 or 2 x 128 rows, K-major,
 //               128B-swizzled operand images copied verbatim from the store)
 //               and their norms; per 128-column b tile the operand tile, norms
@@ -13,10 +13,11 @@
 //   warp 1      allocates 512 TMEM columns; one thread issues tcgen05.mma
 //               (M=128, N=128, K=16 bf16 / K=32 e4m3) into a double-buffered
 //               pair of 128x128 f32 accumulators per a tile.
-//   warps 2-9   epilogue: warp w reads TMEM lane quarter w % 4 of a tile
-//               (w - 2) / 4, one thread per row, 32 columns per tcgen05.ld;
+//   warps 2-17  epilogue: warp w reads TMEM lane quarter w % 4 of a tile
+//               ((w - 2) / 4) % 2, column half (w - 2) / 8 of every b tile,
+//               one thread per row, 16 columns per tcgen05.ld;
 //               d~ = |a|^2 + |b|^2 - 2 acc. Row minima use a 3-input min tree
-//               per 32 columns; column minima use redux.sync.min.f32 per
+//               per 16 columns; column minima use redux.sync.min.f32 per
 //               column, merged across warps in shared memory and across CTAs
 //               with one atomicMin per column and tile.
 #include <cuda_fp8.h>
@@ -325,6 +326,7 @@ struct SlSmem {
     float ascale[256];
     float colpart[2][8][128];  // [tile parity][(a tile, lane quarter)][column]
     float2 rowx[256];          // pass 1: the second column half's row state
+    uint32_t rownear[256];     // pass 1: the second column half's near-chunk count
     uint64_t a_full, a_empty;
     uint64_t b_full[kSlStages], b_empty[kSlStages];
     uint64_t t_full[2], t_empty[2];
@@ -357,8 +359,15 @@ SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_fl
     }
 }
 
+// One CTA of kSlThreads per SM. Warps are spread over the SM's four
+// sub-partitions, each with 16384 registers: 18 warps put 5 on two of them, so
+// 5 x 32 x R <= 16384, R in steps of 8: 96 registers per thread.
+constexpr int kSlWarpsPerQuarter = (kSlThreads / 32 + 3) / 4;
+constexpr int kSlMaxRegs = (16384 / (32 * kSlWarpsPerQuarter)) & ~7;
+static_assert(kSlMaxRegs == 96, "register budget of the 18-warp pass kernel");
+
 template <int PASS, bool FP8, bool DUMP>
-__global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
+__global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
     extern __shared__ uint8_t sl_smem_raw[];
     const uint32_t pad = (1024u - (smem_u32(sl_smem_raw) & 1023u)) & 1023u;
     SlSmem<FP8> &S = *reinterpret_cast<SlSmem<FP8> *>(sl_smem_raw + pad);
@@ -394,11 +403,12 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
     if (warp == 0) {
         // ---------------------------------------------------------- producer
         if (lane == 0) {
-            uint32_t st = 0, sph = 0, iter = 0;
-            for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+            uint32_t st = 0, sph = 0, iter = 0;  // iter: items processed (routed pairs skip pass 2)
+            for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
                 const SlItem item = g.items[it];
                 const PairMeta pm = g.pairs[item.pair];
                 const SlPair sp = g.spairs[item.pair];
+                if (PASS == 2 && sp.routed) continue;
                 if (iter > 0 && !sl_wait(&S.a_empty, (iter - 1) & 1, abort_flag, err)) break;
                 const uint32_t arow = pm.a_row0 + item.rt0 * kTile;  // store row of the first a row
                 uint32_t bytes = item.nat * kOp + item.nat * 512;
@@ -423,6 +433,7 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                     if (FP8) bulk_g2s(S.bscale[st], g.qscale + brow, 512, &S.b_full[st]);
                     if (++st == kSlStages) st = 0, sph ^= 1;
                 }
+                ++iter;
                 if (*abort_flag) break;
             }
         }
@@ -430,9 +441,11 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
         // ---------------------------------------------------------- MMA issue
         constexpr uint32_t idesc = umma_idesc(FP8);
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
-        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
+            if (PASS == 2 && g.spairs[item.pair].routed) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
+            ++iter;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
                 if (!sl_wait(&S.b_full[st], sph, abort_flag, err) || !sl_wait(&S.t_empty[tb], tph ^ 1, abort_flag, err)) {
@@ -483,11 +496,13 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
         const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0, eph = 0;
         const float kInf = __int_as_float(0x7f800000);
-        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x, ++iter) {
+        for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
             const PairMeta pm = g.pairs[item.pair];
             const SlPair sp = g.spairs[item.pair];
+            if (PASS == 2 && sp.routed) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
+            ++iter;
             const bool active = at < (int)item.nat;          // warp-uniform
             const uint32_t i = item.rt0 * kTile + r;          // row within the pair
             const bool rvalid = active && i < pm.na;
@@ -497,6 +512,11 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_empty);
             float m1 = kInf, m2 = kInf;
+            // pass 1: 16-column chunks whose minimum lies within 2 eps above the
+            // running row minimum (new minima excluded), the estimate of the
+            // row's shortlist size that pair routing uses
+            const float w2 = 2.f * sp.eps;
+            uint32_t near = 0;
             const bool own_row = sp.nchunk == 1;
             const uint32_t ridx = sp.rbase + i;
             uint2 *cand = g.rowcand + (size_t)ridx * kSlRowSlots + h * kSlHalfSlots;
@@ -543,10 +563,16 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                 d[4 * k4 + 3] = f2_hi(d1);
                             }
                         }
-                        if (j0 + 16 > pm.nb) {  // ragged last tile: padding columns never win
+                        if (j0 + 16 > pm.nb) {
+                            // ragged last tile: padding columns never win. Pass 1
+                            // gives them +inf (the row state stays ordered); pass 2
+                            // gives them NaN, which no threshold admits, not even
+                            // the +inf of a row with a single finite chunk
+                            // (min.f32 ignores NaN)
+                            const float pad_d = PASS == 1 ? kInf : __int_as_float(0x7fffffff);
 #pragma unroll
                             for (int k = 0; k < 16; ++k)
-                                if (j0 + k >= pm.nb) d[k] = kInf;
+                                if (j0 + k >= pm.nb) d[k] = pad_d;
                         }
                         if constexpr (PASS == 1) {
                             if (DUMP && item.pair == 0 && rvalid) {
@@ -555,6 +581,9 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                     if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = d[k];
                             }
                             const float cm = min16(d);
+                            // FP8 only: the bf16 bound is too tight for rows to go wide
+                            // (the overflow count after pass 2 still routes such pairs)
+                            if constexpr (FP8) near += (cm >= m1 && cm <= m1 + w2) ? 1u : 0u;
                             m2 = fminf(m2, fmaxf(m1, cm));
                             m1 = fminf(m1, cm);
                             if (any_invalid_row) {
@@ -592,10 +621,13 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                                             } else {
 #pragma unroll
                                                 for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
-                                                    if (d[k] <= thr_i) {
+                                                    // once the count passed the capacity, the row is
+                                                    // settled by an exact scan: no more slots needed
+                                                    if (d[k] <= thr_i && ncand <= kSlHalfSlots) {
                                                         const uint32_t sl = atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
                                                         if (sl < kSlHalfSlots)
                                                             cand[sl] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                        ncand = sl + 1;
                                                     }
                                                 }
                                             }
@@ -672,7 +704,10 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
             if (!ok) break;
             if constexpr (PASS == 1) {
                 // merge the two column halves of each row, then store the partial
-                if (h == 1 && active) S.rowx[r] = make_float2(m1, m2);
+                if (h == 1 && active) {
+                    S.rowx[r] = make_float2(m1, m2);
+                    S.rownear[r] = near;
+                }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.ep_bar);
                 if (!sl_wait(&S.ep_bar, eph, abort_flag, err)) break;
@@ -682,7 +717,9 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
                     m2 = fminf(fminf(m2, o.y), fmaxf(m1, o.x));
                     m1 = fminf(m1, o.x);
                     // slot = row within its 256-row group (items of one 128-row tile start mid-group)
-                    g.rowpart[(size_t)item.part * 256 + (i & 255u)] = make_float2(m1, m2);
+                    const size_t slot = (size_t)item.part * 256 + (i & 255u);
+                    g.rowpart[slot] = make_float2(m1, m2);
+                    g.rownear[slot] = near + S.rownear[r];
                 }
             } else {
                 if (own_row && rvalid && thr_i > -kInf) g.rowcnt[2 * ridx + h] = ncand;
@@ -698,51 +735,75 @@ __global__ void __launch_bounds__(kSlThreads, 1) sl_pass_kernel(SlArgs g) {
     }
 }
 
-// ------------------------------------------------------------------ mid
+// ------------------------------------------------------------------ eps
 
-// Per pair: eps from the views' statistics, row thresholds from the pass-1
-// partials, column thresholds from the column minima.
-__global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
-    __shared__ float eps_sh;
-    __shared__ uint32_t unsafe_sh;
-    const uint32_t p = blockIdx.x;
+// Per pair, before pass 1: the error bound eps from the two views'
+// statistics. A pair with non-finite or huge inputs cannot be certified and is
+// routed to the exact kernel.
+__global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= g.npairs) return;
     const PairMeta pm = g.pairs[p];
     SlPair &sp = g.spairs[p];
+    const ViewStat va = g.vstats[sp.view_a], vb = g.vstats[sp.view_b];
+    const double A = __uint_as_float(va.nmax), B = __uint_as_float(vb.nmax);
+    const double Ra = __uint_as_float(va.rho), Rb = __uint_as_float(vb.rho);
+    const double Qa = __uint_as_float(va.nqmax), Qb = __uint_as_float(vb.nqmax);
+    bool unsafe = va.bad || vb.bad || !(A <= 64.0) || !(B <= 64.0);
+    // |d~ - d| <= 2 |a.b - q(a).q(b)| + accumulation and rounding terms, with
+    // |a.b - q(a).q(b)| <= |a - q(a)| |b| + |q(a)| |b - q(b)| (Cauchy-Schwarz).
+    double eps = 2.0 * (Ra * B + Qa * Rb) * (1.0 + 1e-3);
+    eps += 5e-4 * Qa * Qb + 5e-5 * (A * A + B * B) + 2e-5 * (A + B) * (A + B) + 1e-6;
+    if (!(eps < 1e30)) unsafe = true;
+    sp.eps = unsafe ? __int_as_float(0x7f800000) : (float)(eps * (1.0 + 1e-6));
+    sp.unsafe = unsafe ? 1u : 0u;
+    sp.routed = (unsafe && pm.na && pm.nb) ? 1u : 0u;
+    if (sp.routed) atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+}
+
+// ------------------------------------------------------------------ mid
+
+// Per pair: row thresholds from the pass-1 partials, column thresholds from
+// the column minima, and the routing decision from the near-chunk counts.
+__global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
+    __shared__ uint32_t wide_sh, open_sh;
+    const uint32_t p = blockIdx.x;
+    const PairMeta pm = g.pairs[p];
+    const SlPair sp = g.spairs[p];
+    if (sp.routed) return;  // block-uniform
     const float kInf = __int_as_float(0x7f800000);
-    if (threadIdx.x == 0) {
-        const ViewStat va = g.vstats[sp.view_a], vb = g.vstats[sp.view_b];
-        const double A = __uint_as_float(va.nmax), B = __uint_as_float(vb.nmax);
-        const double Ra = __uint_as_float(va.rho), Rb = __uint_as_float(vb.rho);
-        const double Qa = __uint_as_float(va.nqmax), Qb = __uint_as_float(vb.nqmax);
-        bool unsafe = va.bad || vb.bad || !(A <= 64.0) || !(B <= 64.0);
-        // |d~ - d| <= 2 |a.b - q(a).q(b)| + accumulation and rounding terms, with
-        // |a.b - q(a).q(b)| <= |a - q(a)| |b| + |q(a)| |b - q(b)| (Cauchy-Schwarz).
-        double eps = 2.0 * (Ra * B + Qa * Rb) * (1.0 + 1e-3);
-        eps += 5e-4 * Qa * Qb + 5e-5 * (A * A + B * B) + 2e-5 * (A + B) * (A + B) + 1e-6;
-        if (!(eps < 1e30)) unsafe = true;
-        eps_sh = unsafe ? kInf : (float)(eps * (1.0 + 1e-6));
-        unsafe_sh = unsafe ? 1u : 0u;
-        sp.eps = eps_sh;
-        sp.unsafe = unsafe_sh;
-    }
+    if (threadIdx.x == 0) wide_sh = open_sh = 0;
     __syncthreads();
-    const float eps = eps_sh;
-    const bool unsafe = unsafe_sh != 0;
+    const float eps = sp.eps;
     const double r2 = (double)g.ratio2;
     const uint32_t na_pad = (pm.na + kTile - 1) / kTile * kTile;
+    // a row is "wide" when more than half of its 16-column chunks (and more
+    // than the list capacity) came within 2 eps of the running minimum: the
+    // bound is then as wide as the spread of the row's distances, and its
+    // shortlist overflows. (Each column range of pass 1 restarts the running
+    // minimum, so a fixed count alone would misjudge rows split into many.)
+    const uint32_t wide_min = max((uint32_t)kSlRowSlots, (pm.nb + 15) / 16 / 2);
+    uint32_t wide = 0, open = 0;
     for (uint32_t i = threadIdx.x; i < na_pad; i += blockDim.x) {
         float thr = -kInf;
-        if (i < pm.na && !unsafe && pm.nb > 0) {
+        if (i < pm.na && pm.nb > 0) {
             const uint32_t super = i / 256, r = i % 256;
             float m1 = kInf, m2 = kInf;
+            uint32_t near = 0;
             for (uint32_t c = 0; c < sp.nchunk; ++c) {
-                const float2 v = g.rowpart[(size_t)(sp.part_base + super * sp.nchunk + c) * 256 + r];
+                const size_t slot = (size_t)(sp.part_base + super * sp.nchunk + c) * 256 + r;
+                const float2 v = g.rowpart[slot];
+                near += g.rownear[slot];
                 m2 = fminf(fminf(m2, v.y), fmaxf(m1, v.x));
                 m1 = fminf(m1, v.x);
             }
             // certain "no match": d1 >= m1 - eps >= r^2 (m2' + eps) >= fl(r^2 d2) (rounding margin 1e-6)
             const bool no_match = (double)m1 - eps >= r2 * ((double)m2 + eps) * (1.0 + 1e-6);
-            if (!no_match) thr = (float)(((double)m2 + 2.0 * eps) * (1.0 + 1e-6));
+            if (!no_match) {
+                thr = (float)(((double)m2 + 2.0 * eps) * (1.0 + 1e-6));
+                ++open;
+                wide += near > wide_min ? 1u : 0u;
+            }
             if (!(thr == thr)) thr = kInf;  // NaN guard: collect everything
         }
         g.rowthr[sp.rbase + i] = thr;
@@ -750,12 +811,21 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
     const uint32_t nb_pad = (pm.nb + kTile - 1) / kTile * kTile;
     for (uint32_t j = threadIdx.x; j < nb_pad; j += blockDim.x) {
         float thr = -kInf;
-        if (j < pm.nb && !unsafe) {
+        if (j < pm.nb) {
             const float c1 = ord2f(g.colmin[sp.cbase + j]);
             thr = (float)(((double)c1 + 2.0 * eps) * (1.0 + 1e-6));
             if (!(thr == thr)) thr = kInf;
         }
         g.colthr[sp.cbase + j] = thr;
+    }
+    if (wide) atomicAdd(&wide_sh, wide);
+    if (open) atomicAdd(&open_sh, open);
+    __syncthreads();
+    // more than 1/8 of the undecided rows are expected to overflow their
+    // shortlist: settle the whole pair with the exact kernel
+    if (threadIdx.x == 0 && wide_sh * 8 > open_sh && open_sh) {
+        g.spairs[p].routed = 1;
+        atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
     }
 }
 
@@ -793,21 +863,39 @@ SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &s
     return kDecPending;
 }
 
-// One thread per row: decide from the bounds, or queue exact work.
+// One thread per row: decide from the bounds, or queue exact work. A pair
+// with more than 1/8 of its rows overflowing S is routed to the exact kernel
+// instead (one exact scan per row would cost more).
 __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
+    __shared__ uint32_t over_sh;
     const uint32_t p = blockIdx.x;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
+    if (sp.routed) return;  // block-uniform: route_finalize decides its rows
     const float kInf = __int_as_float(0x7f800000);
     const float eps = sp.eps;
     const double r2 = (double)g.ratio2;
+    if (threadIdx.x == 0) over_sh = 0;
+    __syncthreads();
+    uint32_t over = 0;
+    for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
+        const uint32_t ridx = sp.rbase + i;
+        over += (g.rowthr[ridx] > -kInf && (g.rowcnt[2 * ridx] > kSlHalfSlots || g.rowcnt[2 * ridx + 1] > kSlHalfSlots))
+                    ? 1u : 0u;
+    }
+    if (over) atomicAdd(&over_sh, over);
+    __syncthreads();
+    if (over_sh * 8 > pm.na) {
+        if (threadIdx.x == 0) {
+            g.spairs[p].routed = 1;
+            atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+        }
+        return;
+    }
     for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
         const uint32_t ridx = sp.rbase + i;
         uint32_t dec = kDecNone;
-        if (sp.unsafe) {
-            push_scan(g, p, 0, i, 0);
-            dec = kDecPending;
-        } else if (g.rowthr[ridx] > -kInf) {
+        if (g.rowthr[ridx] > -kInf) {
             const uint32_t n0 = g.rowcnt[2 * ridx], n1 = g.rowcnt[2 * ridx + 1];
             const uint32_t n = n0 + n1;
             if (n0 > kSlHalfSlots || n1 > kSlHalfSlots) {
@@ -1046,6 +1134,153 @@ __global__ void __launch_bounds__(256) sl_scan_kernel(SlArgs g) {
     }
 }
 
+// -------------------------------------------------------------- routing
+
+// Exclusive scan over the 1024 threads of a block; returns this thread's
+// prefix and writes the block total.
+SLM_DEV uint32_t block_scan_1024(uint32_t v, uint32_t *sh, uint32_t &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = sh[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        sh[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    total = sh[31];
+    return (w ? sh[w - 1] : 0u) + x - v;
+}
+
+// One CTA of 1024 threads: plans the exact work of the routed pairs. Column
+// chunks per row tile are chosen over all routed pairs together, as the
+// FP32 batch plan does: enough items to fill the GPU, at most kXChunkMax.
+// Writes each routed pair's first item and chunk count, the list of routed
+// pairs and the counters.
+__global__ void __launch_bounds__(1024) sl_route_plan_kernel(SlArgs g) {
+    __shared__ uint32_t sh[32];
+    __shared__ uint32_t carry_items, carry_list;
+    if (g.ctl[kCtlRouteMarks] == 0) return;  // nothing routed: the counters stay 0
+    uint32_t rt = 0, rows = 0, cols = 0, total = 0;
+    for (uint32_t p = threadIdx.x; p < g.npairs; p += blockDim.x)
+        if (g.spairs[p].routed) {
+            const PairMeta pm = g.pairs[p];
+            rt += (pm.na + kTile - 1) / kTile;
+            rows += pm.na;
+            cols += pm.nb;
+        }
+    block_scan_1024(rt, sh, total);
+    const uint32_t rt_total = total;
+    block_scan_1024(rows, sh, total);
+    const uint32_t rows_total = total;
+    block_scan_1024(cols, sh, total);
+    const uint32_t cols_total = total;
+    uint32_t split = 1;
+    if (rt_total && rt_total < g.want_items) split = (g.want_items + rt_total - 1) / rt_total;
+    split = min(split, kXChunkMax);
+    if (threadIdx.x == 0) carry_items = carry_list = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < g.npairs; base += blockDim.x) {
+        const uint32_t p = base + threadIdx.x;
+        uint32_t routed = 0, n = 0, chunks = 0;
+        if (p < g.npairs && g.spairs[p].routed) {
+            const PairMeta pm = g.pairs[p];
+            const uint32_t rt_n = (pm.na + kTile - 1) / kTile, ct_n = (pm.nb + kTile - 1) / kTile;
+            routed = 1;
+            chunks = max(1u, min(split, ct_n));
+            n = rt_n * chunks;
+        }
+        uint32_t t_items = 0, t_list = 0;
+        const uint32_t off = block_scan_1024(n, sh, t_items);
+        const uint32_t idx = block_scan_1024(routed, sh, t_list);
+        const uint32_t ci = carry_items, cl = carry_list;
+        if (routed) {
+            g.spairs[p].xpart = ci + off;
+            g.spairs[p].xchunk = chunks;
+            g.xlist[cl + idx] = p;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            carry_items = ci + t_items;
+            carry_list = cl + t_list;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        uint32_t items = carry_items;
+        if (items > g.xitem_cap) {  // cannot happen with the plan's capacity
+            atomicCAS(g.ctl + 1, 0u, (uint32_t)DERR_BAD_ITEM);
+            items = g.xitem_cap;
+        }
+        g.ctl[kCtlXItems] = items;
+        g.ctl[kCtlRoutedPairs] = carry_list;
+        g.ctl[kCtlRoutedRows] = rows_total;
+        g.ctl[kCtlRoutedCols] = cols_total;
+    }
+}
+
+// Writes the exact work items of the routed pairs and resets their column
+// minima keys (one CTA per routed pair at a time).
+__global__ void __launch_bounds__(256) sl_route_apply_kernel(SlArgs g) {
+    const uint32_t n = g.ctl[kCtlRoutedPairs];
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint32_t p = g.xlist[k];
+        const PairMeta pm = g.pairs[p];
+        const SlPair sp = g.spairs[p];
+        const uint32_t rt_n = (pm.na + kTile - 1) / kTile, ct_n = (pm.nb + kTile - 1) / kTile;
+        const uint32_t chunks = sp.xchunk, nit = rt_n * chunks;
+        for (uint32_t t = threadIdx.x; t < nit; t += blockDim.x) {
+            const uint32_t rt = t / chunks, c = t % chunks;
+            Item it;
+            it.pair = p;
+            it.rt = rt;
+            it.ct0 = (uint32_t)((uint64_t)ct_n * c / chunks);
+            it.ct1 = (uint32_t)((uint64_t)ct_n * (c + 1) / chunks);
+            it.part = sp.xpart + t;  // = xpart + rt * chunks + c
+            it.pad[0] = it.pad[1] = it.pad[2] = 0;
+            if (sp.xpart + t < g.xitem_cap) g.xitems[sp.xpart + t] = it;
+        }
+        if (g.mutual)
+            for (uint32_t j = threadIdx.x; j < pm.nb; j += blockDim.x) g.colbest[pm.col_base + j] = ~0ull;
+    }
+}
+
+// After exact_kernel: the routed pairs' row decisions, as finalize_kernel
+// makes them (matching.rs:204-214), into rowdec.
+__global__ void __launch_bounds__(256) sl_route_finalize_kernel(SlArgs g) {
+    const uint32_t n = g.ctl[kCtlRoutedPairs];
+    const float kInf = __int_as_float(0x7f800000);
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint32_t p = g.xlist[k];
+        const PairMeta pm = g.pairs[p];
+        const SlPair sp = g.spairs[p];
+        for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
+            const uint32_t rt = i / kTile;
+            float d1 = kInf, d2 = kInf;
+            uint32_t j1 = 0xffffffffu;
+            for (uint32_t c = 0; c < sp.xchunk; ++c) {
+                const uint32_t part = sp.xpart + rt * sp.xchunk + c;
+                if (part < g.xitem_cap) merge_rowpart(g.xparts[(size_t)part * kTile + (i % kTile)], d1, d2, j1);
+            }
+            uint32_t dec = kDecNone;
+            if (j1 != 0xffffffffu && d2 < kInf && !(d1 >= __fmul_rn(g.ratio2, d2)))
+                if (!g.mutual || static_cast<uint32_t>(g.colbest[pm.col_base + j1]) == i) dec = j1;
+            g.rowdec[sp.rbase + i] = dec;
+        }
+    }
+}
+
 // -------------------------------------------------------------- compact
 
 __global__ void __launch_bounds__(256) sl_compact_kernel(SlArgs g) {
@@ -1094,9 +1329,15 @@ cudaError_t init_shortlist_kernels() {
     return e;
 }
 
-void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
+int launch_shortlist_eps(const SlArgs &a, cudaStream_t s) {
+    if (!a.npairs) return 0;
+    sl_eps_kernel<<<(a.npairs + 255) / 256, 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
     const int grid = (int)(a.n_items < (uint32_t)sms ? a.n_items : (uint32_t)sms);
-    if (!grid) return;
+    if (!grid) return 0;
     const size_t sb = sl_smem_bytes<false>(), s8 = sl_smem_bytes<true>();
     if (pass == 1) {
         if (a.fp8)
@@ -1111,17 +1352,40 @@ void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
         else
             sl_pass_kernel<2, false, false><<<grid, kSlThreads, sb, s>>>(a);
     }
+    return 1;
 }
 
-void launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
-    if (a.npairs) sl_mid_kernel<<<a.npairs, 256, 0, s>>>(a);
+int launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
+    if (!a.npairs) return 0;
+    sl_mid_kernel<<<a.npairs, 256, 0, s>>>(a);
+    return 1;
 }
 
-void launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
-    if (a.npairs) sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
+int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
+    if (!a.npairs) return 0;
+    const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
+    sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
+    // routed pairs: plan, exact kernel over all their rows and columns, decisions
+    sl_route_plan_kernel<<<1, 1024, 0, s>>>(a);
+    sl_route_apply_kernel<<<rgrid, 256, 0, s>>>(a);
+    ExactArgs x{};
+    x.tiled = a.tiled;
+    x.items = a.xitems;
+    x.n_items = a.xitem_cap;
+    x.n_items_dev = a.ctl + kCtlXItems;
+    x.pairs = a.pairs;
+    x.parts = a.xparts;
+    x.colbest = a.colbest;
+    x.work = a.ctl + kCtlXWork;
+    x.err = a.ctl + 1;
+    x.mutual = a.mutual;
+    x.x2 = 1;
+    launch_exact(x, sms, s);
+    sl_route_finalize_kernel<<<rgrid, 256, 0, s>>>(a);
     sl_rescore_kernel<<<2 * sms, 256, 0, s>>>(a);
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
-    if (a.npairs) sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
+    sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
+    return 8;
 }
 
 }  // namespace slm

@@ -190,16 +190,17 @@ struct slm_plan {
     // shortlist path
     std::vector<SlItem> sitems;
     std::vector<SlPair> spairs;
-    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0;
-    DevBuf d_sitems, d_spairs, d_rowpart, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
-        d_rowdec, d_queue, d_rqueue, d_dump;
+    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0;
+    DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
+        d_rowdec, d_queue, d_rqueue, d_dump, d_xlist, d_xitems, d_xparts;
     bool dump = false;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel(s)
     cudaEvent_t evp[3] = {nullptr, nullptr, nullptr};  // shortlist: after pass 1, mid, pass 2
     uint64_t kernels = 0;                      // kernels per launch
-    void *graph_optiles = nullptr;             // store buffer the captured graph reads
+    void *graph_optiles = nullptr;             // store buffers the captured graph reads
+    void *graph_tiled = nullptr;
     bool launched = false;
     ~slm_plan() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -273,10 +274,11 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     if (supers && supers < want) split = (uint32_t)((want + supers - 1) / supers);
     p->sitems.clear();
     p->spairs.assign(p->np, SlPair{});
-    uint64_t rb = 0, cb = 0, part = 0;
+    uint64_t rb = 0, cb = 0, part = 0, row_tiles = 0;
     for (uint32_t k = 0; k < p->np; ++k) {
         const PairMeta &m = p->meta[k];
         SlPair &sp = p->spairs[k];
+        row_tiles += (m.na + kTile - 1) / kTile;
         sp.rbase = (uint32_t)rb;
         sp.cbase = (uint32_t)cb;
         sp.view_a = pairs[k].i;
@@ -315,9 +317,17 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     p->cols_pad = cb + kTile;
     p->sl_parts = std::max<uint64_t>(part, 1);
     p->queue_cap = std::max<uint64_t>(p->n_slots, 1) + 64;
+    // pairs routed to the exact kernel: at most (row tiles) + (4 x SMs) items
+    p->xitem_cap = row_tiles + 4ull * (uint64_t)std::max(1, c->sms);
+    if (p->xitem_cap >= (1ull << 32)) return fail(SLM_CAPACITY, "batch too large for one plan");
     SLM_TRY(p->d_sitems.ensure(c, sizeof(SlItem) * std::max<size_t>(1, p->sitems.size())));
     SLM_TRY(p->d_spairs.ensure(c, sizeof(SlPair) * std::max<size_t>(1, p->np)));
     SLM_TRY(p->d_rowpart.ensure(c, sizeof(float2) * 256 * p->sl_parts));
+    SLM_TRY(p->d_rownear.ensure(c, sizeof(uint32_t) * 256 * p->sl_parts));
+    SLM_TRY(p->d_xlist.ensure(c, sizeof(uint32_t) * std::max<size_t>(1, p->np)));
+    SLM_TRY(p->d_xitems.ensure(c, sizeof(Item) * p->xitem_cap));
+    SLM_TRY(p->d_xparts.ensure(c, sizeof(RowPart) * kTile * p->xitem_cap));
+    SLM_TRY(p->d_colbest.ensure(c, sizeof(unsigned long long) * std::max<uint64_t>(1, p->n_cols)));
     SLM_TRY(p->d_colmin.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowthr.ensure(c, sizeof(float) * p->rows_pad));
     SLM_TRY(p->d_colthr.ensure(c, sizeof(float) * p->cols_pad));
@@ -411,6 +421,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.items = p->d_sitems.as<SlItem>();
         a.n_items = (uint32_t)p->sitems.size();
         a.rowpart = p->d_rowpart.as<float2>();
+        a.rownear = p->d_rownear.as<uint32_t>();
         a.colmin = p->d_colmin.as<uint32_t>();
         a.rowthr = p->d_rowthr.as<float>();
         a.colthr = p->d_colthr.as<float>();
@@ -428,16 +439,25 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.dump = p->dump ? p->d_dump.as<float>() : nullptr;
         a.slots = p->d_slots.as<uint2>();
         a.counts = p->d_counts.as<uint32_t>();
+        a.tiled = st->tiled.as<float>();
+        a.xlist = p->d_xlist.as<uint32_t>();
+        a.xitems = p->d_xitems.as<Item>();
+        a.xitem_cap = (uint32_t)p->xitem_cap;
+        a.xparts = p->d_xparts.as<RowPart>();
+        a.colbest = p->d_colbest.as<unsigned long long>();
+        a.want_items = 4u * (uint32_t)std::max(1, p->ctx->sms);
+        int nk = 1;  // the colmin fill
         SLM_CU(record_event(p->ev0, s));
-        launch_shortlist_pass(a, 1, p->ctx->sms, s);
+        nk += launch_shortlist_eps(a, s);
+        nk += launch_shortlist_pass(a, 1, p->ctx->sms, s);
         SLM_CU(record_event(p->evp[0], s));
-        launch_shortlist_mid(a, s);
+        nk += launch_shortlist_mid(a, s);
         SLM_CU(record_event(p->evp[1], s));
-        launch_shortlist_pass(a, 2, p->ctx->sms, s);
+        nk += launch_shortlist_pass(a, 2, p->ctx->sms, s);
         SLM_CU(record_event(p->evp[2], s));
-        launch_shortlist_tail(a, p->ctx->sms, s);
+        nk += launch_shortlist_tail(a, p->ctx->sms, s);
         SLM_CU(record_event(p->ev1, s));
-        p->kernels = 1 + 7 + 2;
+        p->kernels = (uint64_t)nk + 2;  // + scan_counts, gather
         uint64_t *offsets = p->d_offsets.as<uint64_t>();
         launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
         launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
@@ -583,8 +603,9 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
         uint32_t w[16];
         SLM_CU(cudaMemcpy(w, p->d_ctl.p, sizeof(w), cudaMemcpyDeviceToHost));
         st->rows_rescored = w[kCtlRescored];
-        st->rows_recomputed = w[kCtlQueueRows];
-        st->cols_recomputed = w[kCtlQueueCols];
+        st->rows_recomputed = (uint64_t)w[kCtlQueueRows] + w[kCtlRoutedRows];
+        st->cols_recomputed = (uint64_t)w[kCtlQueueCols] + w[kCtlRoutedCols];
+        st->pairs_routed = w[kCtlRoutedPairs];
         float e;
         std::memcpy(&e, &w[kCtlMaxErr], sizeof(e));
         st->max_abs_err = e;
@@ -813,25 +834,23 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
     }
     p->launched = false;
     p->dump = p->tune.variant == 2 && prec != SLM_PREC_FP32;
-    if (prec != SLM_PREC_FP32)
-        SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
-    else
-        SLM_TRY(store_sync_fp32(st, stream));
+    // FP32 tiles serve the exact kernel of every path (low precision: routed pairs)
+    SLM_TRY(store_sync_fp32(st, stream));
+    if (prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
     return plan_build(p, pairs);
 }
 
 slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
-    if (p->prec == SLM_PREC_FP32) SLM_TRY(store_sync_fp32(p->st, s));
-    if (p->prec != SLM_PREC_FP32) {
-        const uint64_t v = p->st->lowp_version;
-        SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
-        // a rebuilt operand image may live in new buffers: capture again
-        if (v != p->st->lowp_version && p->exec && p->st->optiles.p != p->graph_optiles) {
-            cudaGraphExecDestroy(p->exec);
-            p->exec = nullptr;
-        }
-        p->graph_optiles = p->st->optiles.p;
+    SLM_TRY(store_sync_fp32(p->st, s));
+    if (p->prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
+    // a store buffer the captured graph reads may have moved: capture again
+    if (p->exec && (p->st->tiled.p != p->graph_tiled ||
+                    (p->prec != SLM_PREC_FP32 && p->st->optiles.p != p->graph_optiles))) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
     }
+    p->graph_tiled = p->st->tiled.p;
+    p->graph_optiles = p->st->optiles.p;
     if (!p->ev0) SLM_CU(cudaEventCreate(&p->ev0));
     if (!p->ev1) SLM_CU(cudaEventCreate(&p->ev1));
     for (cudaEvent_t &e : p->evp)
@@ -1300,7 +1319,9 @@ uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, sl
     if (prec == SLM_PREC_FP32)
         bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
     else
-        bytes += rows * (5 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 8;
+        bytes += rows * (5 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 12 +
+                 pairs.size() * 4 +
+                 (rows / kTile + 4ull * (uint64_t)std::max(1, st->ctx->sms)) * (sizeof(Item) + sizeof(RowPart) * kTile);
     return bytes + bytes / 4;  // DevBuf growth slack
 }
 
@@ -1389,12 +1410,12 @@ void serve_loop(slm_server *srv) {
                 srv->pending.pop_front();
             }
             if (take.empty()) continue;
-            // Low-precision images of the new views, on the upload stream, so
-            // every slot that waits for the upload also sees them.
+            // FP32 tiles and low-precision images of the new views, on the
+            // upload stream, so every slot that waits for the upload sees them.
             {
-                const slm_status ls = srv->opts.prec != SLM_PREC_FP32
-                                          ? store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream)
-                                          : store_sync_fp32(srv->store, srv->ctx->stream);
+                slm_status ls = store_sync_fp32(srv->store, srv->ctx->stream);
+                if (ls == SLM_OK && srv->opts.prec != SLM_PREC_FP32)
+                    ls = store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream);
                 if (ls != SLM_OK) {
                     for (ServeRequest *r : take) serve_fail_request(r, ls);
                     srv->cv_done.notify_all();

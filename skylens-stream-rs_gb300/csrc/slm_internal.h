@@ -25,6 +25,19 @@ struct __align__(16) RowPart {
     uint32_t pad;
 };
 
+#ifdef __CUDACC__
+// Merges a column range's partial into a row state: (d1, lowest j1) and the
+// second smallest of the multiset (matching.rs:182-187 applied per range).
+__device__ __forceinline__ void merge_rowpart(const RowPart &p, float &d1, float &d2, uint32_t &j1) {
+    const float nd2 = fminf(fmaxf(d1, p.d1), fminf(d2, p.d2));
+    if (p.d1 < d1 || (p.d1 == d1 && p.j1 < j1)) {
+        d1 = p.d1;
+        j1 = p.j1;
+    }
+    d2 = nd2;
+}
+#endif
+
 // Per image pair, as planned on the host.
 struct PairMeta {
     uint32_t a_row0, b_row0;  // first store row of the two views (multiples of 128)
@@ -46,7 +59,8 @@ struct Item {
 struct ExactArgs {
     const float *tiled;          // FP32 store tiles
     const Item *items;
-    uint32_t n_items;
+    uint32_t n_items;            // item capacity
+    const uint32_t *n_items_dev; // if set, the item count is min(*n_items_dev, n_items), read on the device
     const PairMeta *pairs;
     RowPart *parts;
     unsigned long long *colbest; // (bits(d) << 32 | i), min-reduced

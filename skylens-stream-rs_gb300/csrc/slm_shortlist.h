@@ -24,6 +24,21 @@
 //                      to rescan.
 //   rescore            one warp per queued row: exact distances of S.
 //   scan               one CTA per queued row or column: exact full scans.
+//
+// Pair routing. When the bound is too loose for a pair's distances (FP8 on
+// unit-length descriptors: eps ~ 0.1 against distance gaps of the same size),
+// most rows would overflow S and be settled one row at a time. Such a pair is
+// routed instead to the tiled exact FP32 kernel, which settles every row and
+// column of it:
+//   - before pass 1: a pair with non-finite or huge inputs (unsafe);
+//   - after pass 1 (mid, FP8): more than 1/8 of its undecided rows are "wide":
+//     more than half of their 16-column chunks (and more than kSlRowSlots) had
+//     a minimum within 2 eps above the running row minimum; pass 2 skips
+//     routed pairs;
+//   - after pass 2 (finalize): more than 1/8 of its rows overflowed S.
+// The routed pairs' exact work items are planned on the device (route_plan,
+// route_apply), run by exact_kernel, and route_finalize writes their rows'
+// decisions; the results stay bit-exact whichever way a pair goes.
 #pragma once
 #include <cstdint>
 
@@ -63,8 +78,12 @@ struct SlPair {
     uint32_t cbase;    // first entry in per-column arrays (multiple of 128)
     uint32_t part_base, nchunk;  // pass-1 row partials: (part_base + (rt0/2)*nchunk + c) * 256 + r
     uint32_t view_a, view_b;
-    float eps;         // written by the mid kernel
-    uint32_t unsafe;   // written by the mid kernel: settle every row exactly
+    float eps;         // written by the eps kernel
+    uint32_t unsafe;   // written by the eps kernel: no certification possible
+    uint32_t routed;   // per launch: settled by the exact FP32 kernel
+    uint32_t xchunk;   // routed: column chunks per 128-row tile
+    uint32_t xpart;    // routed: first exact work item (= first RowPart block)
+    uint32_t pad;
 };
 
 // Row decision codes (per pair row).
@@ -80,7 +99,12 @@ struct SlQueue {
 
 // Counters in the plan's control block (u32 words after work/error).
 enum : int { kCtlRescored = 2, kCtlQueueRows = 3, kCtlQueueCols = 4, kCtlMaxErr = 5, kCtlScanLen = 6,
-             kCtlRescoreLen = 7 };
+             kCtlRescoreLen = 7, kCtlXItems = 8, kCtlXWork = 9, kCtlRoutedPairs = 10, kCtlRoutedRows = 11,
+             kCtlRoutedCols = 12, kCtlRouteMarks = 13 };
+
+// Routed pairs: at most this many column chunks per 128-row tile; the exact
+// items of a launch number at most (routed row tiles) + (4 x SMs).
+constexpr uint32_t kXChunkMax = 16;
 
 struct SlArgs {
     const uint8_t *optiles;      // operand tiles by store row / 128
@@ -93,7 +117,8 @@ struct SlArgs {
     uint32_t npairs;
     const SlItem *items;
     uint32_t n_items;
-    float2 *rowpart;             // pass 1
+    float2 *rowpart;             // pass 1: (m1, m2') per row and column range
+    uint32_t *rownear;           // pass 1: chunks near the running row minimum (routing estimate)
     uint32_t *colmin;            // pass 1: order-preserving encoding of c1
     float *rowthr;               // mid -> pass 2
     float *colthr;               // mid -> pass 2
@@ -111,6 +136,14 @@ struct SlArgs {
     float *dump;                 // debug: d~ of pair 0, [na][nb] (nullptr: off)
     uint2 *slots;
     uint32_t *counts;
+    // pair routing to the exact kernel
+    const float *tiled;          // FP32 store tiles
+    uint32_t *xlist;             // routed pair ids
+    Item *xitems;                // exact work items
+    uint32_t xitem_cap;
+    RowPart *xparts;             // one 128-row block per item
+    unsigned long long *colbest; // by PairMeta::col_base
+    uint32_t want_items;         // exact items wanted to fill the GPU (4 x SMs)
 };
 
 // Store-side builder: one CTA per entry {first store row of the view, rows,
@@ -122,10 +155,11 @@ void launch_pack_lowp(const uint4 *tab, uint32_t ntiles, const float *raw, int f
 cudaError_t init_shortlist_kernels();
 
 // The pipeline of one shortlist launch (after counters are cleared):
-// pass 1, mid, pass 2, then finalize / rescore / scan / compact.
-void launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s);
-void launch_shortlist_mid(const SlArgs &a, cudaStream_t s);
-void launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s);
-
+// eps, pass 1, mid, pass 2, then finalize / routing / rescore / scan / compact.
+// Returns the number of kernels the call launched.
+int launch_shortlist_eps(const SlArgs &a, cudaStream_t s);
+int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s);
+int launch_shortlist_mid(const SlArgs &a, cudaStream_t s);
+int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s);
 
 }  // namespace slm

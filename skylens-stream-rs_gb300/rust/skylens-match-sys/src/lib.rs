@@ -38,6 +38,7 @@ pub struct slm_stats {
     pub max_abs_err: f32,
     pub kernel_launches: u64,
     pub pass_ms: [f32; 2],
+    pub pairs_routed: u64,
 }
 
 #[repr(C)]

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -60,6 +61,7 @@ class Matcher:
         check(self._L.slm_ctx_create(ctypes.byref(opts), ctypes.byref(h)), "slm_ctx_create")
         self._h = h
         self.last_stats: dict | None = None
+        self._stores = weakref.WeakSet()  # closed before the context
 
     @property
     def handle(self):
@@ -74,6 +76,8 @@ class Matcher:
 
     def close(self) -> None:
         if self._h:
+            for st in list(self._stores):
+                st.close()
             self._L.slm_ctx_destroy(self._h)
             self._h = None
 
@@ -130,6 +134,8 @@ class DescriptorStore:
         check(self._L.slm_store_create(m.handle, max_descs, max_views, ctypes.byref(h)), "slm_store_create")
         self._h = h
         self.counts: list[int] = []
+        self._plans = weakref.WeakSet()  # closed before the store
+        m._stores.add(self)
 
     @property
     def handle(self):
@@ -177,6 +183,8 @@ class DescriptorStore:
 
     def close(self) -> None:
         if self._h:
+            for p in list(self._plans):
+                p.close()
             self._L.slm_store_destroy(self._h)
             self._h = None
 
@@ -222,6 +230,7 @@ class BatchPlan:
         self._h = h
         self._out = None
         self.stats: dict | None = None
+        store._plans.add(self)
 
     def launch(self) -> None:
         check(self._L.slm_plan_launch(self._h), "slm_plan_launch")

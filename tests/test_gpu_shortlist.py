@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 
 def eps_bound(a, b, prec):
-    """The bound the mid kernel derives (Cauchy-Schwarz on the rounding residuals)."""
+    """The bound the eps kernel derives (Cauchy-Schwarz on the rounding residuals)."""
     import torch
     def q(x):
         t = torch.from_numpy(x)
