@@ -128,6 +128,18 @@ SLM_DEV void red_add1_if(uint32_t *p, bool pred) {
         : "memory");
 }
 
+// st.global.v2 of (a, b) when pred holds, without a branch.
+SLM_DEV void st_pair_if(uint2 *p, uint32_t a, uint32_t b, bool pred) {
+    asm volatile(
+        "{\n"
+        ".reg .pred q;\n"
+        "setp.ne.u32 q, %3, 0;\n"
+        "@q st.global.v2.u32 [%0], {%1, %2};\n"
+        "}\n" ::"l"(p),
+        "r"(a), "r"(b), "r"((uint32_t)pred)
+        : "memory");
+}
+
 // Minimum of 16 values, and with the minima of its two groups of 8.
 SLM_DEV float min16(const float (&d)[16]) {
     const float a = min3f(d[0], d[1], d[2]), b = min3f(d[3], d[4], d[5]), c = min3f(d[6], d[7], d[8]);
@@ -504,6 +516,9 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
             ++iter;
             const bool active = at < (int)item.nat;          // warp-uniform
+            // warp-uniform: this lane quarter holds at least one row of the pair
+            // (quarters of padding rows skip their chunks)
+            const bool qvalid = active && (item.rt0 + at) * kTile + q * 32 < pm.na;
             const uint32_t i = item.rt0 * kTile + r;          // row within the pair
             const bool rvalid = active && i < pm.na;
             const float na_i = active ? S.anorm[r] : 0.f;
@@ -528,7 +543,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     break;
                 }
                 tc_fence_after();
-                if (active) {
+                if (qvalid) {
                     const bool any_invalid_row = __any_sync(0xffffffffu, !rvalid);
                     const uint32_t tcol = tmem + lane_addr + (tb * 2 + at) * 128 + h * 64;
                     // chunks of 16 columns, two per iteration: loads double-buffered,
@@ -536,6 +551,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     auto chunk = [&](const uint32_t (&vc)[16], int c) {
                         const uint32_t cb = h * 64 + c * 16;   // column within the tile
                         const uint32_t j0 = t * kTile + cb;    // column within the pair
+                        if (j0 >= pm.nb) return;               // padding only (warp-uniform)
                         float d[16];
                         const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][cb]);
                         if constexpr (FP8) {
@@ -614,8 +630,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
 #pragma unroll
                                                 for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
                                                     const bool hit = d[k] <= thr_i;
-                                                    if (hit && ncand < kSlHalfSlots)
-                                                        cand[ncand] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                    st_pair_if(cand + min(ncand, (uint32_t)kSlHalfSlots - 1), j0 + k,
+                                                               __float_as_uint(d[k]), hit && ncand < kSlHalfSlots);
                                                     ncand += hit ? 1u : 0u;
                                                 }
                                             } else {
@@ -690,7 +706,9 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     if (e < 128) {
                         float m = kInf;
                         for (int cmb = 0; cmb < 8; ++cmb)
-                            if ((cmb >> 2) < (int)item.nat) m = fminf(m, S.colpart[tb][cmb][e]);
+                            if ((cmb >> 2) < (int)item.nat &&
+                                (item.rt0 + (cmb >> 2)) * kTile + (cmb & 3) * 32 < pm.na)  // quarter has rows
+                                m = fminf(m, S.colpart[tb][cmb][e]);
                         const uint32_t j = t * kTile + e;
                         if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(m));
                     }
