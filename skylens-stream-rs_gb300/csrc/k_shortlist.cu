@@ -779,6 +779,33 @@ __global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
     if (sp.routed) atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
 }
 
+// ------------------------------------------------------- certified tests
+
+// The decisions below are proved in f32 with directed rounding: each side of
+// a comparison is rounded toward the weaker claim, so a true comparison of the
+// rounded values implies it for the real numbers. The factors cover the
+// reference's own rounding of (r*r)*d2 (at most 2^-24 relative).
+constexpr float kUp = 1.000001f;    // > 1 + 2^-24
+constexpr float kDown = 0.999999f;  // < 1 - 2^-24
+
+// No match for the row: d1 >= m1 - eps >= r^2 (m2 + eps) kUp >= fl(r^2 d2),
+// where m1 - eps bounds d1 from below and m2 + eps bounds d2 from above.
+SLM_DEV bool certain_no_match(float m1, float m2, float eps, float r2) {
+    return __fsub_rd(m1, eps) >= __fmul_ru(__fmul_ru(r2, __fadd_ru(m2, eps)), kUp);
+}
+
+// The ratio test passes: d1 <= a1 + eps < r^2 (a2 - eps) kDown <= fl(r^2 d2).
+SLM_DEV bool certain_ratio_pass(float a1, float a2, float eps, float r2) {
+    return __fadd_ru(a1, eps) < __fmul_rd(__fmul_rd(r2, __fsub_rd(a2, eps)), kDown);
+}
+
+// Window x + 2 eps, rounded up (a larger threshold only admits more); NaN
+// becomes +inf (admit everything).
+SLM_DEV float window_up(float x, float eps) {
+    const float t = __fmul_ru(__fadd_ru(x, 2.f * eps), kUp);
+    return t == t ? t : __int_as_float(0x7f800000);
+}
+
 // ------------------------------------------------------------------ mid
 
 // Per pair: row thresholds from the pass-1 partials, column thresholds from
@@ -793,7 +820,6 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
     if (threadIdx.x == 0) wide_sh = open_sh = 0;
     __syncthreads();
     const float eps = sp.eps;
-    const double r2 = (double)g.ratio2;
     const uint32_t na_pad = (pm.na + kTile - 1) / kTile * kTile;
     // a row is "wide" when more than half of its 16-column chunks (and more
     // than the list capacity) came within 2 eps of the running minimum: the
@@ -815,14 +841,12 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
                 m2 = fminf(fminf(m2, v.y), fmaxf(m1, v.x));
                 m1 = fminf(m1, v.x);
             }
-            // certain "no match": d1 >= m1 - eps >= r^2 (m2' + eps) >= fl(r^2 d2) (rounding margin 1e-6)
-            const bool no_match = (double)m1 - eps >= r2 * ((double)m2 + eps) * (1.0 + 1e-6);
-            if (!no_match) {
-                thr = (float)(((double)m2 + 2.0 * eps) * (1.0 + 1e-6));
+            // m2' bounds the second smallest d~ from above
+            if (!certain_no_match(m1, m2, eps, g.ratio2)) {
+                thr = window_up(m2, eps);
                 ++open;
                 wide += near > wide_min ? 1u : 0u;
             }
-            if (!(thr == thr)) thr = kInf;  // NaN guard: collect everything
         }
         g.rowthr[sp.rbase + i] = thr;
     }
@@ -830,9 +854,7 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
     for (uint32_t j = threadIdx.x; j < nb_pad; j += blockDim.x) {
         float thr = -kInf;
         if (j < pm.nb) {
-            const float c1 = ord2f(g.colmin[sp.cbase + j]);
-            thr = (float)(((double)c1 + 2.0 * eps) * (1.0 + 1e-6));
-            if (!(thr == thr)) thr = kInf;
+            thr = window_up(ord2f(g.colmin[sp.cbase + j]), eps);
         }
         g.colthr[sp.cbase + j] = thr;
     }
@@ -892,7 +914,6 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
     if (sp.routed) return;  // block-uniform: route_finalize decides its rows
     const float kInf = __int_as_float(0x7f800000);
     const float eps = sp.eps;
-    const double r2 = (double)g.ratio2;
     if (threadIdx.x == 0) over_sh = 0;
     __syncthreads();
     uint32_t over = 0;
@@ -938,10 +959,10 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
                 // so the exact two smallest distances are among S. With fewer than
                 // two finite entries the exact second best is infinite
                 // (matching.rs:205: no match).
-                const bool no_match = n < 2 || !(a2 < kInf) ||
-                                      (double)a1 - eps >= r2 * ((double)a2 + eps) * (1.0 + 1e-6);
-                const bool sure = !no_match && (double)a1 + eps < r2 * ((double)a2 - eps) * (1.0 - 1e-6) &&
-                                  (double)a2 - a1 > 2.0 * eps;
+                const bool no_match = n < 2 || !(a2 < kInf) || certain_no_match(a1, a2, eps, g.ratio2);
+                // and the argmin is unique: a2 - a1 > 2 eps
+                const bool sure = !no_match && certain_ratio_pass(a1, a2, eps, g.ratio2) &&
+                                  __fsub_rd(a2, a1) > 2.f * eps;
                 if (sure) {
                     dec = g.mutual ? mutual_from_counts(g, p, sp, i, j1, a1) : j1;
                 } else if (!no_match) {
