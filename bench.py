@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--rates", default="10,50,200,burst",
                     help="serving arrival rates, views/s ('burst': every view at once, the saturated server)")
     ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
+    ap.add_argument("--no-scheduled", action="store_true",
+                    help="skip the scheduled_pairs(PairSchedule::default()) batch with the < 20 filter")
     return ap.parse_args()
 
 
@@ -418,6 +420,32 @@ def main():
         fp32 = {"value": len(z.pairs) / (fms / 1e3), "unit": "image pairs/s", "ms_per_step": fms,
                 "kernel_ms": float(np.mean([k[0] for k in f_kern]))}
 
+    # ---- the run pipeline's own pair set (pipeline.rs:485-496): scheduled_pairs with
+    # PairSchedule::default() and the filter that drops pairs with < 20 matches
+    sched = None
+    if not args.no_scheduled:
+        spairs = sm.scheduled_pairs(z.views)
+        store.autotune(spairs, 0.8, True, prec)
+        splan = store.plan(spairs, 0.8, True, prec, autotune=True)
+        splan.set_min_matches(20)
+        s_ms, _ = timed(splan, max(3, args.steps // 2), 2)
+        sgot, soff = splan.results()
+        cnt = np.diff(soff.astype(np.int64))
+        smism = 0
+        ssel = np.random.Generator(np.random.PCG64(8)).permutation(len(spairs))[:min(100, len(spairs))]
+        for k in ssel:
+            u, v = spairs[int(k)]
+            ref = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=os.cpu_count() or 1)
+            ref = ref if len(ref) >= 20 else ref[:0]
+            smism += not np.array_equal(sgot[int(soff[k]):int(soff[k + 1])], ref)
+        sms = float(np.mean(s_ms))
+        sdist = int(sum(int(z.counts[u]) * int(z.counts[v]) for u, v in spairs))
+        sched = {"schedule": "PairSchedule::default()", "min_matches": 20, "pairs": len(spairs),
+                 "pairs_kept": int((cnt > 0).sum()), "matches_kept": int(soff[-1]), "distances": sdist,
+                 "ms_per_step": sms, "value": len(spairs) / (sms / 1e3), "unit": "image pairs/s",
+                 "bit_exact": {"ok": smism == 0, "pairs_checked": int(len(ssel)), "mismatched_pairs": int(smism)}}
+        splan.close()
+
     # ---- e2e through the C ABI with host buffers
     e2e = None
     out_bytes = 0
@@ -492,7 +520,7 @@ def main():
                        "parallelism": f"replicas{ws}"},
             "distances_per_s": ws * dist_n / (ms / 1e3),
             "bit_exact": {"ok": bit_exact, "pairs_checked": int(nverify), "mismatched_pairs": int(mism)},
-            "fp32_plain": fp32,
+            "fp32_plain": fp32, "scheduled": sched,
             "kernel_ms": kms, "stats": stats_main,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(stats_main.get("kernel_launches", 0)) * args.steps,

@@ -222,6 +222,24 @@ slm_status slm_plan_debug_dump(slm_plan *p, float *out, uint64_t cap);
 /* Bytes of device scratch the plan holds. */
 uint64_t slm_plan_bytes(slm_plan *p);
 
+/* match_pairs' filter (pipeline.rs:494-496): pairs with fewer than
+ * min_matches matches report none from the next launch on (their lists are
+ * not gathered or copied). 0 or 1: no filter. */
+slm_status slm_plan_set_min_matches(slm_plan *p, uint32_t min_matches);
+
+/* The matching half of match_pairs (pipeline.rs:485-496) in one call:
+ * scheduled_pairs(views, sch) (NULL: PairSchedule::default()), ratio_match of
+ * every pair as one batch (store view i = views[i]), and the pairs with at
+ * least min_matches matches, in schedule order: pair k of the result is
+ * pairs_out[k] and its matches are out[offsets[k] .. offsets[k+1]) (offsets
+ * has pairs_cap + 1 entries). SLM_CAPACITY when more than pairs_cap pairs are
+ * kept (*n_pairs = the count needed) or out has fewer than offsets[*n_pairs]
+ * entries. */
+slm_status slm_match_pairs(slm_ctx *ctx, slm_store *st, const uint64_t *views, uint32_t nv,
+                           const slm_pair_schedule *sch, float ratio, int mutual, slm_precision prec,
+                           uint32_t min_matches, slm_pair *pairs_out, uint64_t pairs_cap, uint64_t *n_pairs,
+                           slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *stats);
+
 /* One-shot: plan, launch, read back, destroy. */
 slm_status slm_match_batch(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                            int mutual, slm_precision prec, slm_pair *out, uint64_t cap, uint64_t *offsets,

@@ -78,6 +78,14 @@ __global__ void copy_pairs_kernel(const uint2 *__restrict__ src, const uint64_t 
     if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = (uint32_t)n;
 }
 
+// match_pairs' filter (pipeline.rs:494-496: pairs with fewer than min_matches
+// matches are dropped before RANSAC): such pairs report no matches, so their
+// lists are neither gathered nor copied to the host.
+__global__ void filter_counts_kernel(uint32_t *__restrict__ counts, uint32_t np, uint32_t min_matches) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < np; k += gridDim.x * blockDim.x)
+        if (counts[k] < min_matches) counts[k] = 0;
+}
+
 __global__ void fill_u32_kernel(uint32_t *p, uint64_t n, uint32_t v) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         p[i] = v;
@@ -88,6 +96,10 @@ void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s) {
     uint64_t blocks = (n + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     fill_u32_kernel<<<(unsigned)blocks, 256, 0, s>>>(p, n, v);
+}
+
+void launch_filter_counts(uint32_t *counts, uint32_t np, uint32_t min_matches, cudaStream_t s) {
+    if (np) filter_counts_kernel<<<(np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024, 256, 0, s>>>(counts, np, min_matches);
 }
 
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s) {

@@ -194,6 +194,7 @@ struct slm_plan {
     DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
         d_rowdec, d_queue, d_rqueue, d_dump, d_xlist, d_xitems, d_xparts;
     bool dump = false;
+    uint32_t min_matches = 0;        // pairs with fewer matches report none
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel(s)
@@ -215,6 +216,7 @@ struct slm_plan {
 // Dense compaction of per-pair slots (device) into out + offsets.
 namespace slm {
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s);
+void launch_filter_counts(uint32_t *counts, uint32_t np, uint32_t min_matches, cudaStream_t s);
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s);
 void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
                    uint32_t np, uint2 *dense, uint64_t cap, cudaStream_t s);
@@ -458,6 +460,10 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         nk += launch_shortlist_tail(a, p->ctx->sms, s);
         SLM_CU(record_event(p->ev1, s));
         p->kernels = (uint64_t)nk + 2;  // + scan_counts, gather
+        if (p->min_matches > 1) {
+            launch_filter_counts(p->d_counts.as<uint32_t>(), p->np, p->min_matches, s);
+            p->kernels++;
+        }
         uint64_t *offsets = p->d_offsets.as<uint64_t>();
         launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
         launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
@@ -494,6 +500,10 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         f.slots = p->d_slots.as<uint2>();
         f.counts = p->d_counts.as<uint32_t>();
         launch_finalize(f, s);
+    }
+    if (p->min_matches > 1) {
+        launch_filter_counts(p->d_counts.as<uint32_t>(), p->np, p->min_matches, s);
+        p->kernels++;
     }
     uint64_t *offsets = p->d_offsets.as<uint64_t>();
     launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
@@ -1039,6 +1049,65 @@ extern "C" slm_status slm_match_batch(slm_ctx *c, slm_store *st, const slm_pair 
     slm_plan_destroy(p);
     g_last_error = keep;
     return s;
+}
+
+extern "C" slm_status slm_plan_set_min_matches(slm_plan *p, uint32_t min_matches) {
+    if (!p) return fail(SLM_INVALID_ARG, "NULL plan");
+    if (p->min_matches != min_matches && p->exec) {  // the captured graph has the old filter
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    p->min_matches = min_matches;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_match_pairs(slm_ctx *c, slm_store *st, const uint64_t *views, uint32_t nv,
+                                      const slm_pair_schedule *sch, float ratio, int mutual, slm_precision prec,
+                                      uint32_t min_matches, slm_pair *pairs_out, uint64_t pairs_cap,
+                                      uint64_t *n_pairs, slm_pair *out, uint64_t cap, uint64_t *offsets,
+                                      slm_stats *stats) {
+    if (!c || !st || (nv && !views) || !n_pairs || (pairs_cap && (!pairs_out || !offsets)))
+        return fail(SLM_INVALID_ARG, "NULL argument");
+    if (nv > st->row0.size())
+        return fail(SLM_INVALID_ARG, "views names " + std::to_string(nv) + " views, the store holds " +
+                                         std::to_string(st->row0.size()));
+    *n_pairs = 0;
+    const slm_pair_schedule def = slm_pair_schedule_default();
+    uint64_t total = 0;
+    slm_status s = slm_scheduled_pairs(views, nv, sch ? sch : &def, nullptr, 0, &total);
+    if (s != SLM_OK && s != SLM_CAPACITY) return s;
+    if (total >= (1ull << 32)) return fail(SLM_CAPACITY, "too many scheduled pairs for one batch");
+    std::vector<slm_pair> pairs(std::max<uint64_t>(total, 1));
+    SLM_TRY(slm_scheduled_pairs(views, nv, sch ? sch : &def, pairs.data(), total, &total));
+    const uint32_t np = (uint32_t)total;
+    slm_plan *p = nullptr;
+    SLM_TRY(slm_plan_create(c, st, pairs.data(), np, ratio, mutual, prec, nullptr, &p));
+    p->min_matches = min_matches;
+    std::vector<uint64_t> off(np + 1, 0);
+    s = slm_plan_launch(p);
+    if (s == SLM_OK) s = slm_plan_results(p, out, cap, off.data(), stats);
+    const std::string keep_err = g_last_error;
+    slm_plan_destroy(p);
+    g_last_error = keep_err;
+    if (s != SLM_OK && s != SLM_CAPACITY) return s;
+    // pairs that passed the filter, in schedule order (pipeline.rs:487-496 keeps
+    // the order of the pair list)
+    uint64_t kept = 0;
+    for (uint32_t k = 0; k < np; ++k) {
+        const uint64_t m = off[k + 1] - off[k];
+        if (m < min_matches) continue;  // filtered on the device: m == 0 here
+        if (kept < pairs_cap) {
+            pairs_out[kept] = pairs[k];
+            offsets[kept] = off[k];
+        }
+        ++kept;
+    }
+    *n_pairs = kept;
+    if (kept > pairs_cap)
+        return fail(SLM_CAPACITY, "pairs_cap " + std::to_string(pairs_cap) + " < " + std::to_string(kept) +
+                                      " pairs kept");
+    if (pairs_cap) offsets[kept] = off[np];
+    return s;  // SLM_CAPACITY here: out holds fewer than offsets[kept] matches
 }
 
 // -------------------------------------------------------------- single pair

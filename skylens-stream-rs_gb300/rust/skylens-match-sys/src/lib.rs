@@ -130,4 +130,9 @@ extern "C" {
     pub fn slm_match_batch(ctx: *mut slm_ctx, st: *mut slm_store, pairs: *const slm_pair, np: u32, ratio: f32,
                            mutual: c_int, prec: SlmPrecision, out: *mut slm_pair, cap: u64, offsets: *mut u64,
                            stats: *mut slm_stats) -> SlmStatus;
+    pub fn slm_plan_set_min_matches(p: *mut slm_plan, min_matches: u32) -> SlmStatus;
+    pub fn slm_match_pairs(ctx: *mut slm_ctx, st: *mut slm_store, views: *const u64, nv: u32,
+                           sch: *const slm_pair_schedule, ratio: f32, mutual: c_int, prec: SlmPrecision,
+                           min_matches: u32, pairs_out: *mut slm_pair, pairs_cap: u64, n_pairs: *mut u64,
+                           out: *mut slm_pair, cap: u64, offsets: *mut u64, stats: *mut slm_stats) -> SlmStatus;
 }

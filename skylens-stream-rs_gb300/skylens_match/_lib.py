@@ -118,6 +118,10 @@ SIGNATURES = {
                              P(c_f32)]),
     "slm_match_batch": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int,
                                 P(SlmPair), c_u64, P(c_u64), P(SlmStats)]),
+    "slm_plan_set_min_matches": (c_int, [ctypes.c_void_p, c_u32]),
+    "slm_match_pairs": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(c_u64), c_u32, P(SlmPairSchedule), c_f32, c_int,
+                                c_int, c_u32, P(SlmPair), c_u64, P(c_u64), P(SlmPair), c_u64, P(c_u64),
+                                P(SlmStats)]),
 }
 
 _lock = threading.Lock()

@@ -253,6 +253,11 @@ class BatchPlan:
         pairs, off = self.results()
         return [pairs[int(off[k]):int(off[k + 1])] for k in range(self.np)]
 
+    def set_min_matches(self, min_matches: int) -> None:
+        """match_pairs' filter (pipeline.rs:494-496): from the next launch on,
+        pairs with fewer matches report none (dropped on the device)."""
+        check(self._L.slm_plan_set_min_matches(self._h, int(min_matches)), "slm_plan_set_min_matches")
+
     def nbytes(self) -> int:
         return int(self._L.slm_plan_bytes(self._h))
 
@@ -358,3 +363,36 @@ def scheduled_pairs(views, schedule: PairSchedule | None = None) -> list[tuple[i
     vp = v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
     return _collect(lambda o, cap, n: L.slm_scheduled_pairs(vp, len(v), ctypes.byref(sch), o, cap, n),
                     "slm_scheduled_pairs")
+
+
+def match_scheduled_pairs(store: DescriptorStore, views, schedule: PairSchedule | None = None, ratio: float = 0.8,
+                          mutual: bool = True, precision="bf16", min_matches: int = 20):
+    """The matching half of match_pairs (pipeline.rs:485-496): scheduled_pairs(views,
+    schedule or PairSchedule::default()), ratio_match of every pair as one GPU batch
+    (store view i is views[i]), and the pairs with at least min_matches matches, in
+    schedule order. Returns [(i, j, (M, 2) uint32 matches)]."""
+    L = store._L
+    sch = (schedule or PairSchedule.default())._c()
+    v = _views_array(views)
+    vp = v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    pair_cap = max(1, len(scheduled_pairs(views, schedule)))
+    cap = max(1, sum(store.counts[: len(v)]) * 4)
+    while True:
+        pairs_out = (SlmPair * pair_cap)()
+        offsets = np.zeros(pair_cap + 1, np.uint64)
+        out = (SlmPair * cap)()
+        n = ctypes.c_uint64()
+        st = SlmStats()
+        status = L.slm_match_pairs(store.m.handle, store.handle, vp, len(v), ctypes.byref(sch), ctypes.c_float(ratio),
+                                   int(bool(mutual)), _prec(precision), int(min_matches), pairs_out, pair_cap,
+                                   ctypes.byref(n), out, cap, offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                   ctypes.byref(st))
+        if status == SLM_CAPACITY and n.value <= pair_cap and int(offsets[n.value]) > cap:
+            cap = int(offsets[n.value])  # more matches than room: once more with the count needed
+            continue
+        check(status, "slm_match_pairs")
+        store.m.last_stats = st.as_dict()
+        k = n.value
+        pr = np.frombuffer(pairs_out, dtype=np.uint32, count=2 * k).reshape(-1, 2)
+        mt = np.frombuffer(out, dtype=np.uint32, count=2 * int(offsets[k])).reshape(-1, 2)
+        return [(int(pr[q, 0]), int(pr[q, 1]), mt[int(offsets[q]):int(offsets[q + 1])].copy()) for q in range(k)]
