@@ -154,3 +154,68 @@ pub fn match_pairs<D: Descriptor>(views: &[&[D]], pairs: &[(usize, usize)], rati
         .map(|k| out[off[k] as usize..off[k + 1] as usize].iter().map(|p| (p.i as usize, p.j as usize)).collect())
         .collect()
 }
+
+/// The matching half of `pipeline::match_pairs` with its own pair set and
+/// filter (pipeline.rs:485-496): `scheduled_pairs(views,
+/// &PairSchedule::default())`, `ratio_match(fa, fb, 0.8, true)` per pair on the
+/// GPU, and the pairs with at least `min_matches` matches (20 in the pipeline),
+/// in schedule order. `imgs[v]` are the features of view v, `views[v]` its
+/// (camera, position).
+pub fn match_scheduled_pairs<D: Descriptor>(imgs: &[&[D]], views: &[(usize, usize)], min_matches: u32)
+                                            -> Vec<(usize, usize, Vec<(usize, usize)>)> {
+    assert_eq!(imgs.len(), views.len(), "one feature list per view");
+    let c = ctx();
+    let total: usize = imgs.iter().map(|v| v.len()).sum();
+    let mut store = std::ptr::null_mut();
+    check(unsafe { sys::slm_store_create(c, total as u64, imgs.len() as u32, &mut store) }, "slm_store_create");
+    let mut desc = Vec::with_capacity(total * 128);
+    let (mut offsets, mut counts) = (Vec::new(), Vec::new());
+    for v in imgs {
+        offsets.push((desc.len() / 128) as u64);
+        counts.push(v.len() as u32);
+        desc.extend(pack(v));
+    }
+    check(
+        unsafe {
+            sys::slm_store_add_views(store, desc.as_ptr(), offsets.as_ptr(), counts.as_ptr(), imgs.len() as u32,
+                                     std::ptr::null_mut())
+        },
+        "slm_store_add_views",
+    );
+    let flat: Vec<u64> = views.iter().flat_map(|&(c, p)| [c as u64, p as u64]).collect();
+    let sch = unsafe { sys::slm_pair_schedule_default() };
+    let mut np = 0u64;
+    let st = unsafe {
+        sys::slm_scheduled_pairs(flat.as_ptr(), views.len() as u32, &sch, std::ptr::null_mut(), 0, &mut np)
+    };
+    if st != sys::SLM_CAPACITY && st != sys::SLM_OK {
+        unsafe { sys::slm_store_destroy(store) };
+        check(st, "slm_scheduled_pairs");
+    }
+    let mut sched = vec![sys::slm_pair::default(); (np as usize).max(1)];
+    check(
+        unsafe {
+            sys::slm_scheduled_pairs(flat.as_ptr(), views.len() as u32, &sch, sched.as_mut_ptr(), np, &mut np)
+        },
+        "slm_scheduled_pairs",
+    );
+    // a row matches at most once: the rows of every pair's first view bound the matches
+    let cap = sched[..np as usize].iter().map(|p| imgs[p.i as usize].len()).sum::<usize>().max(1);
+    let mut pairs_out = vec![sys::slm_pair::default(); (np as usize).max(1)];
+    let mut off = vec![0u64; pairs_out.len() + 1];
+    let mut out = vec![sys::slm_pair::default(); cap];
+    let mut kept = 0u64;
+    let st = unsafe {
+        sys::slm_match_pairs(c, store, flat.as_ptr(), views.len() as u32, &sch, 0.8, 1,
+                             sys::SLM_PREC_BF16, min_matches, pairs_out.as_mut_ptr(), pairs_out.len() as u64,
+                             &mut kept, out.as_mut_ptr(), cap as u64, off.as_mut_ptr(), std::ptr::null_mut())
+    };
+    unsafe { sys::slm_store_destroy(store) };
+    check(st, "slm_match_pairs");
+    (0..kept as usize)
+        .map(|k| {
+            let m = out[off[k] as usize..off[k + 1] as usize].iter().map(|p| (p.i as usize, p.j as usize)).collect();
+            (pairs_out[k].i as usize, pairs_out[k].j as usize, m)
+        })
+        .collect()
+}
