@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(128) pack_lowp_kernel(const uint4 *__restrict_
     const uint32_t row = tile * kTile + r;  // row within the view
     const bool valid = row < n;
     const float *src = raw + (size_t)(row0 + row) * kDesc;
-    constexpr uint32_t kTileBytes = FP8 ? kFp8TileBytes : kBf16TileBytes;
+    constexpr uint32_t kTileBytes = FP8 ? kFp8TileBytes : kBf16TileStride;
     uint8_t *dst = optiles + (size_t)(row0 / kTile + tile) * kTileBytes;
     float x[kDesc];
 #pragma unroll
@@ -274,6 +274,19 @@ __global__ void __launch_bounds__(128) pack_lowp_kernel(const uint4 *__restrict_
             *d = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+    if constexpr (!FP8) {
+        // norm extension (slm_shortlist.h): |a|^2 / 2 = hi + lo (the difference
+        // of a float and its bf16 rounding is exact in f32); padding rows stay 0
+        const float half = valid ? 0.5f * nrm : 0.f;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(half);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(half - __bfloat162float(hi));
+        const uint32_t hl = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+        const uint32_t ones = valid ? 0x3f803f80u : 0u;  // two bf16 1.0
+        uint8_t *ext = dst + kBf16TileBytes + (r >> 3) * 384 + (r & 7) * 16;
+        *reinterpret_cast<uint4 *>(ext) = make_uint4(hl, ones, 0u, 0u);        // kc0: hi lo 1 1
+        *reinterpret_cast<uint4 *>(ext + 128) = make_uint4(ones, hl, 0u, 0u);  // kc1: 1 1 hi lo
+        *reinterpret_cast<uint4 *>(ext + 256) = make_uint4(0u, 0u, 0u, 0u);    // kc2
+    }
     norms[row0 + row] = valid ? nrm : 0.f;
     if constexpr (FP8) qscale[row0 + row] = inv;
     // statistics (non-negative floats compare as their bit patterns)
@@ -319,20 +332,35 @@ SLM_DEV uint64_t umma_desc(uint32_t saddr) {
     return d;
 }
 
+// Shared-memory matrix descriptor: K-major without swizzle. Core matrices of
+// 8 rows x 16 bytes (rows 16 bytes apart); lbo = bytes between core matrices
+// along K, sbo = bytes between 8-row groups.
+SLM_DEV uint64_t umma_desc_plain(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3fffu);
+    d |= (uint64_t)((lbo >> 4) & 0x3fffu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3fffu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version; layout type 0 = no swizzle
+    return d;
+}
+
 // Instruction descriptor: f32 accumulate, K-major A and B, M=128, N=128.
-// kind::f16 with bf16 inputs (format 1) or kind::f8f6f4 with e4m3 (format 0).
-__host__ __device__ constexpr uint32_t umma_idesc(bool fp8) {
-    return (1u << 4) | ((fp8 ? 0u : 1u) << 7) | ((fp8 ? 0u : 1u) << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// kind::f16 with bf16 inputs (format 1) or kind::f8f6f4 with e4m3 (format 0);
+// negate_b (bit 14) negates operand B.
+__host__ __device__ constexpr uint32_t umma_idesc(bool fp8, bool negate_b = false) {
+    return (1u << 4) | ((fp8 ? 0u : 1u) << 7) | ((fp8 ? 0u : 1u) << 10) | ((negate_b ? 1u : 0u) << 14) |
+           ((128u >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 template <bool FP8>
 struct SlSmem {
-    static constexpr uint32_t kOp = FP8 ? kFp8TileBytes : kBf16TileBytes;
+    static constexpr uint32_t kOp = FP8 ? kFp8TileBytes : kBf16TileStride;  // bytes per operand tile
+    static constexpr int kStages = FP8 ? kSlStages : 3;                      // b-tile ring depth
     uint8_t A[2][kOp];
-    uint8_t B[kSlStages][kOp];
-    float bnorm[kSlStages][128];
-    float bthr[kSlStages][128];
-    float bscale[kSlStages][128];
+    uint8_t B[kStages][kOp];
+    float bnorm[kStages][128];  // FP8 only (BF16 carries the norms in the operands)
+    float bthr[kStages][128];
+    float bscale[kStages][128];
     float anorm[256];
     float athr[256];
     float ascale[256];
@@ -340,7 +368,7 @@ struct SlSmem {
     float2 rowx[256];          // pass 1: the second column half's row state
     uint32_t rownear[256];     // pass 1: the second column half's near-chunk count
     uint64_t a_full, a_empty;
-    uint64_t b_full[kSlStages], b_empty[kSlStages];
+    uint64_t b_full[kStages], b_empty[kStages];
     uint64_t t_full[2], t_empty[2];
     uint64_t ep_bar;  // epilogue warps: column partials of a tile are stored
     uint32_t tmem_base;
@@ -384,6 +412,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
     const uint32_t pad = (1024u - (smem_u32(sl_smem_raw) & 1023u)) & 1023u;
     SlSmem<FP8> &S = *reinterpret_cast<SlSmem<FP8> *>(sl_smem_raw + pad);
     constexpr uint32_t kOp = SlSmem<FP8>::kOp;
+    constexpr int kStg = SlSmem<FP8>::kStages;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *err = g.ctl + 1;
     volatile uint32_t *abort_flag = &S.abort_flag;
@@ -391,7 +420,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
     if (threadIdx.x == 0) {
         mbar_init(&S.a_full, 1);
         mbar_init(&S.a_empty, 1 + kSlEpWarps);
-        for (int s = 0; s < kSlStages; ++s) {
+        for (int s = 0; s < kStg; ++s) {
             mbar_init(&S.b_full[s], 1);
             mbar_init(&S.b_empty[s], 1 + kSlEpWarps);
         }
@@ -423,13 +452,13 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                 if (PASS == 2 && sp.routed) continue;
                 if (iter > 0 && !sl_wait(&S.a_empty, (iter - 1) & 1, abort_flag, err)) break;
                 const uint32_t arow = pm.a_row0 + item.rt0 * kTile;  // store row of the first a row
-                uint32_t bytes = item.nat * kOp + item.nat * 512;
+                uint32_t bytes = item.nat * kOp;
                 if (PASS == 2) bytes += item.nat * 512;
-                if (FP8) bytes += item.nat * 512;
+                if (FP8) bytes += item.nat * 1024;  // norms and scales
                 mbar_arrive_expect_tx(&S.a_full, bytes);
                 for (uint32_t a = 0; a < item.nat; ++a) {
                     bulk_g2s(S.A[a], g.optiles + (size_t)(arow / kTile + a) * kOp, kOp, &S.a_full);
-                    bulk_g2s(&S.anorm[a * 128], g.norms + arow + a * 128, 512, &S.a_full);
+                    if (FP8) bulk_g2s(&S.anorm[a * 128], g.norms + arow + a * 128, 512, &S.a_full);
                     if (PASS == 2)
                         bulk_g2s(&S.athr[a * 128], g.rowthr + sp.rbase + (item.rt0 + a) * kTile, 512, &S.a_full);
                     if (FP8) bulk_g2s(&S.ascale[a * 128], g.qscale + arow + a * 128, 512, &S.a_full);
@@ -437,13 +466,13 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                 for (uint32_t t = item.ct0; t < item.ct1; ++t) {
                     if (!sl_wait(&S.b_empty[st], sph ^ 1, abort_flag, err)) break;
                     const uint32_t brow = pm.b_row0 + t * kTile;
-                    uint32_t bb = kOp + 512 + (PASS == 2 ? 512 : 0) + (FP8 ? 512 : 0);
+                    uint32_t bb = kOp + (PASS == 2 ? 512 : 0) + (FP8 ? 1024 : 0);
                     mbar_arrive_expect_tx(&S.b_full[st], bb);
                     bulk_g2s(S.B[st], g.optiles + (size_t)(brow / kTile) * kOp, kOp, &S.b_full[st]);
-                    bulk_g2s(S.bnorm[st], g.norms + brow, 512, &S.b_full[st]);
+                    if (FP8) bulk_g2s(S.bnorm[st], g.norms + brow, 512, &S.b_full[st]);
                     if (PASS == 2) bulk_g2s(S.bthr[st], g.colthr + sp.cbase + t * kTile, 512, &S.b_full[st]);
                     if (FP8) bulk_g2s(S.bscale[st], g.qscale + brow, 512, &S.b_full[st]);
-                    if (++st == kSlStages) st = 0, sph ^= 1;
+                    if (++st == kStg) st = 0, sph ^= 1;
                 }
                 ++iter;
                 if (*abort_flag) break;
@@ -452,6 +481,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA issue
         constexpr uint32_t idesc = umma_idesc(FP8);
+        constexpr uint32_t idesc_neg = umma_idesc(FP8, true);
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
@@ -475,17 +505,20 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 mma_f8(d_tmem, umma_desc(abase + k * 32), umma_desc(bbase + k * 32), idesc, k > 0);
                         } else {
 #pragma unroll
-                            for (int k = 0; k < 8; ++k) {  // K = 16 bf16 = 32 bytes per step
+                            for (int k = 0; k < 8; ++k) {  // K = 16 bf16 = 32 bytes per step; -a.b
                                 const uint32_t off = (k >> 2) * 16384 + (k & 3) * 32;
-                                mma_f16(d_tmem, umma_desc(abase + off), umma_desc(bbase + off), idesc, k > 0);
+                                mma_f16(d_tmem, umma_desc(abase + off), umma_desc(bbase + off), idesc_neg, k > 0);
                             }
+                            // + (|a|^2 + |b|^2) / 2: A from kc0, B from kc1 of the norm extension
+                            mma_f16(d_tmem, umma_desc_plain(abase + kBf16TileBytes, 128, 384),
+                                    umma_desc_plain(bbase + kBf16TileBytes + 128, 128, 384), idesc, true);
                         }
                     }
                     mma_commit(&S.b_empty[st]);
                     mma_commit(&S.t_full[tb]);
                 }
                 __syncwarp();
-                if (++st == kSlStages) st = 0, sph ^= 1;
+                if (++st == kStg) st = 0, sph ^= 1;
                 tb ^= 1;
                 if (tb == 0) tph ^= 1;
             }
@@ -508,6 +541,10 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0, eph = 0;
         const float kInf = __int_as_float(0x7f800000);
+        // BF16 accumulators hold d~ / 2 (norms folded into the product): the
+        // epilogue compares in that domain and scales by 2 (exact) where values
+        // leave the kernel; FP8 computes d~ itself
+        constexpr float kDom = FP8 ? 1.f : 2.f;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
             const PairMeta pm = g.pairs[item.pair];
@@ -521,8 +558,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             const bool qvalid = active && (item.rt0 + at) * kTile + q * 32 < pm.na;
             const uint32_t i = item.rt0 * kTile + r;          // row within the pair
             const bool rvalid = active && i < pm.na;
-            const float na_i = active ? S.anorm[r] : 0.f;
-            const float thr_i = (PASS == 2 && active) ? S.athr[r] : -kInf;
+            const float na_i = (FP8 && active) ? S.anorm[r] : 0.f;
+            const float thr_i = (PASS == 2 && active) ? S.athr[r] * (1.f / kDom) : -kInf;
             const float sa_i = (FP8 && active) ? S.ascale[r] : 1.f;
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_empty);
@@ -553,8 +590,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                         const uint32_t j0 = t * kTile + cb;    // column within the pair
                         if (j0 >= pm.nb) return;               // padding only (warp-uniform)
                         float d[16];
-                        const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][cb]);
                         if constexpr (FP8) {
+                            const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][cb]);
                             const float4 *bs4 = reinterpret_cast<const float4 *>(&S.bscale[st][cb]);
                             const float m2sa = -2.f * sa_i;
 #pragma unroll
@@ -566,18 +603,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                     d[4 * k4 + e] = fmaf(__uint_as_float(vc[4 * k4 + e]), m2sa * sbv[e], na_i + nbv[e]);
                             }
                         } else {
-                            const u64x na2 = f2_pack(na_i, na_i), m22 = f2_pack(-2.f, -2.f);
 #pragma unroll
-                            for (int k4 = 0; k4 < 4; ++k4) {
-                                const ulonglong2 nb = *reinterpret_cast<const ulonglong2 *>(&bn4[k4]);
-                                const u64x w0 = f2_add(na2, nb.x), w1 = f2_add(na2, nb.y);
-                                const u64x d0 = f2_fma(f2_pack(__uint_as_float(vc[4 * k4]), __uint_as_float(vc[4 * k4 + 1])), m22, w0);
-                                const u64x d1 = f2_fma(f2_pack(__uint_as_float(vc[4 * k4 + 2]), __uint_as_float(vc[4 * k4 + 3])), m22, w1);
-                                d[4 * k4 + 0] = f2_lo(d0);
-                                d[4 * k4 + 1] = f2_hi(d0);
-                                d[4 * k4 + 2] = f2_lo(d1);
-                                d[4 * k4 + 3] = f2_hi(d1);
-                            }
+                            for (int k = 0; k < 16; ++k) d[k] = __uint_as_float(vc[k]);  // d~ / 2
                         }
                         if (j0 + 16 > pm.nb) {
                             // ragged last tile: padding columns never win. Pass 1
@@ -594,7 +621,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                             if (DUMP && item.pair == 0 && rvalid) {
 #pragma unroll
                                 for (int k = 0; k < 16; ++k)
-                                    if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = d[k];
+                                    if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = kDom * d[k];
                             }
                             const float cm = min16(d);
                             // FP8 only: the bf16 bound is too tight for rows to go wide
@@ -631,7 +658,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                                 for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
                                                     const bool hit = d[k] <= thr_i;
                                                     st_pair_if(cand + min(ncand, (uint32_t)kSlHalfSlots - 1), j0 + k,
-                                                               __float_as_uint(d[k]), hit && ncand < kSlHalfSlots);
+                                                               __float_as_uint(kDom * d[k]), hit && ncand < kSlHalfSlots);
                                                     ncand += hit ? 1u : 0u;
                                                 }
                                             } else {
@@ -642,7 +669,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                                     if (d[k] <= thr_i && ncand <= kSlHalfSlots) {
                                                         const uint32_t sl = atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
                                                         if (sl < kSlHalfSlots)
-                                                            cand[sl] = make_uint2(j0 + k, __float_as_uint(d[k]));
+                                                            cand[sl] = make_uint2(j0 + k, __float_as_uint(kDom * d[k]));
                                                         ncand = sl + 1;
                                                     }
                                                 }
@@ -656,9 +683,17 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 float x[16];
 #pragma unroll
                                 for (int k4 = 0; k4 < 4; ++k4) {
+                                    // x = d - thr in the accumulator domain (the sign is exact)
                                     const ulonglong2 tt = bt2[k4];
-                                    const u64x x0 = f2_sub(f2_pack(d[4 * k4], d[4 * k4 + 1]), tt.x);
-                                    const u64x x1 = f2_sub(f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]), tt.y);
+                                    u64x x0, x1;
+                                    if constexpr (FP8) {
+                                        x0 = f2_sub(f2_pack(d[4 * k4], d[4 * k4 + 1]), tt.x);
+                                        x1 = f2_sub(f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]), tt.y);
+                                    } else {
+                                        const u64x mhalf = f2_pack(-0.5f, -0.5f);
+                                        x0 = f2_fma(tt.x, mhalf, f2_pack(d[4 * k4], d[4 * k4 + 1]));
+                                        x1 = f2_fma(tt.y, mhalf, f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]));
+                                    }
                                     x[4 * k4 + 0] = f2_lo(x0);
                                     x[4 * k4 + 1] = f2_hi(x0);
                                     x[4 * k4 + 2] = f2_lo(x1);
@@ -710,12 +745,12 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 (item.rt0 + (cmb >> 2)) * kTile + (cmb & 3) * 32 < pm.na)  // quarter has rows
                                 m = fminf(m, S.colpart[tb][cmb][e]);
                         const uint32_t j = t * kTile + e;
-                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(m));
+                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(kDom * m));
                     }
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.b_empty[st]);
-                if (++st == kSlStages) st = 0, sph ^= 1;
+                if (++st == kStg) st = 0, sph ^= 1;
                 tb ^= 1;
                 if (tb == 0) tph ^= 1;
             }
@@ -736,7 +771,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     m1 = fminf(m1, o.x);
                     // slot = row within its 256-row group (items of one 128-row tile start mid-group)
                     const size_t slot = (size_t)item.part * 256 + (i & 255u);
-                    g.rowpart[slot] = make_float2(m1, m2);
+                    g.rowpart[slot] = make_float2(kDom * m1, kDom * m2);
                     g.rownear[slot] = near + S.rownear[r];
                 }
             } else {
@@ -772,6 +807,10 @@ __global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
     // |a.b - q(a).q(b)| <= |a - q(a)| |b| + |q(a)| |b - q(b)| (Cauchy-Schwarz).
     double eps = 2.0 * (Ra * B + Qa * Rb) * (1.0 + 1e-3);
     eps += 5e-4 * Qa * Qb + 5e-5 * (A * A + B * B) + 2e-5 * (A + B) * (A + B) + 1e-6;
+    // BF16: the tensor core also accumulates the folded norms (|a|^2 + |b|^2) / 2
+    // and their bf16 split (relative 2^-17); the accumulation is taken as no
+    // better than 2^-11 relative to that magnitude, doubled with d~
+    if (!g.fp8) eps += 5e-4 * (A * A + B * B);
     if (!(eps < 1e30)) unsafe = true;
     sp.eps = unsafe ? __int_as_float(0x7f800000) : (float)(eps * (1.0 + 1e-6));
     sp.unsafe = unsafe ? 1u : 0u;

@@ -800,7 +800,7 @@ slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
     if (st->lowp_version == st->version && st->lowp_fp8 == (int)fp8) return SLM_OK;
     slm_ctx *c = st->ctx;
     const uint64_t tiles = std::max<uint64_t>(st->max_rows / kTile, 1);
-    const size_t tb = fp8 ? kFp8TileBytes : kBf16TileBytes;
+    const size_t tb = fp8 ? kFp8TileBytes : kBf16TileStride;
     const bool fresh = st->lowp_fp8 != (int)fp8 || st->lowp_epoch != st->epoch;
     size_t first = fresh ? 0 : st->lowp_views;
     SLM_TRY(st->optiles.ensure(c, tiles * tb));

@@ -53,8 +53,19 @@ constexpr int kSlEpWarps = 16;     // epilogue warps
 constexpr int kSlThreads = 32 * (2 + kSlEpWarps);  // producer, MMA, epilogue
 
 // Operand tile sizes per 128 descriptors.
-constexpr uint32_t kBf16TileBytes = 128 * 128 * 2;  // 32 KiB, 128B-swizzled, K-major
-constexpr uint32_t kFp8TileBytes = 128 * 128;       // 16 KiB
+//
+// BF16 tiles carry the squared norms into the tensor-core product: after the
+// 32 KiB K-major 128B-swizzled image of the components comes a 6 KiB
+// extension, K-major without swizzle, with three 16-byte core-matrix columns
+// per row: kc0 = [hi, lo, 1, 1, 0..], kc1 = [1, 1, hi, lo, 0..], kc2 = 0, where
+// hi + lo is |v|^2 / 2 split into two bf16. A tile read as operand A from kc0
+// and as operand B from kc1 contributes (|a|^2 + |b|^2) / 2 in one K = 16 step;
+// the 8 steps over the components run with B negated, so the accumulator holds
+// d~ / 2 = (|a|^2 + |b|^2) / 2 - a.b directly.
+constexpr uint32_t kBf16TileBytes = 128 * 128 * 2;                    // 32 KiB components
+constexpr uint32_t kBf16ExtBytes = 16 * 3 * 128;                      // 6 KiB: 16 row groups x 3 core matrices
+constexpr uint32_t kBf16TileStride = kBf16TileBytes + kBf16ExtBytes;  // 38 KiB per tile (1024-byte multiple)
+constexpr uint32_t kFp8TileBytes = 128 * 128;                         // 16 KiB
 
 // Per view, from the pack kernel: float bits of non-negative maxima
 // (atomicMax on the bit pattern orders them), and a non-finite flag.

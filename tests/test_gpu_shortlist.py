@@ -31,6 +31,8 @@ def eps_bound(a, b, prec):
     Qa, Qb = np.linalg.norm(qa, axis=1).max(), np.linalg.norm(qb, axis=1).max()
     eps = 2 * (Ra * B + Qa * Rb) * (1 + 1e-3)
     eps += 5e-4 * Qa * Qb + 5e-5 * (A * A + B * B) + 2e-5 * (A + B) ** 2 + 1e-6
+    if prec == "bf16":  # the norms are folded into the tensor-core product
+        eps += 5e-4 * (A * A + B * B)
     return eps
 
 
