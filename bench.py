@@ -450,20 +450,25 @@ def main():
     e2e = None
     out_bytes = 0
     if not args.no_e2e:
+        # the match lists come back into pinned host buffers through slm_plan_results
+        out_h = torch.empty((max(plan.total_rows, 1), 2), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        off_h = torch.empty(len(z.pairs) + 1, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
         for _ in range(2):
             store.clear()
             store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
             plan.launch()
-            plan.results()
+            total = plan.results_into(out_h, off_h)
+        ref_pr, ref_of = plan.results()
+        assert total == int(ref_of[-1]) and np.array_equal(out_h[:total], ref_pr)
         t = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
             store.clear()
             store.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
             plan.launch()
-            pr, of = plan.results()
+            total = plan.results_into(out_h, off_h)
             t.append(time.perf_counter() - t0)
-            out_bytes = pr.nbytes + of.nbytes
+            out_bytes = total * 8 + off_h.nbytes
         e2e_s = float(np.mean(t))
         e2e = {"value": ws * len(z.pairs) / e2e_s, "unit": "image pairs/s", "ms_per_step": 1e3 * e2e_s,
                "h2d_bytes_per_step": int(z.desc.nbytes), "d2h_bytes_per_step": int(out_bytes)}

@@ -91,6 +91,36 @@ __global__ void fill_u32_kernel(uint32_t *p, uint64_t n, uint32_t v) {
         p[i] = v;
 }
 
+// Rows of many views from one staging buffer into their padded store rows.
+// The table travels as the kernel parameter (no upload):
+// e[v] = {first staging row, first store row, rows, 0}; blockIdx.x = view,
+// blockIdx.y strides over its rows.
+constexpr uint32_t kScatterMax = 1024;
+struct ScatterTab {
+    uint4 e[kScatterMax];
+};
+
+__global__ void __launch_bounds__(256) scatter_rows_kernel(const ScatterTab tab, const float4 *__restrict__ src,
+                                                           float4 *__restrict__ dst) {
+    const uint4 t = tab.e[blockIdx.x];
+    constexpr uint32_t kRow4 = 128 / 4;  // float4 per descriptor
+    const uint64_t n4 = (uint64_t)t.z * kRow4;
+    const float4 *s = src + (uint64_t)t.x * kRow4;
+    float4 *d = dst + (uint64_t)t.y * kRow4;
+    for (uint64_t k = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x; k < n4; k += (uint64_t)gridDim.y * blockDim.x)
+        d[k] = s[k];
+}
+
+void launch_scatter_rows(const uint4 *tab, uint32_t n, const float *src, float *dst, cudaStream_t s) {
+    for (uint32_t b = 0; b < n; b += kScatterMax) {
+        const uint32_t m = n - b < kScatterMax ? n - b : kScatterMax;
+        ScatterTab t;
+        for (uint32_t k = 0; k < m; ++k) t.e[k] = tab[b + k];
+        scatter_rows_kernel<<<dim3(m, 8), 256, 0, s>>>(t, reinterpret_cast<const float4 *>(src),
+                                                         reinterpret_cast<float4 *>(dst));
+    }
+}
+
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s) {
     if (!n) return;
     uint64_t blocks = (n + 255) / 256;

@@ -168,6 +168,7 @@ struct slm_store {
     uint64_t fp32_epoch = ~0ull;             // FP32 tiles, built lazily the same way
     size_t fp32_views = 0;
     DevBuf tiletab;                          // {row0, n, tile, view} per tile to pack
+    DevBuf staging;                          // slm_store_add_views: the host rows, before the scatter
     DevBuf optiles, norms, qscale, vstats;
 };
 
@@ -216,6 +217,7 @@ struct slm_plan {
 // Dense compaction of per-pair slots (device) into out + offsets.
 namespace slm {
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s);
+void launch_scatter_rows(const uint4 *tab, uint32_t n, const float *src, float *dst, cudaStream_t s);
 void launch_filter_counts(uint32_t *counts, uint32_t np, uint32_t min_matches, cudaStream_t s);
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s);
 void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
@@ -573,25 +575,37 @@ slm_status store_reserve(slm_store *st, uint64_t rows) {
     return SLM_OK;
 }
 
-slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool device_src, cudaStream_t s,
-                        uint32_t *id) {
-    const uint64_t padded = pad_rows(n);
-    if (st->row0.size() >= st->max_views && st->max_views)
+// Room for `views` more views of `padded` rows in total.
+slm_status store_check_room(const slm_store *st, uint64_t views, uint64_t padded) {
+    if (st->max_views && st->row0.size() + views > st->max_views)
         return fail(SLM_CAPACITY, "store view capacity " + std::to_string(st->max_views) + " reached");
     if (st->rows_used + padded > st->max_rows)
         return fail(SLM_CAPACITY, "store descriptor capacity exceeded: " + std::to_string(st->rows_used + padded) +
                                       " > " + std::to_string(st->max_rows) + " padded rows");
     if (st->rows_used + padded >= (1ull << 32)) return fail(SLM_CAPACITY, "store exceeds 2^32 rows");
+    return SLM_OK;
+}
+
+// Bookkeeping of one appended view of n rows; returns its first store row.
+uint64_t store_place(slm_store *st, uint32_t n, uint32_t *id) {
+    const uint64_t row0 = st->rows_used;
+    if (id) *id = (uint32_t)st->row0.size();
+    st->row0.push_back((uint32_t)row0);
+    st->n.push_back(n);
+    st->rows_used += pad_rows(n);
+    st->version++;
+    return row0;
+}
+
+slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool device_src, cudaStream_t s,
+                        uint32_t *id) {
+    SLM_TRY(store_check_room(st, 1, pad_rows(n)));
     float *raw = st->raw.as<float>() + st->rows_used * kDesc;
     if (n) {
         SLM_CU(cudaMemcpyAsync(raw, desc, (size_t)n * kDesc * sizeof(float),
                                device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
     }
-    if (id) *id = (uint32_t)st->row0.size();
-    st->row0.push_back((uint32_t)st->rows_used);
-    st->n.push_back(n);
-    st->rows_used += padded;
-    st->version++;
+    store_place(st, n, id);
     return SLM_OK;
 }
 
@@ -740,14 +754,39 @@ extern "C" slm_status slm_store_add_view(slm_store *st, const float *desc, uint3
     return store_append(st, desc, n, false, st->ctx->stream, view_id);
 }
 
+// Many views from one host buffer: one host-to-device copy of the rows they
+// span into a staging buffer, then one kernel launch per 1024 views scatters
+// them into their padded store rows (instead of one copy per view, each with
+// its own call overhead). All views are checked for room before any is added.
 extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets,
                                           const uint32_t *counts, uint32_t nviews, uint32_t *ids) {
     if (!st || (!desc && nviews) || (nviews && (!offsets || !counts))) return fail(SLM_INVALID_ARG, "NULL argument");
     SLM_TRY(ctx_check_device(st->ctx));
+    uint64_t lo = ~0ull, hi = 0, padded = 0;
+    for (uint32_t v = 0; v < nviews; ++v) {
+        padded += pad_rows(counts[v]);
+        if (!counts[v]) continue;
+        lo = std::min<uint64_t>(lo, offsets[v]);
+        hi = std::max<uint64_t>(hi, offsets[v] + counts[v]);
+    }
+    SLM_TRY(store_check_room(st, nviews, padded));
+    cudaStream_t s = st->ctx->stream;
+    if (hi > lo) {
+        SLM_TRY(st->staging.ensure(st->ctx, (size_t)(hi - lo) * kDesc * sizeof(float)));
+        SLM_CU(cudaMemcpyAsync(st->staging.p, desc + lo * kDesc, (size_t)(hi - lo) * kDesc * sizeof(float),
+                               cudaMemcpyHostToDevice, s));
+    }
+    std::vector<uint4> tab;  // {first staging row, first store row, rows, 0}
+    tab.reserve(nviews);
     for (uint32_t v = 0; v < nviews; ++v) {
         uint32_t id = 0;
-        SLM_TRY(store_append(st, desc + offsets[v] * kDesc, counts[v], false, st->ctx->stream, &id));
+        const uint64_t row0 = store_place(st, counts[v], &id);
         if (ids) ids[v] = id;
+        if (counts[v]) tab.push_back(make_uint4((uint32_t)(offsets[v] - lo), (uint32_t)row0, counts[v], 0u));
+    }
+    if (!tab.empty()) {
+        launch_scatter_rows(tab.data(), (uint32_t)tab.size(), st->staging.as<float>(), st->raw.as<float>(), s);
+        SLM_CU(cudaGetLastError());
     }
     return SLM_OK;
 }

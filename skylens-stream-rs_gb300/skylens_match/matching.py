@@ -13,6 +13,7 @@ SlmError (there is no CPU fallback).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import threading
 import weakref
@@ -51,6 +52,20 @@ def _pairs_array(pairs) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(pairs, dtype=np.uint32).reshape(-1, 2))
 
 
+_live_matchers: "weakref.WeakSet[Matcher]" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_matchers() -> None:
+    """Free contexts (and their stores and plans) while the CUDA runtime is
+    still up: objects left to interpreter shutdown would be freed after it."""
+    for m in list(_live_matchers):
+        try:
+            m.close()
+        except Exception:
+            pass
+
+
 class Matcher:
     """A libslm context on one CUDA device (thread-safe)."""
 
@@ -62,6 +77,7 @@ class Matcher:
         self._h = h
         self.last_stats: dict | None = None
         self._stores = weakref.WeakSet()  # closed before the context
+        _live_matchers.add(self)
 
     @property
     def handle(self):
@@ -248,6 +264,19 @@ class BatchPlan:
         total = int(offsets[-1])
         pairs = np.frombuffer(self._out, dtype=np.uint32, count=2 * total).reshape(-1, 2).copy()
         return pairs, offsets
+
+    def results_into(self, out: np.ndarray, offsets: np.ndarray) -> int:
+        """slm_plan_results straight into caller buffers (no copy): out is a
+        C-contiguous (cap, 2) uint32 array (pinned memory reads back fastest),
+        offsets a (np + 1,) uint64 array. Returns the number of matches."""
+        assert out.dtype == np.uint32 and out.ndim == 2 and out.shape[1] == 2 and out.flags.c_contiguous
+        assert offsets.dtype == np.uint64 and offsets.shape == (self.np + 1,) and offsets.flags.c_contiguous
+        st = SlmStats()
+        check(self._L.slm_plan_results(self._h, out.ctypes.data_as(ctypes.POINTER(SlmPair)), len(out),
+                                       offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.byref(st)),
+              "slm_plan_results")
+        self.stats = st.as_dict()
+        return int(offsets[-1])
 
     def per_pair(self):
         pairs, off = self.results()
