@@ -360,6 +360,7 @@ struct SlSmem {
     uint8_t B[kStages][kOp];
     float bnorm[kStages][128];  // FP8 only (BF16 carries the norms in the operands)
     float bthr[kStages][128];
+    float bthr2[kStages][128];  // pass 2, items of two pairs: the second pair's column thresholds
     float bscale[kStages][128];
     float anorm[256];
     float athr[256];
@@ -397,6 +398,15 @@ SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_fl
             }
         }
     }
+}
+
+// Items of two pairs (odd row-tile counts sharing a b view).
+SLM_DEV bool item_two_pairs(const SlItem &it) { return it.nat == 2 && it.pair[1] != it.pair[0]; }
+
+// Pass 2 skips an item when every pair it serves was routed to the exact
+// kernel (all roles read the same flags: mid wrote them).
+SLM_DEV bool item_routed(const SlArgs &g, const SlItem &it) {
+    return g.spairs[it.pair[0]].routed && (it.nat == 1 || g.spairs[it.pair[1]].routed);
 }
 
 // One CTA of kSlThreads per SM. Warps are spread over the SM's four
@@ -447,30 +457,38 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             uint32_t st = 0, sph = 0, iter = 0;  // iter: items processed (routed pairs skip pass 2)
             for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
                 const SlItem item = g.items[it];
-                const PairMeta pm = g.pairs[item.pair];
-                const SlPair sp = g.spairs[item.pair];
-                if (PASS == 2 && sp.routed) continue;
+                if (PASS == 2 && item_routed(g, item)) continue;
                 if (iter > 0 && !sl_wait(&S.a_empty, (iter - 1) & 1, abort_flag, err)) break;
-                const uint32_t arow = pm.a_row0 + item.rt0 * kTile;  // store row of the first a row
+                const bool two = item_two_pairs(item);
+                const PairMeta pm = g.pairs[item.pair[0]];  // both pairs have this b view
+                const uint32_t cbase0 = g.spairs[item.pair[0]].cbase;
+                const uint32_t cbase1 = two ? g.spairs[item.pair[1]].cbase : 0;
                 uint32_t bytes = item.nat * kOp;
                 if (PASS == 2) bytes += item.nat * 512;
                 if (FP8) bytes += item.nat * 1024;  // norms and scales
                 mbar_arrive_expect_tx(&S.a_full, bytes);
-                for (uint32_t a = 0; a < item.nat; ++a) {
-                    bulk_g2s(S.A[a], g.optiles + (size_t)(arow / kTile + a) * kOp, kOp, &S.a_full);
-                    if (FP8) bulk_g2s(&S.anorm[a * 128], g.norms + arow + a * 128, 512, &S.a_full);
+#pragma unroll
+                for (uint32_t a = 0; a < 2; ++a) {  // static indices keep the item in registers
+                    if (a >= item.nat) break;
+                    const uint32_t pa = item.pair[a];
+                    const uint32_t arow = g.pairs[pa].a_row0 + item.rt[a] * kTile;  // store row of the tile
+                    bulk_g2s(S.A[a], g.optiles + (size_t)(arow / kTile) * kOp, kOp, &S.a_full);
+                    if (FP8) bulk_g2s(&S.anorm[a * 128], g.norms + arow, 512, &S.a_full);
                     if (PASS == 2)
-                        bulk_g2s(&S.athr[a * 128], g.rowthr + sp.rbase + (item.rt0 + a) * kTile, 512, &S.a_full);
-                    if (FP8) bulk_g2s(&S.ascale[a * 128], g.qscale + arow + a * 128, 512, &S.a_full);
+                        bulk_g2s(&S.athr[a * 128], g.rowthr + g.spairs[pa].rbase + item.rt[a] * kTile, 512, &S.a_full);
+                    if (FP8) bulk_g2s(&S.ascale[a * 128], g.qscale + arow, 512, &S.a_full);
                 }
                 for (uint32_t t = item.ct0; t < item.ct1; ++t) {
                     if (!sl_wait(&S.b_empty[st], sph ^ 1, abort_flag, err)) break;
                     const uint32_t brow = pm.b_row0 + t * kTile;
-                    uint32_t bb = kOp + (PASS == 2 ? 512 : 0) + (FP8 ? 1024 : 0);
+                    uint32_t bb = kOp + (PASS == 2 ? (two ? 1024 : 512) : 0) + (FP8 ? 1024 : 0);
                     mbar_arrive_expect_tx(&S.b_full[st], bb);
                     bulk_g2s(S.B[st], g.optiles + (size_t)(brow / kTile) * kOp, kOp, &S.b_full[st]);
                     if (FP8) bulk_g2s(S.bnorm[st], g.norms + brow, 512, &S.b_full[st]);
-                    if (PASS == 2) bulk_g2s(S.bthr[st], g.colthr + sp.cbase + t * kTile, 512, &S.b_full[st]);
+                    if (PASS == 2) {
+                        bulk_g2s(S.bthr[st], g.colthr + cbase0 + t * kTile, 512, &S.b_full[st]);
+                        if (two) bulk_g2s(S.bthr2[st], g.colthr + cbase1 + t * kTile, 512, &S.b_full[st]);
+                    }
                     if (FP8) bulk_g2s(S.bscale[st], g.qscale + brow, 512, &S.b_full[st]);
                     if (++st == kStg) st = 0, sph ^= 1;
                 }
@@ -485,7 +503,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
-            if (PASS == 2 && g.spairs[item.pair].routed) continue;
+            if (PASS == 2 && item_routed(g, item)) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
             ++iter;
             bool ok = true;
@@ -547,16 +565,27 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         constexpr float kDom = FP8 ? 1.f : 2.f;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
-            const PairMeta pm = g.pairs[item.pair];
-            const SlPair sp = g.spairs[item.pair];
-            if (PASS == 2 && sp.routed) continue;
+            if (PASS == 2 && item_routed(g, item)) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
             ++iter;
-            const bool active = at < (int)item.nat;          // warp-uniform
+            const bool two = item_two_pairs(item);
+            // this warp's a tile (clamped to tile 0); selects, not indexing: the
+            // item stays in registers
+            const bool mine1 = at == 1 && item.nat == 2;
+            const uint32_t pid = mine1 ? item.pair[1] : item.pair[0];
+            const PairMeta pm = g.pairs[pid];
+            const SlPair sp = g.spairs[pid];
+            // pass 1 merges the column partials of each pair of the item
+            const uint32_t na0 = g.pairs[item.pair[0]].na, na1 = two ? g.pairs[item.pair[1]].na : na0;
+            const uint32_t cb0 = g.spairs[item.pair[0]].cbase, cb1 = two ? g.spairs[item.pair[1]].cbase : cb0;
+            // warp-uniform: the warp's a tile exists and its pair is still open
+            const bool active = at < (int)item.nat && !(PASS == 2 && sp.routed);
+            const uint32_t rt = mine1 ? item.rt[1] : item.rt[0];
+            const uint32_t mypart = mine1 ? item.part[1] : item.part[0];
             // warp-uniform: this lane quarter holds at least one row of the pair
             // (quarters of padding rows skip their chunks)
-            const bool qvalid = active && (item.rt0 + at) * kTile + q * 32 < pm.na;
-            const uint32_t i = item.rt0 * kTile + r;          // row within the pair
+            const bool qvalid = active && rt * kTile + q * 32 < pm.na;
+            const uint32_t i = rt * kTile + q * 32 + lane;    // row within the pair
             const bool rvalid = active && i < pm.na;
             const float na_i = (FP8 && active) ? S.anorm[r] : 0.f;
             const float thr_i = (PASS == 2 && active) ? S.athr[r] * (1.f / kDom) : -kInf;
@@ -618,7 +647,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 if (j0 + k >= pm.nb) d[k] = pad_d;
                         }
                         if constexpr (PASS == 1) {
-                            if (DUMP && item.pair == 0 && rvalid) {
+                            if (DUMP && pid == 0 && rvalid) {
 #pragma unroll
                                 for (int k = 0; k < 16; ++k)
                                     if (j0 + k < pm.nb) g.dump[(size_t)i * pm.nb + j0 + k] = kDom * d[k];
@@ -679,7 +708,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 }
                             }
                             if (rvalid) {
-                                const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(&S.bthr[st][cb]);
+                                const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(
+                                    two && at == 1 ? &S.bthr2[st][cb] : &S.bthr[st][cb]);
                                 float x[16];
 #pragma unroll
                                 for (int k4 = 0; k4 < 4; ++k4) {
@@ -737,15 +767,24 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                         break;
                     }
                     eph ^= 1;
+                    // one thread per column and pair of the item: the minimum over
+                    // the (a tile, lane quarter) partials of that pair
                     const int e = threadIdx.x - 64;  // 0..511
-                    if (e < 128) {
+                    const int grp = e >> 7;
+                    if (e < (two ? 256 : 128)) {
+                        const int col = e & 127;
                         float m = kInf;
-                        for (int cmb = 0; cmb < 8; ++cmb)
-                            if ((cmb >> 2) < (int)item.nat &&
-                                (item.rt0 + (cmb >> 2)) * kTile + (cmb & 3) * 32 < pm.na)  // quarter has rows
-                                m = fminf(m, S.colpart[tb][cmb][e]);
-                        const uint32_t j = t * kTile + e;
-                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[sp.cbase + j], f2ord(kDom * m));
+#pragma unroll
+                        for (int cmb = 0; cmb < 8; ++cmb) {
+                            const int ca = cmb >> 2;  // a tile of the partial
+                            const uint32_t rt_c = ca ? item.rt[1] : item.rt[0];
+                            const uint32_t na_c = ca ? na1 : na0;
+                            if (ca < (int)item.nat && (!two || ca == grp) &&
+                                rt_c * kTile + (cmb & 3) * 32 < na_c)  // quarter has rows
+                                m = fminf(m, S.colpart[tb][cmb][col]);
+                        }
+                        const uint32_t j = t * kTile + col;
+                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[(grp ? cb1 : cb0) + j], f2ord(kDom * m));
                     }
                 }
                 __syncwarp();
@@ -770,7 +809,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     m2 = fminf(fminf(m2, o.y), fmaxf(m1, o.x));
                     m1 = fminf(m1, o.x);
                     // slot = row within its 256-row group (items of one 128-row tile start mid-group)
-                    const size_t slot = (size_t)item.part * 256 + (i & 255u);
+                    const size_t slot = (size_t)mypart * 256 + (i & 255u);
                     g.rowpart[slot] = make_float2(kDom * m1, kDom * m2);
                     g.rownear[slot] = near + S.rownear[r];
                 }
@@ -1460,7 +1499,7 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     x.x2 = 1;
     launch_exact(x, sms, s);
     sl_route_finalize_kernel<<<rgrid, 256, 0, s>>>(a);
-    sl_rescore_kernel<<<2 * sms, 256, 0, s>>>(a);
+    sl_rescore_kernel<<<5 * sms, 256, 0, s>>>(a);  // 40 warps per SM: latency-bound gathers
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
     sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
     return 8;

@@ -8,14 +8,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <map>
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "slm.h"
@@ -299,13 +300,15 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
                 for (uint32_t half = 0; half < 2 / per; ++half)
                 for (uint32_t ch = 0; ch < chunks; ++ch) {
                     SlItem it{};
-                    it.pair = k;
-                    it.rt0 = 2 * s2 + half;
-                    if (it.rt0 >= rt_n) continue;
-                    it.nat = std::min(per, rt_n - it.rt0);
+                    const uint32_t rt0 = 2 * s2 + half;
+                    if (rt0 >= rt_n) continue;
+                    it.nat = std::min(per, rt_n - rt0);
+                    it.pair[0] = it.pair[1] = k;
+                    it.rt[0] = rt0;
+                    it.rt[1] = rt0 + 1;
+                    it.part[0] = it.part[1] = (uint32_t)(part + s2 * chunks + ch);
                     it.ct0 = (uint32_t)((uint64_t)ct_n * ch / chunks);
                     it.ct1 = (uint32_t)((uint64_t)ct_n * (ch + 1) / chunks);
-                    it.part = (uint32_t)(part + s2 * chunks + ch);
                     if (it.ct1 > it.ct0) p->sitems.push_back(it);
                 }
             part += (uint64_t)ns * chunks;
@@ -314,6 +317,35 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
         cb += pad_rows(m.nb);
     }
     if (rb >= (1ull << 32) || cb >= (1ull << 32)) return fail(SLM_CAPACITY, "batch too large for one plan");
+    // The last row tile of a pair with an odd tile count makes a one-tile item,
+    // which leaves half of the epilogue warps idle. Two such tiles of pairs
+    // with the same b view and column range share one item.
+    if (p->tune.row_tiles != 1) {
+        std::map<std::tuple<uint32_t, uint32_t, uint32_t>, size_t> open;  // (b view, ct0, ct1) -> waiting item
+        std::vector<SlItem> merged;
+        merged.reserve(p->sitems.size());
+        std::vector<bool> gone(p->sitems.size(), false);
+        for (size_t x = 0; x < p->sitems.size(); ++x) {
+            const SlItem &it = p->sitems[x];
+            if (it.nat != 1) continue;
+            const auto key = std::make_tuple(p->spairs[it.pair[0]].view_b, it.ct0, it.ct1);
+            auto f = open.find(key);
+            if (f == open.end()) {
+                open.emplace(key, x);
+                continue;
+            }
+            SlItem &w = p->sitems[f->second];  // the waiting tile becomes tile 0
+            w.nat = 2;
+            w.pair[1] = it.pair[0];
+            w.rt[1] = it.rt[0];
+            w.part[1] = it.part[0];
+            gone[x] = true;
+            open.erase(f);
+        }
+        for (size_t x = 0; x < p->sitems.size(); ++x)
+            if (!gone[x]) merged.push_back(p->sitems[x]);
+        p->sitems.swap(merged);
+    }
     std::stable_sort(p->sitems.begin(), p->sitems.end(), [](const SlItem &x, const SlItem &y) {
         return (uint64_t)(x.ct1 - x.ct0) * x.nat > (uint64_t)(y.ct1 - y.ct0) * y.nat;
     });

@@ -76,11 +76,17 @@ struct ViewStat {
     uint32_t bad;    // nonzero: some component is not finite
 };
 
-// Work item: rows [rt0*128, rt0*128 + nat*128) of a pair (nat 1 or 2 tiles)
-// against column tiles [ct0, ct1) of b.
+// Work item: nat (1 or 2) a tiles of 128 rows against column tiles [ct0, ct1)
+// of one b view. A tile a is row tile rt[a] of pair pair[a]; its pass-1 row
+// partials go to block part[a] (slot (rt[a] * 128 + row) % 256 of it). Both
+// tiles usually belong to one pair (rt[1] = rt[0] + 1, part[1] = part[0]);
+// two pairs with the same b view and column range, each with an odd number of
+// row tiles, share an item for their last tiles, so that no item runs with
+// half of the epilogue warps idle.
 struct SlItem {
-    uint32_t pair, rt0, nat, ct0, ct1, part;
-    uint32_t pad[2];
+    uint32_t pair[2], rt[2], part[2];
+    uint32_t nat, ct0, ct1;
+    uint32_t pad[3];
 };
 
 // Per-pair extras of the shortlist path.
