@@ -1,0 +1,56 @@
+"""GPU: the descriptor store's batched upload (slm_store_add_views).
+
+Many views come from one host buffer through one host-to-device copy and a
+scatter kernel into padded store rows. Views may be empty, listed out of
+buffer order, leave gaps in the buffer or share rows; a batch that does not
+fit is refused whole, leaving the store as it was.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import skylens_match as sm
+from skylens_match import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_add_views_layouts(matcher):
+    rng = np.random.Generator(np.random.PCG64(41))
+    buf = synth.sift_like(rng, 1000)
+    # (offset, count) per view: out of order, a gap (rows 600-699 unused), an
+    # empty view, one view that overlaps another, a single row
+    spec = [(700, 300), (0, 250), (250, 0), (250, 350), (100, 200), (999, 1)]
+    st = matcher.store(sum(c for _, c in spec), len(spec))
+    ids = st.add_views_packed(buf, [o for o, _ in spec], [c for _, c in spec])
+    assert ids == list(range(len(spec)))
+    views = [buf[o:o + c] for o, c in spec]
+    pairs = [(u, v) for u in range(len(spec)) for v in range(len(spec)) if u != v]
+    for prec in ("fp32", "bf16"):
+        plan = st.plan(pairs, 0.8, True, prec)
+        plan.launch()
+        got = plan.per_pair()
+        for k, (u, v) in enumerate(pairs):
+            assert np.array_equal(got[k], O.ratio_match_np(views[u], views[v], 0.8, True, threads=8)), (prec, u, v)
+        plan.close()
+    st.close()
+
+
+def test_add_views_refused_whole(matcher):
+    rng = np.random.Generator(np.random.PCG64(42))
+    buf = synth.sift_like(rng, 300)
+    st = matcher.store(300, 3)
+    st.add_views_packed(buf, [0], [100])
+    with pytest.raises(sm.SlmError) as e:
+        st.add_views_packed(buf, [0, 100, 200], [100, 100, 100])  # four views in a store of three
+    assert "capacity" in str(e.value)
+    assert len(st) == 1
+    # the store still works and takes a batch that fits
+    assert st.add_views_packed(buf, [100, 200], [100, 100]) == [1, 2]
+    plan = st.plan([(0, 1), (2, 0)], 0.8, True, "bf16")
+    plan.launch()
+    got = plan.per_pair()
+    assert np.array_equal(got[0], O.ratio_match_np(buf[:100], buf[100:200], 0.8, True, threads=4))
+    assert np.array_equal(got[1], O.ratio_match_np(buf[200:], buf[:100], 0.8, True, threads=4))
+    plan.close()
+    st.close()
