@@ -1022,15 +1022,25 @@ __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
                 const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
                 float a1 = kInf, a2 = kInf;
                 uint32_t j1 = 0xffffffffu;
-                for (uint32_t k = 0; k < n; ++k) {
-                    const uint2 e = S[k < n0 ? k : kSlHalfSlots + (k - n0)];
-                    const float v = __uint_as_float(e.y);
-                    if (v < a1 || (v == a1 && e.x < j1)) {
-                        a2 = a1;
-                        a1 = v;
-                        j1 = e.x;
-                    } else if (v < a2) {
-                        a2 = v;
+                // four entries per step, loaded before they are used (independent loads)
+                for (uint32_t k0 = 0; k0 < n; k0 += 4) {
+                    uint2 e[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint32_t k = k0 + q;
+                        e[q] = k < n ? S[k < n0 ? k : kSlHalfSlots + (k - n0)] : make_uint2(0xffffffffu, 0x7f800000u);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (k0 + q >= n) break;
+                        const float v = __uint_as_float(e[q].y);
+                        if (v < a1 || (v == a1 && e[q].x < j1)) {
+                            a2 = a1;
+                            a1 = v;
+                            j1 = e[q].x;
+                        } else if (v < a2) {
+                            a2 = v;
+                        }
                     }
                 }
                 // S holds every column with d~ <= T, T >= (second smallest d~) + 2 eps,
