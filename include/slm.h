@@ -51,8 +51,14 @@ typedef enum {
 typedef enum {
     SLM_PREC_FP32 = 0, /* plain exact FP32 kernel */
     SLM_PREC_BF16 = 1, /* tcgen05 BF16 shortlist + exact FP32 rescore */
-    SLM_PREC_FP8 = 2   /* tcgen05 FP8 E4M3 shortlist + exact FP32 rescore */
+    SLM_PREC_FP8 = 2,  /* tcgen05 FP8 E4M3 shortlist + exact FP32 rescore */
+    SLM_PREC_AUTO = 3  /* BF16 from SLM_AUTO_BF16_DISTANCES distances up (one call or one
+                          batch), FP32 below, where the shortlist's fixed cost dominates */
 } slm_precision;
+
+/* SLM_PREC_AUTO's switch point, measured on GB300 through slm_ratio_match:
+ * 2048 x 2048 descriptors FP32 0.24 ms / BF16 0.28 ms, 3072 x 3072 0.36 / 0.34 ms. */
+#define SLM_AUTO_BF16_DISTANCES 6000000ull
 
 typedef struct {
     uint32_t i, j;

@@ -680,6 +680,23 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
     return SLM_OK;
 }
 
+bool prec_valid(slm_precision p) {
+    return p == SLM_PREC_FP32 || p == SLM_PREC_BF16 || p == SLM_PREC_FP8 || p == SLM_PREC_AUTO;
+}
+
+// SLM_PREC_AUTO for a call or batch of `distances` distances.
+slm_precision resolve_prec(slm_precision p, uint64_t distances) {
+    if (p != SLM_PREC_AUTO) return p;
+    return distances >= SLM_AUTO_BF16_DISTANCES ? SLM_PREC_BF16 : SLM_PREC_FP32;
+}
+
+uint64_t batch_distances(const slm_store *st, const slm_pair *pairs, uint32_t np) {
+    uint64_t d = 0;
+    for (uint32_t k = 0; k < np; ++k)
+        if (pairs[k].i < st->n.size() && pairs[k].j < st->n.size()) d += (uint64_t)st->n[pairs[k].i] * st->n[pairs[k].j];
+    return d;
+}
+
 slm_status validate_ratio(float ratio) {
     if (!std::isfinite(ratio)) return fail(SLM_INVALID_ARG, "ratio must be finite");
     return SLM_OK;
@@ -902,6 +919,7 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
     p->np = np;
     p->ratio = ratio;
     p->mutual = mutual ? 1 : 0;
+    prec = resolve_prec(prec, prec == SLM_PREC_AUTO ? batch_distances(st, pairs, np) : 0);
     p->prec = prec;
     p->tune = tune ? *tune : slm_tune{};
     if (!p->tune.use_graph) p->tune.use_graph = 1;
@@ -978,8 +996,10 @@ uint64_t tune_key(const slm_store *st, const slm_pair *pairs, uint32_t np, int m
 extern "C" slm_status slm_autotune(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                                    int mutual, slm_precision prec, slm_tune *best, float *best_ms) {
     if (!c || !st || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (!prec_valid(prec)) return fail(SLM_INVALID_ARG, "unknown precision");
     SLM_TRY(validate_ratio(ratio));
     SLM_TRY(ctx_check_device(c));
+    prec = resolve_prec(prec, prec == SLM_PREC_AUTO ? batch_distances(st, pairs, np) : 0);
     std::vector<slm_tune> grid;
     const uint32_t ips[3] = {2, 4, 8};
     for (uint32_t a = 0; a < 2; ++a)
@@ -1035,11 +1055,11 @@ extern "C" slm_status slm_autotune(slm_ctx *c, slm_store *st, const slm_pair *pa
 extern "C" slm_status slm_plan_create(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                                       int mutual, slm_precision prec, const slm_tune *tune, slm_plan **out) {
     if (!c || !st || !out || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
-    if (prec != SLM_PREC_FP32 && prec != SLM_PREC_BF16 && prec != SLM_PREC_FP8)
-        return fail(SLM_INVALID_ARG, "unknown precision");
+    if (!prec_valid(prec)) return fail(SLM_INVALID_ARG, "unknown precision");
     SLM_TRY(validate_ratio(ratio));
     *out = nullptr;
     SLM_TRY(ctx_check_device(c));
+    prec = resolve_prec(prec, prec == SLM_PREC_AUTO ? batch_distances(st, pairs, np) : 0);
     slm_tune t = tune ? *tune : slm_tune{};
     if (t.autotune) {
         const uint64_t key = tune_key(st, pairs, np, mutual, prec);
@@ -1214,8 +1234,7 @@ slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float 
                            slm_precision prec) {
     if (!c) return fail(SLM_INVALID_ARG, "NULL context");
     if ((na && !a) || (nb && !b)) return fail(SLM_INVALID_ARG, "NULL descriptor array");
-    if (prec != SLM_PREC_FP32 && prec != SLM_PREC_BF16 && prec != SLM_PREC_FP8)
-        return fail(SLM_INVALID_ARG, "unknown precision");
+    if (!prec_valid(prec)) return fail(SLM_INVALID_ARG, "unknown precision");
     return validate_ratio(ratio);
 }
 
@@ -1225,6 +1244,7 @@ extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, c
                                       float ratio, int mutual, slm_precision prec, slm_pair *out, uint32_t cap,
                                       uint32_t *n_out, slm_stats *st) {
     SLM_TRY(check_pair_args(c, a, na, b, nb, ratio, prec));
+    prec = resolve_prec(prec, (uint64_t)na * nb);
     if (!n_out || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL output");
     *n_out = 0;
     if (st) std::memset(st, 0, sizeof(*st));
@@ -1260,6 +1280,7 @@ extern "C" slm_status slm_ratio_match_device(slm_ctx *c, const float *d_a, uint3
                                              float ratio, int mutual, slm_precision prec, slm_pair *d_out,
                                              uint32_t cap, uint32_t *d_count) {
     SLM_TRY(check_pair_args(c, d_a, na, d_b, nb, ratio, prec));
+    prec = resolve_prec(prec, (uint64_t)na * nb);
     if (!d_count || (cap && !d_out)) return fail(SLM_INVALID_ARG, "NULL output");
     SLM_TRY(ctx_check_device(c));
     if (na == 0 || nb < 2) {
@@ -1593,8 +1614,7 @@ void serve_loop(slm_server *srv) {
 extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server **out) {
     if (!opts || !out) return fail(SLM_INVALID_ARG, "NULL argument");
     *out = nullptr;
-    if (opts->prec != SLM_PREC_FP32 && opts->prec != SLM_PREC_BF16 && opts->prec != SLM_PREC_FP8)
-        return fail(SLM_INVALID_ARG, "unknown precision");
+    if (!prec_valid(opts->prec)) return fail(SLM_INVALID_ARG, "unknown precision");
     SLM_TRY(validate_ratio(opts->ratio));
     auto *srv = new (std::nothrow) slm_server();
     if (!srv) return fail(SLM_OOM, "host allocation failed");

@@ -26,6 +26,8 @@ pub enum Precision {
     Fp32,
     Bf16,
     Fp8,
+    /// BF16 for large calls and batches, FP32 for small ones (libslm decides).
+    Auto,
 }
 
 impl Precision {
@@ -34,6 +36,7 @@ impl Precision {
             Precision::Fp32 => sys::SLM_PREC_FP32,
             Precision::Bf16 => sys::SLM_PREC_BF16,
             Precision::Fp8 => sys::SLM_PREC_FP8,
+            Precision::Auto => sys::SLM_PREC_AUTO,
         }
     }
 }
@@ -70,9 +73,10 @@ fn pack<D: Descriptor>(v: &[D]) -> Vec<f32> {
     out
 }
 
-/// Drop-in for `skylens_core::matching::ratio_match` (BF16 shortlist, exact).
+/// Drop-in for `skylens_core::matching::ratio_match` (exact; the BF16
+/// shortlist for large pairs, the plain FP32 kernel for small ones).
 pub fn ratio_match<D: Descriptor>(a: &[D], b: &[D], ratio: f32, mutual: bool) -> Vec<(usize, usize)> {
-    ratio_match_with(a, b, ratio, mutual, Precision::Bf16)
+    ratio_match_with(a, b, ratio, mutual, Precision::Auto)
 }
 
 pub fn ratio_match_with<D: Descriptor>(a: &[D], b: &[D], ratio: f32, mutual: bool, p: Precision)
@@ -145,7 +149,7 @@ pub fn match_pairs<D: Descriptor>(views: &[&[D]], pairs: &[(usize, usize)], rati
     let mut out = vec![sys::slm_pair::default(); cap];
     let mut off = vec![0u64; pairs.len() + 1];
     let st = unsafe {
-        sys::slm_match_batch(c, store, raw.as_ptr(), raw.len() as u32, ratio, mutual as i32, sys::SLM_PREC_BF16,
+        sys::slm_match_batch(c, store, raw.as_ptr(), raw.len() as u32, ratio, mutual as i32, sys::SLM_PREC_AUTO,
                              out.as_mut_ptr(), cap as u64, off.as_mut_ptr(), std::ptr::null_mut())
     };
     unsafe { sys::slm_store_destroy(store) };
@@ -207,7 +211,7 @@ pub fn match_scheduled_pairs<D: Descriptor>(imgs: &[&[D]], views: &[(usize, usiz
     let mut kept = 0u64;
     let st = unsafe {
         sys::slm_match_pairs(c, store, flat.as_ptr(), views.len() as u32, &sch, 0.8, 1,
-                             sys::SLM_PREC_BF16, min_matches, pairs_out.as_mut_ptr(), pairs_out.len() as u64,
+                             sys::SLM_PREC_AUTO, min_matches, pairs_out.as_mut_ptr(), pairs_out.len() as u64,
                              &mut kept, out.as_mut_ptr(), cap as u64, off.as_mut_ptr(), std::ptr::null_mut())
     };
     unsafe { sys::slm_store_destroy(store) };

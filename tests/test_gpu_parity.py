@@ -235,3 +235,25 @@ def test_autotuned_plan(matcher, prec):
         assert np.array_equal(per[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16)), k
     plan.close()
     st.close()
+
+
+def test_auto_precision(matcher):
+    """SLM_PREC_AUTO: the plain FP32 kernel below SLM_AUTO_BF16_DISTANCES, the
+    BF16 shortlist from there up (5 and 15 kernels per launch); exact both ways."""
+    for n, path in ((800, "fp32"), (3000, "bf16")):
+        a, b = synth.pair_large(n, 0.5, 0.05, seed=n)
+        got = matcher.ratio_match_np(a, b, 0.8, True, "auto")
+        launches = matcher.last_stats["kernel_launches"]
+        assert (launches < 10) == (path == "fp32"), (n, launches)
+        assert np.array_equal(got, O.ratio_match_np(a, b, 0.8, True, threads=16)), n
+    z = synth.zone(positions=4, n_range=(100, 300), seed=43)  # a small batch: 2.4M distances in total
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    st.add_views_packed(z.desc, z.offsets, z.counts)
+    plan = st.plan(z.pairs, 0.8, True, "auto")
+    plan.launch()
+    got = plan.per_pair()
+    assert plan.stats["kernel_launches"] < 10
+    for k, (u, v) in enumerate(z.pairs):
+        assert np.array_equal(got[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=8))
+    plan.close()
+    st.close()
