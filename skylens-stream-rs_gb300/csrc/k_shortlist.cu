@@ -7,19 +7,21 @@
 //
 // Tensor-core kernel (sl_pass_kernel, one persistent CTA per SM, 18 warps):
 //   warp 0      TMA producer: per item the a tiles (1 or 2 x 128 rows, K-major,
-//               128B-swizzled operand images copied verbatim from the store)
-//               and their norms; per 128-column b tile the operand tile, norms
-//               (and, in pass 2, column thresholds) through a 4-slot ring.
+//               128B-swizzled operand images copied verbatim from the store;
+//               FP8 also norms and scales); per 128-column b tile the operand
+//               tile (and, in pass 2, column thresholds) through a ring of 3
+//               (BF16) or 4 (FP8) slots.
 //   warp 1      allocates 512 TMEM columns; one thread issues tcgen05.mma
 //               (M=128, N=128, K=16 bf16 / K=32 e4m3) into a double-buffered
-//               pair of 128x128 f32 accumulators per a tile.
+//               pair of 128x128 f32 accumulators per a tile. BF16 adds a ninth
+//               K step over the norm extension (slm_shortlist.h), so the
+//               accumulator is d~ / 2.
 //   warps 2-17  epilogue: warp w reads TMEM lane quarter w % 4 of a tile
 //               ((w - 2) / 4) % 2, column half (w - 2) / 8 of every b tile,
-//               one thread per row, 16 columns per tcgen05.ld;
-//               d~ = |a|^2 + |b|^2 - 2 acc. Row minima use a 3-input min tree
-//               per 16 columns; column minima use redux.sync.min.f32 per
-//               column, merged across warps in shared memory and across CTAs
-//               with one atomicMin per column and tile.
+//               one thread per row, 16 columns per tcgen05.ld. Row minima use
+//               a 3-input min tree per 16 columns; column minima use
+//               redux.sync.min.f32 per column, merged across warps in shared
+//               memory and across CTAs with one atomicMin per column and tile.
 #include <cuda_fp8.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -48,7 +48,7 @@ namespace slm {
 
 constexpr int kSlHalfSlots = 16;   // S capacity per row and column half
 constexpr int kSlRowSlots = 2 * kSlHalfSlots;
-constexpr int kSlStages = 4;       // b-tile ring depth
+constexpr int kSlStages = 4;       // b-tile ring depth (FP8; BF16 tiles are larger: 3)
 constexpr int kSlEpWarps = 16;     // epilogue warps
 constexpr int kSlThreads = 32 * (2 + kSlEpWarps);  // producer, MMA, epilogue
 
