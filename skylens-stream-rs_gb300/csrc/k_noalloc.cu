@@ -10,9 +10,12 @@
 // one file-scope device array, so it allocates nothing: the caller passes only
 // the inputs, the output buffer and the stream.
 //
-// The array is kNoAllocBytes (about 5.1 MiB) and every device that loads the
-// library holds it until the process exits. Its size sets the limit: na and nb
-// at most SLM_NOALLOC_MAX_DESCS (4096) descriptors each.
+// The array is kNoAllocBytes (about 5.1 MiB: the scratch layout of
+// single_layout for 4096 x 4096) and every device that loads the library
+// holds it until the process exits. Its size sets the limit: na and nb at
+// most SLM_NOALLOC_MAX_DESCS (4096) descriptors each. The same pipeline
+// (single_exact_enqueue) serves small host-side FP32 calls of slm_ratio_match
+// from a per-workspace scratch block.
 //
 // The first call on a device sets that device up (resolves the array's device
 // address with cudaGetSymbolAddress and sets the exact kernel's shared-memory
@@ -34,22 +37,20 @@ namespace slm {
 namespace {
 
 constexpr uint32_t kNaMax = SLM_NOALLOC_MAX_DESCS;
-constexpr uint32_t kTilesMax = kNaMax / kTile;     // row or column tiles per operand
-constexpr uint32_t kChunksMax = 16;                 // column chunks per row tile
-constexpr uint32_t kItemsMax = kTilesMax * kChunksMax;
+constexpr uint32_t kChunksMax = 16;  // column chunks per row tile
 
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
-// Scratch layout (byte offsets into the array).
-constexpr size_t kOffTiled = 0;
-constexpr size_t kOffItems = kOffTiled + align256(sizeof(float) * (size_t)kTileFloats * 2 * kTilesMax);
-constexpr size_t kOffParts = kOffItems + align256(sizeof(Item) * kItemsMax);
-constexpr size_t kOffMeta = kOffParts + align256(sizeof(RowPart) * kTile * kItemsMax);
-constexpr size_t kOffColbest = kOffMeta + align256(sizeof(PairMeta));
-constexpr size_t kOffSlots = kOffColbest + align256(sizeof(unsigned long long) * kNaMax);
-constexpr size_t kOffCounts = kOffSlots + align256(sizeof(uint2) * kNaMax);
-constexpr size_t kOffCtl = kOffCounts + align256(sizeof(uint32_t));
-constexpr size_t kNoAllocBytes = kOffCtl + align256(sizeof(uint32_t) * 16);
+// Largest layout (na = nb = kNaMax): the size of the static array.
+constexpr size_t max_layout_bytes() {
+    const size_t tiles = kNaMax / kTile;
+    const size_t items = tiles * kChunksMax;
+    return align256(sizeof(float) * (size_t)kTileFloats * 2 * tiles) + align256(sizeof(Item) * items) +
+           align256(sizeof(RowPart) * kTile * items) + align256(sizeof(PairMeta)) +
+           align256(sizeof(unsigned long long) * kNaMax) + align256(sizeof(uint2) * kNaMax) +
+           align256(sizeof(uint32_t)) + align256(sizeof(uint32_t) * 16);
+}
+constexpr size_t kNoAllocBytes = max_layout_bytes();
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -65,20 +66,19 @@ DeviceSetup g_setup[kMaxDevices];
 
 // Writes the single pair's metadata and its work items, clears the work
 // counter, error word and match count.
-__global__ void noalloc_setup_kernel(unsigned char *scratch, uint32_t na, uint32_t nb, uint32_t chunks) {
-    Item *items = reinterpret_cast<Item *>(scratch + kOffItems);
-    PairMeta *meta = reinterpret_cast<PairMeta *>(scratch + kOffMeta);
-    uint32_t *ctl = reinterpret_cast<uint32_t *>(scratch + kOffCtl);
-    uint32_t *counts = reinterpret_cast<uint32_t *>(scratch + kOffCounts);
-    const uint32_t rt_n = (na + kTile - 1) / kTile, ct_n = (nb + kTile - 1) / kTile;
-    const uint32_t n_items = rt_n * chunks;
+__global__ void single_setup_kernel(unsigned char *scratch, SingleLayout L, uint32_t na, uint32_t nb) {
+    Item *items = reinterpret_cast<Item *>(scratch + L.items);
+    PairMeta *meta = reinterpret_cast<PairMeta *>(scratch + L.meta);
+    uint32_t *ctl = reinterpret_cast<uint32_t *>(scratch + L.ctl);
+    uint32_t *counts = reinterpret_cast<uint32_t *>(scratch + L.counts);
+    const uint32_t chunks = L.chunks, n_items = L.rt_n * chunks;
     for (uint32_t k = threadIdx.x; k < n_items; k += blockDim.x) {
         const uint32_t rt = k / chunks, c = k % chunks;
         Item it;
         it.pair = 0;
         it.rt = rt;
-        it.ct0 = (uint32_t)((uint64_t)ct_n * c / chunks);
-        it.ct1 = (uint32_t)((uint64_t)ct_n * (c + 1) / chunks);
+        it.ct0 = (uint32_t)((uint64_t)L.ct_n * c / chunks);
+        it.ct1 = (uint32_t)((uint64_t)L.ct_n * (c + 1) / chunks);
         it.part = k;  // = rt * chunks + c, the layout finalize_kernel reads
         it.pad[0] = it.pad[1] = it.pad[2] = 0;
         items[k] = it;
@@ -86,7 +86,7 @@ __global__ void noalloc_setup_kernel(unsigned char *scratch, uint32_t na, uint32
     if (threadIdx.x == 0) {
         PairMeta m;
         m.a_row0 = 0;
-        m.b_row0 = rt_n * kTile;
+        m.b_row0 = L.rt_n * kTile;
         m.na = na;
         m.nb = nb;
         m.nchunk = chunks;
@@ -101,10 +101,11 @@ __global__ void noalloc_setup_kernel(unsigned char *scratch, uint32_t na, uint32
 
 // Copies the match list to the caller's buffer (at most cap pairs) and writes
 // the full count, or 0xffffffff if a bounded device wait gave up.
-__global__ void noalloc_copy_kernel(const unsigned char *scratch, slm_pair *out, uint32_t cap, uint32_t *d_count) {
-    const uint2 *slots = reinterpret_cast<const uint2 *>(scratch + kOffSlots);
-    const uint32_t n = *reinterpret_cast<const uint32_t *>(scratch + kOffCounts);
-    const uint32_t err = reinterpret_cast<const uint32_t *>(scratch + kOffCtl)[1];
+__global__ void single_copy_kernel(const unsigned char *scratch, SingleLayout L, slm_pair *out, uint32_t cap,
+                                   uint32_t *d_count) {
+    const uint2 *slots = reinterpret_cast<const uint2 *>(scratch + L.slots);
+    const uint32_t n = *reinterpret_cast<const uint32_t *>(scratch + L.counts);
+    const uint32_t err = reinterpret_cast<const uint32_t *>(scratch + L.ctl)[1];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n && t < cap; t += gridDim.x * blockDim.x) {
         const uint2 v = slots[t];
         out[t].i = v.x;
@@ -153,6 +154,71 @@ slm_status device_setup(int dev, DeviceSetup *out) {
 
 }  // namespace
 
+SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs) {
+    SingleLayout L{};
+    L.rt_n = (na + kTile - 1) / kTile;
+    L.ct_n = (nb + kTile - 1) / kTile;
+    const uint32_t want = (uint32_t)(sms > 0 ? sms : 1) * 4;
+    uint32_t chunks = L.rt_n ? (want + L.rt_n - 1) / L.rt_n : 1;
+    chunks = chunks > L.ct_n ? L.ct_n : chunks;
+    chunks = chunks > kChunksMax ? kChunksMax : chunks;
+    L.chunks = chunks < 1 ? 1 : chunks;
+    const size_t items = (size_t)L.rt_n * L.chunks;
+    size_t o = 0;
+    L.tiled = o, o += align256(sizeof(float) * (size_t)kTileFloats * (L.rt_n + L.ct_n));
+    L.items = o, o += align256(sizeof(Item) * items);
+    L.parts = o, o += align256(sizeof(RowPart) * kTile * items);
+    L.meta = o, o += align256(sizeof(PairMeta));
+    L.colbest = o, o += align256(sizeof(unsigned long long) * (nb ? nb : 1));
+    L.slots = o, o += align256(sizeof(uint2) * (na ? na : 1));
+    L.counts = o, o += align256(sizeof(uint32_t));
+    L.ctl = o, o += align256(sizeof(uint32_t) * 16);
+    if (inputs) {  // row-major inputs and the result block [count, pad, pairs]
+        L.raw_a = o, o += align256(sizeof(float) * kDesc * (size_t)(na ? na : 1));
+        L.raw_b = o, o += align256(sizeof(float) * kDesc * (size_t)(nb ? nb : 1));
+        L.out = o, o += align256(8 + sizeof(slm_pair) * (size_t)(na ? na : 1));
+    }
+    L.bytes = o;
+    return L;
+}
+
+// The exact FP32 match of one pair (pack -> exact_kernel -> finalize -> copy)
+// over a scratch block laid out by single_layout: no metadata from the host.
+cudaError_t single_exact_enqueue(unsigned char *sc, const SingleLayout &L, const float *d_a, uint32_t na,
+                                 const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
+                                 uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s) {
+    const uint32_t n_items = L.rt_n * L.chunks;
+    float *tiled = reinterpret_cast<float *>(sc + L.tiled);
+    single_setup_kernel<<<1, 256, 0, s>>>(sc, L, na, nb);
+    if (mutual) launch_fill_u64(reinterpret_cast<unsigned long long *>(sc + L.colbest), nb, ~0ull, s);
+    launch_pack_fp32(d_a, na, tiled, 0, s);
+    launch_pack_fp32(d_b, nb, tiled, L.rt_n, s);
+    ExactArgs a{};
+    a.tiled = tiled;
+    a.items = reinterpret_cast<const Item *>(sc + L.items);
+    a.n_items = n_items;
+    a.pairs = reinterpret_cast<const PairMeta *>(sc + L.meta);
+    a.parts = reinterpret_cast<RowPart *>(sc + L.parts);
+    a.colbest = reinterpret_cast<unsigned long long *>(sc + L.colbest);
+    a.work = reinterpret_cast<uint32_t *>(sc + L.ctl);
+    a.err = reinterpret_cast<uint32_t *>(sc + L.ctl) + 1;
+    a.mutual = mutual ? 1 : 0;
+    a.x2 = 1;
+    launch_exact(a, (int)(n_items < (uint32_t)sms ? n_items : (uint32_t)sms), s);
+    FinalizeArgs f{};
+    f.pairs = a.pairs;
+    f.npairs = 1;
+    f.parts = a.parts;
+    f.colbest = a.colbest;
+    f.ratio2 = ratio * ratio;
+    f.mutual = a.mutual;
+    f.slots = reinterpret_cast<uint2 *>(sc + L.slots);
+    f.counts = reinterpret_cast<uint32_t *>(sc + L.counts);
+    launch_finalize(f, s);
+    single_copy_kernel<<<16, 256, 0, s>>>(sc, L, d_out, cap, d_count);
+    return cudaGetLastError();
+}
+
 }  // namespace slm
 
 using namespace slm;
@@ -185,44 +251,10 @@ extern "C" slm_status slm_ratio_match_device_noalloc(const float *d_a, uint32_t 
         }
         return SLM_OK;
     }
-    const uint32_t rt_n = (na + kTile - 1) / kTile, ct_n = (nb + kTile - 1) / kTile;
-    const uint32_t want = (uint32_t)ds.sms * 4;
-    uint32_t chunks = (want + rt_n - 1) / rt_n;
-    if (chunks > ct_n) chunks = ct_n;
-    if (chunks > kChunksMax) chunks = kChunksMax;
-    if (chunks < 1) chunks = 1;
-    const uint32_t n_items = rt_n * chunks;
-    unsigned char *sc = ds.scratch;
-    float *tiled = reinterpret_cast<float *>(sc + kOffTiled);
-
-    noalloc_setup_kernel<<<1, 256, 0, s>>>(sc, na, nb, chunks);
-    if (mutual) launch_fill_u64(reinterpret_cast<unsigned long long *>(sc + kOffColbest), nb, ~0ull, s);
-    launch_pack_fp32(d_a, na, tiled, 0, s);
-    launch_pack_fp32(d_b, nb, tiled, rt_n, s);
-    ExactArgs a{};
-    a.tiled = tiled;
-    a.items = reinterpret_cast<const Item *>(sc + kOffItems);
-    a.n_items = n_items;
-    a.pairs = reinterpret_cast<const PairMeta *>(sc + kOffMeta);
-    a.parts = reinterpret_cast<RowPart *>(sc + kOffParts);
-    a.colbest = reinterpret_cast<unsigned long long *>(sc + kOffColbest);
-    a.work = reinterpret_cast<uint32_t *>(sc + kOffCtl);
-    a.err = reinterpret_cast<uint32_t *>(sc + kOffCtl) + 1;
-    a.mutual = mutual ? 1 : 0;
-    a.x2 = 1;
-    launch_exact(a, (int)(n_items < (uint32_t)ds.sms ? n_items : (uint32_t)ds.sms), s);
-    FinalizeArgs f{};
-    f.pairs = a.pairs;
-    f.npairs = 1;
-    f.parts = a.parts;
-    f.colbest = a.colbest;
-    f.ratio2 = ratio * ratio;
-    f.mutual = a.mutual;
-    f.slots = reinterpret_cast<uint2 *>(sc + kOffSlots);
-    f.counts = reinterpret_cast<uint32_t *>(sc + kOffCounts);
-    launch_finalize(f, s);
-    noalloc_copy_kernel<<<16, 256, 0, s>>>(sc, d_out, cap, d_count);
-    const cudaError_t le = cudaGetLastError();
+    const SingleLayout L = single_layout(na, nb, ds.sms, false);
+    if (L.bytes > kNoAllocBytes) return na_fail(SLM_INTERNAL, "scratch layout exceeds the static array");
+    const cudaError_t le = single_exact_enqueue(ds.scratch, L, d_a, na, d_b, nb, ratio, mutual, d_out, cap, d_count,
+                                                ds.sms, s);
     if (le != cudaSuccess) return na_fail(SLM_CUDA_ERROR, std::string("launch failed: ") + cudaGetErrorString(le));
     return SLM_OK;
 }

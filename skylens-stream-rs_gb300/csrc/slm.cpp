@@ -557,6 +557,8 @@ struct Workspace {
     cudaStream_t stream = nullptr;
     slm_store store;
     slm_plan plan;
+    DevBuf single;                   // FP32 single-pair calls: inputs, scratch and result block
+    std::vector<unsigned char> single_out;
 };
 
 namespace {
@@ -1240,6 +1242,44 @@ slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float 
 
 }  // namespace
 
+namespace {
+
+// An FP32 single-pair call without a store or a plan: the inputs go into the
+// workspace's scratch block, the metadata is made on the device, and the
+// count and pairs come back in one copy (7 kernels, 2 uploads, 1 read-back).
+slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t na, const float *b, uint32_t nb,
+                            float ratio, int mutual, slm_pair *out, uint32_t cap, uint32_t *n_out, slm_stats *st) {
+    const SingleLayout L = single_layout(na, nb, c->sms, true);
+    SLM_TRY(w->single.ensure(c, L.bytes));
+    unsigned char *sc = w->single.as<unsigned char>();
+    cudaStream_t s = w->stream;
+    SLM_CU(cudaMemcpyAsync(sc + L.raw_a, a, (size_t)na * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
+    SLM_CU(cudaMemcpyAsync(sc + L.raw_b, b, (size_t)nb * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
+    SLM_CU(single_exact_enqueue(sc, L, reinterpret_cast<const float *>(sc + L.raw_a), na,
+                                reinterpret_cast<const float *>(sc + L.raw_b), nb, ratio, mutual,
+                                reinterpret_cast<slm_pair *>(sc + L.out + 8), na,
+                                reinterpret_cast<uint32_t *>(sc + L.out), c->sms, s));
+    const size_t bytes = 8 + sizeof(slm_pair) * (size_t)na;
+    w->single_out.resize(bytes);
+    SLM_CU(cudaMemcpyAsync(w->single_out.data(), sc + L.out, bytes, cudaMemcpyDeviceToHost, s));
+    SLM_CU(cudaStreamSynchronize(s));
+    uint32_t n = 0;
+    std::memcpy(&n, w->single_out.data(), sizeof(n));
+    if (n == 0xffffffffu) return fail(SLM_TIMEOUT, "device wait gave up");
+    *n_out = n;
+    if (st) {
+        st->pairs = 1;
+        st->distances = (uint64_t)na * nb;
+        st->matches = n;
+        st->kernel_launches = mutual ? 7 : 6;
+    }
+    if (n > cap) return fail(SLM_CAPACITY, "need " + std::to_string(n) + " pairs, have " + std::to_string(cap));
+    if (n) std::memcpy(out, w->single_out.data() + 8, sizeof(slm_pair) * (size_t)n);
+    return SLM_OK;
+}
+
+}  // namespace
+
 extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb,
                                       float ratio, int mutual, slm_precision prec, slm_pair *out, uint32_t cap,
                                       uint32_t *n_out, slm_stats *st) {
@@ -1257,6 +1297,7 @@ extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, c
     Workspace *w = nullptr;
     SLM_TRY(ws_acquire(c, &w));
     WsGuard guard{c, w};
+    if (prec == SLM_PREC_FP32) return single_pair_fp32(c, w, a, na, b, nb, ratio, mutual, out, cap, n_out, st);
     SLM_TRY(single_pair_enqueue(c, w, a, na, b, nb, ratio, mutual, prec, false));
     slm_plan *p = &w->plan;
     SLM_CU(cudaStreamSynchronize(w->stream));

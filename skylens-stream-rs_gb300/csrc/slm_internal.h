@@ -5,6 +5,8 @@
 
 #include <cstdint>
 
+#include "slm.h"
+
 namespace slm {
 
 constexpr int kDesc = 128;      // descriptor length (features.rs:496)
@@ -95,5 +97,20 @@ void launch_finalize(const FinalizeArgs &a, cudaStream_t s);
 void launch_fill_u64(unsigned long long *p, uint64_t n, unsigned long long v, cudaStream_t s);
 // Sets the message slm_last_error() returns on this host thread.
 void set_last_error(const char *msg);
+
+// Scratch layout of one exact FP32 pair match with its metadata made on the
+// device (byte offsets; `inputs` adds room for the row-major inputs and a
+// result block [count, pad, pairs]).
+struct SingleLayout {
+    size_t tiled, items, parts, meta, colbest, slots, counts, ctl, raw_a, raw_b, out, bytes;
+    uint32_t rt_n, ct_n, chunks;
+};
+SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs);
+// Enqueues setup, packing, exact_kernel, finalize and the copy of at most cap
+// pairs into d_out with the count (0xffffffff: a device wait gave up) into
+// *d_count. Returns the launch status.
+cudaError_t single_exact_enqueue(unsigned char *scratch, const SingleLayout &L, const float *d_a, uint32_t na,
+                                 const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
+                                 uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s);
 
 }  // namespace slm
