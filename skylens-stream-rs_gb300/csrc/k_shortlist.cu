@@ -701,6 +701,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                                         const uint32_t sl = atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
                                                         if (sl < kSlHalfSlots)
                                                             cand[sl] = make_uint2(j0 + k, __float_as_uint(kDom * d[k]));
+                                                        else if (sl == kSlHalfSlots)  // this half overflowed just now
+                                                            atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
                                                         ncand = sl + 1;
                                                     }
                                                 }
@@ -816,7 +818,10 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     g.rownear[slot] = near + S.rownear[r];
                 }
             } else {
-                if (own_row && rvalid && thr_i > -kInf) g.rowcnt[2 * ridx + h] = ncand;
+                if (own_row && rvalid && thr_i > -kInf) {
+                    g.rowcnt[2 * ridx + h] = ncand;
+                    if (ncand > kSlHalfSlots) atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
+                }
             }
         }
     }
@@ -888,14 +893,23 @@ SLM_DEV float window_up(float x, float eps) {
 
 // ------------------------------------------------------------------ mid
 
-// Per pair: row thresholds from the pass-1 partials, column thresholds from
-// the column minima, and the routing decision from the near-chunk counts.
+// Row blocks of a pair: enough for its rows and its columns.
+SLM_DEV uint32_t pair_blocks(const PairMeta &pm) {
+    const uint32_t n = max(pm.na, pm.nb);
+    return max(1u, (n + kSlRowBlock - 1) / kSlRowBlock);
+}
+
+// One CTA per pair and block of kSlRowBlock rows and columns: row thresholds
+// from the pass-1 partials, column thresholds from the column minima, and the
+// near-chunk counts; the last CTA of a pair to finish makes the routing
+// decision from the pair's totals.
 __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
-    __shared__ uint32_t wide_sh, open_sh;
-    const uint32_t p = blockIdx.x;
+    __shared__ uint32_t wide_sh, open_sh, last_sh;
+    const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
-    if (sp.routed) return;  // block-uniform
+    const uint32_t nblk = pair_blocks(pm);
+    if (sp.routed || blk >= nblk) return;  // block-uniform
     const float kInf = __int_as_float(0x7f800000);
     if (threadIdx.x == 0) wide_sh = open_sh = 0;
     __syncthreads();
@@ -908,7 +922,8 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
     // minimum, so a fixed count alone would misjudge rows split into many.)
     const uint32_t wide_min = max((uint32_t)kSlRowSlots, (pm.nb + 15) / 16 / 2);
     uint32_t wide = 0, open = 0;
-    for (uint32_t i = threadIdx.x; i < na_pad; i += blockDim.x) {
+    const uint32_t r0 = blk * kSlRowBlock, r1 = min(r0 + kSlRowBlock, na_pad);
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
         float thr = -kInf;
         if (i < pm.na && pm.nb > 0) {
             const uint32_t super = i / 256, r = i % 256;
@@ -931,21 +946,34 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
         g.rowthr[sp.rbase + i] = thr;
     }
     const uint32_t nb_pad = (pm.nb + kTile - 1) / kTile * kTile;
-    for (uint32_t j = threadIdx.x; j < nb_pad; j += blockDim.x) {
+    const uint32_t c0 = blk * kSlRowBlock, c1 = min(c0 + kSlRowBlock, nb_pad);
+    for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
         float thr = -kInf;
-        if (j < pm.nb) {
-            thr = window_up(ord2f(g.colmin[sp.cbase + j]), eps);
-        }
+        if (j < pm.nb) thr = window_up(ord2f(g.colmin[sp.cbase + j]), eps);
         g.colthr[sp.cbase + j] = thr;
     }
     if (wide) atomicAdd(&wide_sh, wide);
     if (open) atomicAdd(&open_sh, open);
     __syncthreads();
-    // more than 1/8 of the undecided rows are expected to overflow their
-    // shortlist: settle the whole pair with the exact kernel
-    if (threadIdx.x == 0 && wide_sh * 8 > open_sh && open_sh) {
-        g.spairs[p].routed = 1;
-        atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+    if (threadIdx.x == 0) {
+        uint32_t *pc = g.pairctl + 4 * (size_t)p;
+        if (wide_sh) atomicAdd(&pc[kPcWide], wide_sh);
+        if (open_sh) atomicAdd(&pc[kPcOpen], open_sh);
+        __threadfence();
+        last_sh = atomicAdd(&pc[kPcMidDone], 1u) == nblk - 1;
+    }
+    __syncthreads();
+    if (last_sh && threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t *pc = g.pairctl + 4 * (size_t)p;
+        const uint32_t w = atomicAdd(const_cast<uint32_t *>(&pc[kPcWide]), 0u);
+        const uint32_t o = atomicAdd(const_cast<uint32_t *>(&pc[kPcOpen]), 0u);
+        // more than 1/8 of the undecided rows are expected to overflow their
+        // shortlist: settle the whole pair with the exact kernel
+        if (w * 8 > o && o) {
+            g.spairs[p].routed = 1;
+            atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+        }
     }
 }
 
@@ -983,35 +1011,27 @@ SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &s
     return kDecPending;
 }
 
-// One thread per row: decide from the bounds, or queue exact work. A pair
-// with more than 1/8 of its rows overflowing S is routed to the exact kernel
-// instead (one exact scan per row would cost more).
+// One thread per row (CTA per pair and row block): decide from the bounds, or
+// queue exact work. A pair with more than 1/8 as many overflowed row halves
+// (counted by pass 2) as rows is routed to the exact kernel instead (one exact
+// scan per row would cost more).
 __global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
-    __shared__ uint32_t over_sh;
-    const uint32_t p = blockIdx.x;
+    const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
-    if (sp.routed) return;  // block-uniform: route_finalize decides its rows
+    if (sp.routed || blk * kSlRowBlock >= pm.na) return;  // block-uniform: route_finalize decides its rows
     const float kInf = __int_as_float(0x7f800000);
     const float eps = sp.eps;
-    if (threadIdx.x == 0) over_sh = 0;
-    __syncthreads();
-    uint32_t over = 0;
-    for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
-        const uint32_t ridx = sp.rbase + i;
-        over += (g.rowthr[ridx] > -kInf && (g.rowcnt[2 * ridx] > kSlHalfSlots || g.rowcnt[2 * ridx + 1] > kSlHalfSlots))
-                    ? 1u : 0u;
-    }
-    if (over) atomicAdd(&over_sh, over);
-    __syncthreads();
-    if (over_sh * 8 > pm.na) {
-        if (threadIdx.x == 0) {
+    // every CTA of the pair reads the same total (written by the previous kernel)
+    if (g.pairctl[4 * (size_t)p + kPcOver] * 8 > pm.na) {
+        if (blk == 0 && threadIdx.x == 0) {
             g.spairs[p].routed = 1;
             atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
         }
         return;
     }
-    for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
+    const uint32_t r1 = min(blk * kSlRowBlock + kSlRowBlock, pm.na);
+    for (uint32_t i = blk * kSlRowBlock + threadIdx.x; i < r1; i += blockDim.x) {
         const uint32_t ridx = sp.rbase + i;
         uint32_t dec = kDecNone;
         if (g.rowthr[ridx] > -kInf) {
@@ -1394,7 +1414,8 @@ __global__ void __launch_bounds__(256) sl_route_finalize_kernel(SlArgs g) {
         const uint32_t p = g.xlist[k];
         const PairMeta pm = g.pairs[p];
         const SlPair sp = g.spairs[p];
-        for (uint32_t i = threadIdx.x; i < pm.na; i += blockDim.x) {
+        const uint32_t r1 = min(blockIdx.y * kSlRowBlock + kSlRowBlock, pm.na);  // this CTA's row block
+        for (uint32_t i = blockIdx.y * kSlRowBlock + threadIdx.x; i < r1; i += blockDim.x) {
             const uint32_t rt = i / kTile;
             float d1 = kInf, d2 = kInf;
             uint32_t j1 = 0xffffffffu;
@@ -1412,17 +1433,23 @@ __global__ void __launch_bounds__(256) sl_route_finalize_kernel(SlArgs g) {
 
 // -------------------------------------------------------------- compact
 
+// Matches of a pair's row block in ascending i, at the block's slot range
+// (CTA per pair and row block); the block's count goes to blkcnt and the
+// pair's total to counts.
 __global__ void __launch_bounds__(256) sl_compact_kernel(SlArgs g) {
     __shared__ uint32_t warp_tot[8];
-    const uint32_t p = blockIdx.x;
+    const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
+    const uint32_t r0 = blk * kSlRowBlock;
+    if (r0 >= pm.na) return;  // block-uniform
+    const uint32_t r1 = min(r0 + kSlRowBlock, pm.na);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t base = 0;
-    for (uint32_t row0 = 0; row0 < pm.na; row0 += 256) {
+    for (uint32_t row0 = r0; row0 < r1; row0 += 256) {
         const uint32_t i = row0 + tid;
         uint32_t dec = kDecNone;
-        if (i < pm.na) dec = g.rowdec[sp.rbase + i];
+        if (i < r1) dec = g.rowdec[sp.rbase + i];
         if (dec == kDecPending) {
             atomicCAS(g.ctl + 1, 0u, (uint32_t)DERR_BAD_ITEM);
             dec = kDecNone;
@@ -1437,11 +1464,36 @@ __global__ void __launch_bounds__(256) sl_compact_kernel(SlArgs g) {
             off += (w < wid) ? warp_tot[w] : 0;
             tot += warp_tot[w];
         }
-        if (flag) g.slots[pm.slot_off + base + off + wpre] = make_uint2(i, dec);
+        if (flag) g.slots[pm.slot_off + r0 + base + off + wpre] = make_uint2(i, dec);
         base += tot;
         __syncthreads();
     }
-    if (tid == 0) g.counts[p] = base;
+    if (tid == 0) {
+        g.blkcnt[sp.blk + blk] = base;
+        if (base) atomicAdd(&g.counts[p], base);
+    }
+}
+
+// One CTA per pair: its row blocks' matches, in order, to the dense list.
+__global__ void __launch_bounds__(256) sl_gather_kernel(SlArgs g, const uint64_t *__restrict__ slot_off,
+                                                        const uint64_t *__restrict__ offsets, uint2 *__restrict__ dense,
+                                                        uint64_t cap) {
+    const uint32_t p = blockIdx.x;
+    if (g.counts[p] == 0) return;  // no matches, or filtered out
+    const uint32_t na = g.pairs[p].na, blk = g.spairs[p].blk;
+    uint64_t dst = offsets[p];
+    for (uint32_t b = 0; b * kSlRowBlock < na; ++b) {
+        const uint32_t n = g.blkcnt[blk + b];
+        const uint64_t src = slot_off[p] + (uint64_t)b * kSlRowBlock;
+        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x)
+            if (dst + t < cap) dense[dst + t] = g.slots[src + t];
+        dst += n;
+    }
+}
+
+void launch_gather_blocks(const SlArgs &a, const uint64_t *slot_off, const uint64_t *offsets, uint2 *dense,
+                          uint64_t cap, cudaStream_t s) {
+    if (a.npairs) sl_gather_kernel<<<a.npairs, 256, 0, s>>>(a, slot_off, offsets, dense, cap);
 }
 
 // ---------------------------------------------------------------- launch
@@ -1486,14 +1538,15 @@ int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
 
 int launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
     if (!a.npairs) return 0;
-    sl_mid_kernel<<<a.npairs, 256, 0, s>>>(a);
+    sl_mid_kernel<<<dim3(a.npairs, a.row_blocks), 256, 0, s>>>(a);
     return 1;
 }
 
 int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     if (!a.npairs) return 0;
     const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
-    sl_finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
+    const dim3 per_block(a.npairs, a.row_blocks);  // CTA per pair and row block
+    sl_finalize_kernel<<<per_block, 256, 0, s>>>(a);
     // routed pairs: plan, exact kernel over all their rows and columns, decisions
     sl_route_plan_kernel<<<1, 1024, 0, s>>>(a);
     sl_route_apply_kernel<<<rgrid, 256, 0, s>>>(a);
@@ -1510,10 +1563,10 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     x.mutual = a.mutual;
     x.x2 = 1;
     launch_exact(x, sms, s);
-    sl_route_finalize_kernel<<<rgrid, 256, 0, s>>>(a);
+    sl_route_finalize_kernel<<<dim3(rgrid, a.row_blocks), 256, 0, s>>>(a);
     sl_rescore_kernel<<<5 * sms, 256, 0, s>>>(a);  // 40 warps per SM: latency-bound gathers
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
-    sl_compact_kernel<<<a.npairs, 256, 0, s>>>(a);
+    sl_compact_kernel<<<per_block, 256, 0, s>>>(a);
     return 8;
 }
 

@@ -192,9 +192,10 @@ struct slm_plan {
     // shortlist path
     std::vector<SlItem> sitems;
     std::vector<SlPair> spairs;
-    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0;
+    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0, row_blocks_total = 0;
+    uint32_t row_blocks = 1;  // the most row blocks of any pair
     DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
-        d_rowdec, d_queue, d_rqueue, d_dump, d_xlist, d_xitems, d_xparts;
+        d_rowdec, d_queue, d_rqueue, d_dump, d_xlist, d_xitems, d_xparts, d_blkcnt, d_pairctl;
     bool dump = false;
     uint32_t min_matches = 0;        // pairs with fewer matches report none
     cudaGraphExec_t exec = nullptr;
@@ -279,11 +280,16 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     if (supers && supers < want) split = (uint32_t)((want + supers - 1) / supers);
     p->sitems.clear();
     p->spairs.assign(p->np, SlPair{});
-    uint64_t rb = 0, cb = 0, part = 0, row_tiles = 0;
+    uint64_t rb = 0, cb = 0, part = 0, row_tiles = 0, blk = 0;
+    p->row_blocks = 1;
     for (uint32_t k = 0; k < p->np; ++k) {
         const PairMeta &m = p->meta[k];
         SlPair &sp = p->spairs[k];
         row_tiles += (m.na + kTile - 1) / kTile;
+        // row blocks of the per-pair kernels after pass 1
+        sp.blk = (uint32_t)blk;
+        blk += (m.na + kSlRowBlock - 1) / kSlRowBlock;
+        p->row_blocks = std::max(p->row_blocks, (std::max(m.na, m.nb) + kSlRowBlock - 1) / kSlRowBlock);
         sp.rbase = (uint32_t)rb;
         sp.cbase = (uint32_t)cb;
         sp.view_a = pairs[k].i;
@@ -360,6 +366,9 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     SLM_TRY(p->d_spairs.ensure(c, sizeof(SlPair) * std::max<size_t>(1, p->np)));
     SLM_TRY(p->d_rowpart.ensure(c, sizeof(float2) * 256 * p->sl_parts));
     SLM_TRY(p->d_rownear.ensure(c, sizeof(uint32_t) * 256 * p->sl_parts));
+    p->row_blocks_total = blk;
+    SLM_TRY(p->d_blkcnt.ensure(c, sizeof(uint32_t) * std::max<uint64_t>(1, blk)));
+    SLM_TRY(p->d_pairctl.ensure(c, 4 * sizeof(uint32_t) * std::max<size_t>(1, p->np)));
     SLM_TRY(p->d_xlist.ensure(c, sizeof(uint32_t) * std::max<size_t>(1, p->np)));
     SLM_TRY(p->d_xitems.ensure(c, sizeof(Item) * p->xitem_cap));
     SLM_TRY(p->d_xparts.ensure(c, sizeof(RowPart) * kTile * p->xitem_cap));
@@ -445,6 +454,8 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         launch_fill_u32(p->d_colmin.as<uint32_t>(), p->cols_pad, 0xff800000u, s);  // encodes +inf
         SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, 2 * sizeof(uint32_t) * p->rows_pad, s));
         SLM_CU(cudaMemsetAsync(p->d_colcnt.p, 0, sizeof(uint32_t) * p->cols_pad, s));
+        SLM_CU(cudaMemsetAsync(p->d_pairctl.p, 0, 4 * sizeof(uint32_t) * p->np, s));
+        SLM_CU(cudaMemsetAsync(p->d_counts.p, 0, sizeof(uint32_t) * p->np, s));  // compact adds its blocks
         SlArgs a{};
         a.optiles = st->optiles.as<uint8_t>();
         a.norms = st->norms.as<float>();
@@ -475,6 +486,9 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.dump = p->dump ? p->d_dump.as<float>() : nullptr;
         a.slots = p->d_slots.as<uint2>();
         a.counts = p->d_counts.as<uint32_t>();
+        a.blkcnt = p->d_blkcnt.as<uint32_t>();
+        a.pairctl = p->d_pairctl.as<uint32_t>();
+        a.row_blocks = p->row_blocks;
         a.tiled = st->tiled.as<float>();
         a.xlist = p->d_xlist.as<uint32_t>();
         a.xitems = p->d_xitems.as<Item>();
@@ -500,8 +514,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         }
         uint64_t *offsets = p->d_offsets.as<uint64_t>();
         launch_scan_counts(p->d_counts.as<uint32_t>(), p->np, offsets, s);
-        launch_gather(p->d_slots.as<uint2>(), offsets + (p->np + 1), p->d_counts.as<uint32_t>(), offsets, p->np,
-                      p->d_dense.as<uint2>(), p->n_slots, s);
+        launch_gather_blocks(a, offsets + (p->np + 1), offsets, p->d_dense.as<uint2>(), p->n_slots, s);
         SLM_CU(cudaGetLastError());
         return SLM_OK;
     }
@@ -1522,7 +1535,7 @@ uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, sl
         bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
     else
         bytes += rows * (5 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 12 +
-                 pairs.size() * 4 +
+                 pairs.size() * (4 + 16) + (rows / kSlRowBlock + pairs.size()) * 4 +
                  (rows / kTile + 4ull * (uint64_t)std::max(1, st->ctx->sms)) * (sizeof(Item) + sizeof(RowPart) * kTile);
     return bytes + bytes / 4;  // DevBuf growth slack
 }

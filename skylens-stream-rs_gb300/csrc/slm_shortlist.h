@@ -35,7 +35,8 @@
 //     more than half of their 16-column chunks (and more than kSlRowSlots) had
 //     a minimum within 2 eps above the running row minimum; pass 2 skips
 //     routed pairs;
-//   - after pass 2 (finalize): more than 1/8 of its rows overflowed S.
+//   - after pass 2 (finalize): more than 1/8 as many row halves as rows
+//     overflowed S (pass 2 counts them).
 // The routed pairs' exact work items are planned on the device (route_plan,
 // route_apply), run by exact_kernel, and route_finalize writes their rows'
 // decisions; the results stay bit-exact whichever way a pair goes.
@@ -100,8 +101,16 @@ struct SlPair {
     uint32_t routed;   // per launch: settled by the exact FP32 kernel
     uint32_t xchunk;   // routed: column chunks per 128-row tile
     uint32_t xpart;    // routed: first exact work item (= first RowPart block)
-    uint32_t pad;
+    uint32_t blk;      // first entry of the pair's row blocks in SlArgs::blkcnt
 };
+
+// The per-pair kernels after pass 1 (mid, finalize, compact, route_finalize)
+// run one CTA per pair and block of this many rows (and columns), so that a
+// single large pair spreads over many CTAs.
+constexpr uint32_t kSlRowBlock = 2048;
+
+// Per-pair counters of one launch (SlArgs::pairctl, 4 words per pair).
+enum : int { kPcWide = 0, kPcOpen = 1, kPcMidDone = 2, kPcOver = 3 };
 
 // Row decision codes (per pair row).
 constexpr uint32_t kDecNone = 0xffffffffu;
@@ -151,8 +160,11 @@ struct SlArgs {
     int mutual;
     int fp8;
     float *dump;                 // debug: d~ of pair 0, [na][nb] (nullptr: off)
-    uint2 *slots;
+    uint2 *slots;                // pair p, row block b: matches from slot_off + b * kSlRowBlock
     uint32_t *counts;
+    uint32_t *blkcnt;            // matches per row block
+    uint32_t *pairctl;           // kPc* counters, zeroed per launch
+    uint32_t row_blocks;         // the most row blocks of any pair (second grid dimension)
     // pair routing to the exact kernel
     const float *tiled;          // FP32 store tiles
     uint32_t *xlist;             // routed pair ids
@@ -178,5 +190,9 @@ int launch_shortlist_eps(const SlArgs &a, cudaStream_t s);
 int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s);
 int launch_shortlist_mid(const SlArgs &a, cudaStream_t s);
 int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s);
+// Dense results of a shortlist launch: pair p's row blocks in order, pairs
+// with counts[p] == 0 (none, or filtered out) skipped.
+void launch_gather_blocks(const SlArgs &a, const uint64_t *slot_off, const uint64_t *offsets, uint2 *dense,
+                          uint64_t cap, cudaStream_t s);
 
 }  // namespace slm
