@@ -118,15 +118,16 @@ SLM_DEV void tmem_wait_ld16(uint32_t (&r)[16]) {
                  : "memory");
 }
 
-// atomicAdd(p, 1) when pred holds, without a branch (no return value).
-SLM_DEV void red_add1_if(uint32_t *p, bool pred) {
+// atomicAdd(p, 1) when x <= 0 (not for NaN), without a branch (no return
+// value); the comparison sits in the same block as the predicated red.
+SLM_DEV void red_add1_le0(uint32_t *p, float x) {
     asm volatile(
         "{\n"
         ".reg .pred q;\n"
-        "setp.ne.u32 q, %1, 0;\n"
+        "setp.le.f32 q, %1, 0f00000000;\n"
         "@q red.relaxed.gpu.global.add.u32 [%0], 1;\n"
         "}\n" ::"l"(p),
-        "r"((uint32_t)pred)
+        "f"(x)
         : "memory");
 }
 
@@ -148,22 +149,13 @@ SLM_DEV float min16(const float (&d)[16]) {
     const float e = min3f(d[9], d[10], d[11]), f = min3f(d[12], d[13], d[14]);
     return fminf(min3f(a, b, c), min3f(e, f, d[15]));
 }
-SLM_DEV float min16g(const float (&d)[16], float (&gm)[2]) {
+// Minimum of 16 values, and with the minima of its four groups of 4: a rare
+// hit below a threshold is then looked for in 4 values (measured faster than
+// groups of 2 or 8 on the pass-2 tests).
+SLM_DEV float min16q(const float (&d)[16], float (&g4)[4]) {
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
-        gm[q] = fminf(min3f(d[8 * q], d[8 * q + 1], d[8 * q + 2]),
-                      min3f(d[8 * q + 3], d[8 * q + 4], min3f(d[8 * q + 5], d[8 * q + 6], d[8 * q + 7])));
-    return fminf(gm[0], gm[1]);
-}
-
-// Minimum of 32 values plus the minima of its four groups of 8, so that a
-// rare hit below a threshold scans 8 values instead of 32.
-SLM_DEV float min32g(const float (&d)[32], float (&gm)[4]) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-        gm[q] = fminf(min3f(d[8 * q], d[8 * q + 1], d[8 * q + 2]),
-                      min3f(d[8 * q + 3], d[8 * q + 4], min3f(d[8 * q + 5], d[8 * q + 6], d[8 * q + 7])));
-    return fminf(min3f(gm[0], gm[1], gm[2]), gm[3]);
+    for (int q = 0; q < 4; ++q) g4[q] = min3f(d[4 * q], d[4 * q + 1], fminf(d[4 * q + 2], d[4 * q + 3]));
+    return min3f(g4[0], g4[1], fminf(g4[2], g4[3]));
 }
 
 // Exact reference distance (matching.rs:146-155): lane k = components 8c+k.
@@ -677,22 +669,29 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                         } else {
                             {
                                 // rows certain to have no match carry thr_i = -inf: no hit
-                                float gm[2];
-                                const float cm = min16g(d, gm);
+                                float g4[4];
+                                const float cm = min16q(d, g4);
                                 if (cm <= thr_i) {
+                                    if (own_row) {
+                                        // the item owns the whole row: predicated stores, running count
 #pragma unroll
-                                    for (int qq = 0; qq < 2; ++qq) {
-                                        if (gm[qq] <= thr_i) {
-                                            if (own_row) {
-                                                // the item owns the whole row: predicated stores, running count
+                                        for (int qq = 0; qq < 4; ++qq) {
+                                            if (g4[qq] <= thr_i) {
 #pragma unroll
-                                                for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
+                                                for (int k = 4 * qq; k < 4 * qq + 4; ++k) {
                                                     const bool hit = d[k] <= thr_i;
                                                     st_pair_if(cand + min(ncand, (uint32_t)kSlHalfSlots - 1), j0 + k,
                                                                __float_as_uint(kDom * d[k]), hit && ncand < kSlHalfSlots);
                                                     ncand += hit ? 1u : 0u;
                                                 }
-                                            } else {
+                                            }
+                                        }
+                                    } else {
+                                        // rows shared with other items: slots by atomics, 8 values per
+                                        // group (a path the zone's pairs rarely take: kept small)
+#pragma unroll
+                                        for (int qq = 0; qq < 2; ++qq) {
+                                            if (fminf(g4[2 * qq], g4[2 * qq + 1]) <= thr_i) {
 #pragma unroll
                                                 for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
                                                     // once the count passed the capacity, the row is
@@ -733,15 +732,15 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                     x[4 * k4 + 2] = f2_lo(x1);
                                     x[4 * k4 + 3] = f2_hi(x1);
                                 }
-                                float gm[2];
-                                const float xm = min16g(x, gm);
+                                float g4[4];
+                                const float xm = min16q(x, g4);
                                 if (xm <= 0.f) {
                                     uint32_t *cc = g.colcnt + sp.cbase + j0;
 #pragma unroll
-                                    for (int qq = 0; qq < 2; ++qq)
-                                        if (gm[qq] <= 0.f) {
+                                    for (int qq = 0; qq < 4; ++qq)
+                                        if (g4[qq] <= 0.f) {
 #pragma unroll
-                                            for (int k = 8 * qq; k < 8 * qq + 8; ++k) red_add1_if(cc + k, x[k] <= 0.f);
+                                            for (int k = 4 * qq; k < 4 * qq + 4; ++k) red_add1_le0(cc + k, x[k]);
                                         }
                                 }
                             }
