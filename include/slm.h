@@ -101,6 +101,11 @@ slm_status slm_ctx_destroy(slm_ctx *ctx);
 void *slm_ctx_stream(slm_ctx *ctx);
 /* Bytes currently allocated by the context and its stores/plans. */
 uint64_t slm_ctx_bytes_in_use(slm_ctx *ctx);
+/* Self-test of the bounded device waits (no reference counterpart): one GPU
+ * thread waits on a barrier that nothing completes and gives up after `polls`
+ * polls (1..65536). Returns SLM_TIMEOUT, the status every timed-out kernel
+ * wait reports, with the context still usable; anything else is a failure. */
+slm_status slm_selftest_wait_timeout(slm_ctx *ctx, uint32_t polls);
 
 /* ------------------------------------------------------ single pair */
 

@@ -465,4 +465,21 @@ void launch_finalize(const FinalizeArgs &a, cudaStream_t s) {
     if (a.npairs) finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
 }
 
+// Self-test of the bounded waits: thread 0 waits on an mbarrier that expects
+// one arrival nobody makes, gives up after `polls` polls and records
+// DERR_TIMEOUT_BAR in *err, the path every kernel's timed-out wait takes.
+__global__ void wait_selftest_kernel(uint32_t polls, uint32_t *err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait(&bar, 0, err, polls);
+}
+
+void launch_wait_selftest(uint32_t polls, uint32_t *err, cudaStream_t s) {
+    wait_selftest_kernel<<<1, 32, 0, s>>>(polls, err);
+}
+
 }  // namespace slm

@@ -1112,6 +1112,8 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t qn = min(g.ctl[kCtlRescoreLen], g.queue_cap);
     const float kInf = __int_as_float(0x7f800000);
+    uint32_t w_rows = 0;  // statistics of this warp's rows, added once at the end
+    float w_err = 0.f;
     for (uint32_t e = gw; e < qn; e += nw) {
         const SlQueue qe = g.rqueue[e];
         const PairMeta pm = g.pairs[qe.pair];
@@ -1149,13 +1151,17 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
             }
         }
         if (lane == 0) {
-            atomicAdd(&g.ctl[kCtlRescored], 1u);
-            if (maxerr == maxerr) atomicMax(&g.ctl[kCtlMaxErr], __float_as_uint(maxerr));
+            ++w_rows;
+            if (maxerr == maxerr) w_err = fmaxf(w_err, maxerr);
             uint32_t dec = kDecNone;
             if (ej != 0xffffffffu && e2 < kInf && !(e1 >= __fmul_rn(g.ratio2, e2)))
                 dec = g.mutual ? mutual_from_counts(g, qe.pair, sp, qe.i, ej, ad) : ej;
             g.rowdec[ridx] = dec;
         }
+    }
+    if (lane == 0 && w_rows) {
+        atomicAdd(&g.ctl[kCtlRescored], w_rows);
+        atomicMax(&g.ctl[kCtlMaxErr], __float_as_uint(w_err));  // non-negative: bits order as values
     }
 }
 

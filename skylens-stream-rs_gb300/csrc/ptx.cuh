@@ -3,12 +3,12 @@
 #pragma once
 #include <cstdint>
 
+#include "slm_internal.h"
+
 #define SLM_DEV __device__ __forceinline__
 
 namespace slm {
 
-// Device error codes written to the per-launch error word.
-enum : uint32_t { DERR_NONE = 0, DERR_TIMEOUT_BAR = 1, DERR_BAD_ITEM = 2, DERR_TIMEOUT_MMA = 3 };
 
 // Upper bound on polls of one mbarrier phase. try_wait itself suspends for a
 // hardware-defined time slice, so this is many seconds of waiting.
@@ -49,9 +49,9 @@ SLM_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase with the given parity to complete. Returns false
-// (and records DERR_TIMEOUT_BAR) if it did not complete within kWaitLimit polls.
-SLM_DEV bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err) {
-    for (uint32_t it = 0; it < kWaitLimit; ++it)
+// (and records DERR_TIMEOUT_BAR) if it did not complete within `limit` polls.
+SLM_DEV bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err, uint32_t limit = kWaitLimit) {
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicCAS(err, DERR_NONE, DERR_TIMEOUT_BAR);
     return false;

@@ -659,7 +659,9 @@ slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool devic
 slm_status check_status_word(slm_plan *p) {
     uint32_t err = 0;
     SLM_CU(cudaMemcpy(&err, p->d_ctl.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    if (err) return fail(SLM_TIMEOUT, "device wait gave up (code " + std::to_string(err) + ")");
+    if (err == DERR_TIMEOUT_BAR || err == DERR_TIMEOUT_MMA)
+        return fail(SLM_TIMEOUT, "device wait gave up (code " + std::to_string(err) + ")");
+    if (err) return fail(SLM_INTERNAL, "device invariant failed (code " + std::to_string(err) + ")");
     return SLM_OK;
 }
 
@@ -781,6 +783,22 @@ extern "C" slm_status slm_ctx_destroy(slm_ctx *c) {
 extern "C" void *slm_ctx_stream(slm_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
 
 extern "C" uint64_t slm_ctx_bytes_in_use(slm_ctx *c) { return c ? c->used.load() : 0; }
+
+extern "C" slm_status slm_selftest_wait_timeout(slm_ctx *c, uint32_t polls) {
+    if (!c) return fail(SLM_INVALID_ARG, "NULL context");
+    if (polls < 1 || polls > 65536) return fail(SLM_INVALID_ARG, "polls must be in 1..65536");
+    SLM_TRY(ctx_check_device(c));
+    DevBuf word;
+    SLM_TRY(word.ensure(c, sizeof(uint32_t)));
+    SLM_CU(cudaMemsetAsync(word.p, 0, sizeof(uint32_t), c->stream));
+    launch_wait_selftest(polls, word.as<uint32_t>(), c->stream);
+    SLM_CU(cudaGetLastError());
+    uint32_t err = 0;
+    SLM_CU(cudaMemcpyAsync(&err, word.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    SLM_CU(cudaStreamSynchronize(c->stream));
+    if (err == DERR_TIMEOUT_BAR) return fail(SLM_TIMEOUT, "device wait gave up (self-test, as expected)");
+    return fail(SLM_INTERNAL, "wait self-test: the wait did not give up (error word " + std::to_string(err) + ")");
+}
 
 // ------------------------------------------------------------------ stores
 

@@ -9,6 +9,11 @@
 
 namespace slm {
 
+// Device error codes written to a launch's error word: a bounded wait gave up
+// (TIMEOUT_*), or an invariant failed (BAD_ITEM: a work queue overflowed, a
+// routing plan did not fit, a row was left undecided).
+enum : uint32_t { DERR_NONE = 0, DERR_TIMEOUT_BAR = 1, DERR_BAD_ITEM = 2, DERR_TIMEOUT_MMA = 3 };
+
 constexpr int kDesc = 128;      // descriptor length (features.rs:496)
 constexpr int kTile = 128;      // rows per store tile
 constexpr int kTileFloats = kTile * kDesc;
@@ -94,6 +99,9 @@ void launch_exact(const ExactArgs &a, int grid, cudaStream_t s);
 // cannot load on the device.
 cudaError_t init_exact_kernels();
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s);
+// One thread waits on a barrier that never completes for `polls` polls and
+// records DERR_TIMEOUT_BAR in *err (self-test of the bounded waits).
+void launch_wait_selftest(uint32_t polls, uint32_t *err, cudaStream_t s);
 void launch_fill_u64(unsigned long long *p, uint64_t n, unsigned long long v, cudaStream_t s);
 // Sets the message slm_last_error() returns on this host thread.
 void set_last_error(const char *msg);

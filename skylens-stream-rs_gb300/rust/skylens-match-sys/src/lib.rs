@@ -92,6 +92,7 @@ pub struct slm_plan {
 extern "C" {
     pub fn slm_status_str(s: SlmStatus) -> *const c_char;
     pub fn slm_last_error() -> *const c_char;
+    pub fn slm_selftest_wait_timeout(ctx: *mut slm_ctx, polls: u32) -> SlmStatus;
     pub fn slm_ctx_create(opts: *const slm_opts, out: *mut *mut slm_ctx) -> SlmStatus;
     pub fn slm_ctx_destroy(ctx: *mut slm_ctx) -> SlmStatus;
     pub fn slm_ctx_stream(ctx: *mut slm_ctx) -> *mut c_void;

@@ -79,6 +79,7 @@ class SlmError(RuntimeError):
 SIGNATURES = {
     "slm_status_str": (ctypes.c_char_p, [c_int]),
     "slm_last_error": (ctypes.c_char_p, []),
+    "slm_selftest_wait_timeout": (c_int, [ctypes.c_void_p, c_u32]),
     "slm_ctx_create": (c_int, [P(SlmOpts), P(ctypes.c_void_p)]),
     "slm_ctx_destroy": (c_int, [ctypes.c_void_p]),
     "slm_ctx_stream": (ctypes.c_void_p, [ctypes.c_void_p]),

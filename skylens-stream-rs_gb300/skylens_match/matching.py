@@ -90,6 +90,11 @@ class Matcher:
     def bytes_in_use(self) -> int:
         return int(self._L.slm_ctx_bytes_in_use(self._h))
 
+    def selftest_wait_timeout(self, polls: int = 256) -> int:
+        """Runs the bounded-wait self-test (slm_selftest_wait_timeout) and
+        returns its status: SLM_TIMEOUT when the device wait gave up as it must."""
+        return int(self._L.slm_selftest_wait_timeout(self._h, polls))
+
     def close(self) -> None:
         if self._h:
             for st in list(self._stores):
