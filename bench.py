@@ -266,6 +266,7 @@ def run_pairs(args):
     from skylens_match import synth
     m = sm.Matcher()
     ext = torch.cuda.ExternalStream(m.stream)
+    pk, _ = peaks()
     cases = [("pair800", synth.pair_800(0)), ("pair8192", synth.pair_large(8192, 0.5, 0.05, seed=2)),
              ("pair32768", synth.pair_fp8(32768, seed=4))]
     out = []
@@ -293,7 +294,13 @@ def run_pairs(args):
             plan.results()
             s = plan.stats
             ms = float(np.median(times))
+            # small pairs: bytes the pair must move (both operand images and
+            # the match list) against the measured HBM copy rate
+            nbytes = (len(a) + len(b)) * 128 * {"fp32": 4, "bf16": 2, "fp8": 1}[prec] + len(got) * 8
+            hbm = nbytes / (ms / 1e3) / 1e9
             row["precisions"][prec] = {"ms": ms, "distances_per_s": len(a) * len(b) / (ms / 1e3),
+                                       "hbm": {"bytes": nbytes, "achieved_gbs": hbm, "peak_gbs": pk["hbm_gbs"],
+                                               "frac": hbm / pk["hbm_gbs"]},
                                        "bit_exact": bool(np.array_equal(got, ref)), "matches": int(len(got)),
                                        "rows_rescored_frac": s["rows_rescored"] / len(a),
                                        "rows_recomputed_frac": s["rows_recomputed"] / len(a),
@@ -549,10 +556,21 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        r, dr, n, dt = cpu_baseline(z, args.cpu_seconds, os.cpu_count() or 1)
-        cpu = {"value": r, "unit": "image pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"{n} of {len(z.pairs)} zone pairs in a fixed random order ({dt:.1f} s)",
-               "distances_per_s": dr}
+        # three repeats on all host threads (value = their median) and three on
+        # one thread, each repeat over the same pairs in the same order
+        cores = os.cpu_count() or 1
+        runs = [cpu_baseline(z, args.cpu_seconds / 3, cores) for _ in range(3)]
+        one = [cpu_baseline(z, args.cpu_seconds / 6, 1) for _ in range(3)]
+        med = float(np.median([x[0] for x in runs]))
+        cpu = {"value": med, "unit": "image pairs/s", "cores": cores, "kind": "port",
+               "sample": f"{int(np.median([x[2] for x in runs]))} of {len(z.pairs)} zone pairs in a fixed random "
+                         f"order per repeat (~{args.cpu_seconds / 3:.0f} s), 3 repeats",
+               "median": med, "min": float(min(x[0] for x in runs)),
+               "distances_per_s": float(np.median([x[1] for x in runs])),
+               "one_thread": {"median": float(np.median([x[0] for x in one])), "min": float(min(x[0] for x in one)),
+                              "unit": "image pairs/s",
+                              "sample": f"{int(np.median([x[2] for x in one]))} pairs per repeat "
+                                        f"(~{args.cpu_seconds / 6:.0f} s), 3 repeats"}}
 
     line = {"metric": METRIC, "value": value, "unit": "image pairs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
