@@ -193,8 +193,8 @@ typedef struct {
     uint32_t items_per_sm;  /* FP32: target work items per SM when splitting columns */
     uint32_t shortlist_k;   /* shortlist slots per row (BF16/FP8) */
     uint32_t use_graph;     /* 1: replay a captured CUDA graph (default), 2: plain launches */
-    uint32_t variant;       /* FP32: 0 packed f32x2 sub/add with scalar squares
-                               (default), 1 all scalar; both IEEE, bit-exact.
+    uint32_t variant;       /* FP32: 0 packed f32x2 arithmetic (default), 1 all
+                               scalar; both IEEE, bit-exact.
                                BF16/FP8: 2 keeps the approximate distances of pair 0
                                for slm_plan_debug_dump (diagnostics) */
     uint32_t row_tiles;     /* BF16/FP8: 128-row a tiles per work item, 1 or 2 (0: 2) */

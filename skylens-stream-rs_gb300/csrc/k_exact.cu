@@ -141,6 +141,11 @@ SLM_DEV u64 f2_add(u64 a, u64 b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+SLM_DEV u64 f2_fma(u64 a, u64 b, u64 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 SLM_DEV u64 f2_pack(float lo, float hi) {
     u64 d;
     asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
@@ -153,7 +158,7 @@ SLM_DEV float f2_hi(u64 v) { return __uint_as_float(static_cast<uint32_t>(v >> 3
 // columns of B (both tiles in [slot][row] layout).
 template <bool X2>
 SLM_DEV void tile_distances(const float *__restrict__ sa, const float *__restrict__ sb, int ty, int tx,
-                            float (&d)[8][8]) {
+                            u64 zero2, float (&d)[8][8]) {
     if constexpr (!X2) {
         float s[8][8];
 #pragma unroll
@@ -194,8 +199,11 @@ SLM_DEV void tile_distances(const float *__restrict__ sa, const float *__restric
     } else {
         // Packed pairs of columns (c, c+1): {a_r, a_r} - {b_c, b_c+1}. A packed
         // multiply followed by a packed add is contracted to a packed FMA by the
-        // code generator (measured: 25 % of distances off by an ulp), so the
-        // squares are scalar IEEE multiplies.
+        // code generator (measured: 25 % of distances off by an ulp). The square
+        // is therefore a packed FMA t * t + z with z a run-time zero (a kernel
+        // argument the compiler cannot fold): rounded once, it is exactly
+        // RN(t * t) (t * t >= 0, + 0 changes nothing), and no contraction with
+        // the following add is possible.
         u64 s[8][4];
 #pragma unroll
         for (int r = 0; r < 8; ++r)
@@ -219,10 +227,8 @@ SLM_DEV void tile_distances(const float *__restrict__ sa, const float *__restric
                     const u64 ar = f2_pack(av[r], av[r]);
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        // packed sub and add, scalar multiplies: the compiler must not
-                        // see a packed multiply feeding a packed add (it would fuse them)
                         const u64 t = f2_sub(ar, bv[c]);
-                        const u64 tt = f2_pack(__fmul_rn(f2_lo(t), f2_lo(t)), __fmul_rn(f2_hi(t), f2_hi(t)));
+                        const u64 tt = f2_fma(t, t, zero2);
                         acc[r][c] = (c16 == 0) ? tt : f2_add(acc[r][c], tt);
                     }
                 }
@@ -264,6 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) exact_kernel(ExactArgs g) {
     // Items planned on the device (pairs routed from the shortlist path) come
     // with their count in device memory, written by an earlier kernel.
     const uint32_t n_items = g.n_items_dev ? min(*g.n_items_dev, g.n_items) : g.n_items;
+    const u64 zero2 = f2_pack(g.zero, g.zero);
 
     uint32_t a_phase = 0;
     uint32_t seq = 0;  // b tiles consumed by this CTA (selects ring slot and parity)
@@ -316,7 +323,7 @@ __global__ void __launch_bounds__(kThreads, 1) exact_kernel(ExactArgs g) {
             const uint32_t cb = seq & 1;
             if (mine) {
                 float d[8][8];
-                tile_distances<X2>(S.A, S.B[slot], ty, tx, d);
+                tile_distances<X2>(S.A, S.B[slot], ty, tx, zero2, d);
 
                 uint32_t jc[8];
                 bool cvalid[8];

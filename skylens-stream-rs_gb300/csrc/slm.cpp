@@ -531,7 +531,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.work = ctl;
         a.err = ctl + 1;
         a.mutual = p->mutual;
-        a.x2 = p->tune.variant == 1 ? 0 : 1;  // packed sub/add with scalar squares; 1: all scalar
+        a.x2 = p->tune.variant == 1 ? 0 : 1;  // packed f32x2 arithmetic; 1: all scalar
         // External records so that the events become timing nodes under graph capture.
         SLM_CU(record_event(p->ev0, s));
         if (a.n_items) launch_exact(a, std::min<int>(p->ctx->sms, (int)a.n_items), s);

@@ -75,6 +75,7 @@ struct ExactArgs {
     uint32_t *err;               // device error word (zeroed per launch)
     int mutual;
     int x2;                      // 1: packed f32x2 arithmetic
+    float zero;                  // 0.0f, read at run time: the addend of the packed squares
 };
 
 struct FinalizeArgs {
