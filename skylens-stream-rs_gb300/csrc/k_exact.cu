@@ -427,22 +427,40 @@ void launch_exact(const ExactArgs &a, int grid, cudaStream_t s) {
 // -------------------------------------------------------------- finalize
 
 // One CTA per pair: merge the row partials of every column chunk, apply
-// matching.rs:204-214 and write matches in ascending i.
-__global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs g) {
-    __shared__ uint32_t warp_tot[8];
+// matching.rs:204-214 and write matches in ascending i. One thread per row and
+// step, partials loaded four at a time: a batch of few pairs runs 1024 threads
+// per pair, since a single small pair is a chain of dependent loads, not a
+// bandwidth problem; larger batches run 256 (more pairs resident per SM).
+constexpr int kFinThreadsMax = 1024;
+
+__global__ void __launch_bounds__(kFinThreadsMax) finalize_kernel(FinalizeArgs g) {
+    __shared__ uint32_t warp_tot[kFinThreadsMax / 32];
+    const uint32_t nthr = blockDim.x;
+    const int nwarps = (int)(nthr >> 5);
     const PairMeta pm = g.pairs[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const float kInf = __int_as_float(0x7f800000);
     uint32_t base = 0;
-    for (uint32_t row0 = 0; row0 < pm.na; row0 += 256) {
+    for (uint32_t row0 = 0; row0 < pm.na; row0 += nthr) {
         const uint32_t i = row0 + tid;
         uint32_t flag = 0, jout = 0;
         if (i < pm.na) {
             const uint32_t rt = i / kTile;
-            float d1 = __int_as_float(0x7f800000), d2 = __int_as_float(0x7f800000);
+            float d1 = kInf, d2 = kInf;
             uint32_t j1 = 0xffffffffu;
-            for (uint32_t c = 0; c < pm.nchunk; ++c)
-                merge_rowpart(g.parts[(size_t)(pm.part_base + rt * pm.nchunk + c) * kTile + (i % kTile)], d1, d2, j1);
-            const bool d2_finite = d2 < __int_as_float(0x7f800000);
+            const RowPart *pr = g.parts + (size_t)(pm.part_base + rt * pm.nchunk) * kTile + (i % kTile);
+            for (uint32_t c0 = 0; c0 < pm.nchunk; c0 += 4) {
+                RowPart q[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    // an absent chunk merges as the neutral partial (inf, inf, none)
+                    q[u] = RowPart{kInf, kInf, 0xffffffffu, 0u};
+                    if (c0 + u < pm.nchunk) q[u] = pr[(size_t)(c0 + u) * kTile];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) merge_rowpart(q[u], d1, d2, j1);
+            }
+            const bool d2_finite = d2 < kInf;
             if (j1 != 0xffffffffu && d2_finite && !(d1 >= __fmul_rn(g.ratio2, d2))) {
                 if (!g.mutual || static_cast<uint32_t>(g.colbest[pm.col_base + j1]) == i) {
                     flag = 1;
@@ -456,7 +474,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs g) {
         if (lane == 0) warp_tot[wid] = __popc(ballot);
         __syncthreads();
         uint32_t off = 0, tot = 0;
-        for (int w = 0; w < 8; ++w) {
+        for (int w = 0; w < nwarps; ++w) {
             const uint32_t t = warp_tot[w];
             off += (w < wid) ? t : 0;
             tot += t;
@@ -469,7 +487,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs g) {
 }
 
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s) {
-    if (a.npairs) finalize_kernel<<<a.npairs, 256, 0, s>>>(a);
+    if (a.npairs) finalize_kernel<<<a.npairs, a.npairs <= kFewPairs ? kFinThreadsMax : 256, 0, s>>>(a);
 }
 
 // Self-test of the bounded waits: thread 0 waits on an mbarrier that expects

@@ -902,7 +902,7 @@ SLM_DEV uint32_t pair_blocks(const PairMeta &pm) {
 // from the pass-1 partials, column thresholds from the column minima, and the
 // near-chunk counts; the last CTA of a pair to finish makes the routing
 // decision from the pair's totals.
-__global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
+__global__ void __launch_bounds__(1024) sl_mid_kernel(SlArgs g) {
     __shared__ uint32_t wide_sh, open_sh, last_sh;
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
@@ -928,12 +928,27 @@ __global__ void __launch_bounds__(256) sl_mid_kernel(SlArgs g) {
             const uint32_t super = i / 256, r = i % 256;
             float m1 = kInf, m2 = kInf;
             uint32_t near = 0;
-            for (uint32_t c = 0; c < sp.nchunk; ++c) {
-                const size_t slot = (size_t)(sp.part_base + super * sp.nchunk + c) * 256 + r;
-                const float2 v = g.rowpart[slot];
-                near += g.rownear[slot];
-                m2 = fminf(fminf(m2, v.y), fmaxf(m1, v.x));
-                m1 = fminf(m1, v.x);
+            // the column ranges' partials, four independent loads per step (an
+            // absent range merges as (inf, inf), near 0)
+            const size_t slot0 = (size_t)(sp.part_base + super * sp.nchunk) * 256 + r;
+            for (uint32_t c0 = 0; c0 < sp.nchunk; c0 += 4) {
+                float2 v[4];
+                uint32_t nr[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    v[u] = make_float2(kInf, kInf);
+                    nr[u] = 0;
+                    if (c0 + u < sp.nchunk) {
+                        v[u] = g.rowpart[slot0 + (size_t)(c0 + u) * 256];
+                        nr[u] = g.rownear[slot0 + (size_t)(c0 + u) * 256];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    near += nr[u];
+                    m2 = fminf(fminf(m2, v[u].y), fmaxf(m1, v[u].x));
+                    m1 = fminf(m1, v[u].x);
+                }
             }
             // m2' bounds the second smallest d~ from above
             if (!certain_no_match(m1, m2, eps, g.ratio2)) {
@@ -1014,7 +1029,7 @@ SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &s
 // queue exact work. A pair with more than 1/8 as many overflowed row halves
 // (counted by pass 2) as rows is routed to the exact kernel instead (one exact
 // scan per row would cost more).
-__global__ void __launch_bounds__(256) sl_finalize_kernel(SlArgs g) {
+__global__ void __launch_bounds__(1024) sl_finalize_kernel(SlArgs g) {
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
@@ -1543,7 +1558,7 @@ int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
 
 int launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
     if (!a.npairs) return 0;
-    sl_mid_kernel<<<dim3(a.npairs, a.row_blocks), 256, 0, s>>>(a);
+    sl_mid_kernel<<<dim3(a.npairs, a.row_blocks), a.npairs <= kFewPairs ? 1024 : 256, 0, s>>>(a);
     return 1;
 }
 
@@ -1551,7 +1566,7 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     if (!a.npairs) return 0;
     const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
     const dim3 per_block(a.npairs, a.row_blocks);  // CTA per pair and row block
-    sl_finalize_kernel<<<per_block, 256, 0, s>>>(a);
+    sl_finalize_kernel<<<per_block, a.npairs <= kFewPairs ? 1024 : 256, 0, s>>>(a);
     // routed pairs: plan, exact kernel over all their rows and columns, decisions
     sl_route_plan_kernel<<<1, 1024, 0, s>>>(a);
     sl_route_apply_kernel<<<rgrid, 256, 0, s>>>(a);

@@ -25,6 +25,11 @@ __host__ __device__ inline int perm_slot(int k) { return (k & 7) * 16 + (k >> 3)
 
 // Store tile layout (FP32): tile[slot][row], 128 x 128 floats = 64 KiB.
 
+// Batches of at most this many pairs run their per-pair kernels (finalize,
+// mid) with 1024 threads per pair instead of 256: with few pairs the GPU is
+// not full and each pair's rows are a chain of dependent loads.
+constexpr uint32_t kFewPairs = 64;
+
 // Per-row partial state of an exact scan over a column range.
 struct __align__(16) RowPart {
     float d1, d2;   // smallest and second smallest distance (multiset)
