@@ -771,8 +771,11 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     }
                     eph ^= 1;
                     // one thread per column and pair of the item: the minimum over
-                    // the (a tile, lane quarter) partials of that pair
-                    const int e = threadIdx.x - 64;  // 0..511
+                    // the (a tile, lane quarter) partials of that pair. The 8 epilogue
+                    // warps on SM sub-partitions 2 and 3 do it (e = 0..255); 0 and 1
+                    // also host the producer and MMA warps
+                    const int wq = warp & 3;
+                    const int e = wq >= 2 ? ((((warp - 2) >> 2) * 2 + (wq - 2)) * 32 + lane) : 512;
                     const int grp = e >> 7;
                     if (e < (two ? 256 : 128)) {
                         const int col = e & 127;
