@@ -257,3 +257,39 @@ def test_auto_precision(matcher):
         assert np.array_equal(got[k], O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=8))
     plan.close()
     st.close()
+
+
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_random_batches(matcher, prec, seed):
+    """Seeded random batches: views of 0-700 rows built from a shared pool of
+    descriptors (exact duplicates, near-duplicates at sigma 0.001-0.05, fresh
+    draws), random pairs including self-pairs and repeats, both mutual
+    settings; every pair's list equals the oracle's."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pool = synth.sift_like(rng, 3000)
+    views = []
+    for _ in range(24):
+        n = int(rng.choice([0, 1, 2, 3, 17, 127, 128, 129]) if rng.random() < 0.3 else rng.integers(30, 701))
+        src = pool[rng.integers(0, len(pool), size=n)]
+        kind = rng.random(n)
+        sig = rng.choice([0.001, 0.01, 0.05], size=n).astype(np.float32)
+        noisy = synth.noisy_copy(rng, src, sig)
+        fresh = synth.sift_like(rng, n)
+        v = np.where(kind[:, None] < 0.3, src, np.where(kind[:, None] < 0.8, noisy, fresh)).astype(np.float32)
+        views.append(np.ascontiguousarray(v))
+    counts = np.array([len(v) for v in views], np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    desc = np.concatenate([v for v in views if len(v)] or [np.zeros((0, 128), np.float32)]).astype(np.float32)
+    pairs = rng.integers(0, len(views), size=(60, 2)).astype(np.uint32)
+    st = matcher.store(int(counts.sum()), len(views))
+    st.add_views_packed(desc, offsets, counts)
+    for mutual in (True, False):
+        ratio = 0.8 if mutual else 0.95
+        plan = st.plan(pairs, ratio, mutual, prec)
+        plan.launch()
+        got = plan.per_pair()
+        for k, (u, v) in enumerate(pairs):
+            want = O.ratio_match_np(views[int(u)], views[int(v)], ratio, mutual, threads=8)
+            assert np.array_equal(got[k], want), (prec, seed, mutual, k, int(u), int(v))
+        plan.close()
+    st.close()
