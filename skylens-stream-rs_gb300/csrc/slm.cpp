@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -72,6 +74,10 @@ struct slm_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sms = 0;
+    // Kernels may read pageable host memory directly (address translation over
+    // the CPU-GPU link, as on Grace-based GB300 systems): single-pair inputs are
+    // then read by the packing kernels where they lie instead of being copied.
+    bool host_direct = false;
     uint64_t budget = 0;
     std::atomic<uint64_t> used{0};
     std::mutex mu;
@@ -763,6 +769,13 @@ extern "C" slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out) {
     size_t fre = 0, tot = 0;
     cudaMemGetInfo(&fre, &tot);
     c->budget = (opts && opts->hbm_budget) ? opts->hbm_budget : (uint64_t)fre;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    const char *no_direct = std::getenv("SLM_NO_HOST_DIRECT");
+    c->host_direct = pageable == 1 && !(no_direct && no_direct[0] == '1');
     *out = c;
     return SLM_OK;
 }
@@ -1284,12 +1297,17 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
     SLM_TRY(w->single.ensure(c, L.bytes));
     unsigned char *sc = w->single.as<unsigned char>();
     cudaStream_t s = w->stream;
-    SLM_CU(cudaMemcpyAsync(sc + L.raw_a, a, (size_t)na * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
-    SLM_CU(cudaMemcpyAsync(sc + L.raw_b, b, (size_t)nb * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
-    SLM_CU(single_exact_enqueue(sc, L, reinterpret_cast<const float *>(sc + L.raw_a), na,
-                                reinterpret_cast<const float *>(sc + L.raw_b), nb, ratio, mutual,
-                                reinterpret_cast<slm_pair *>(sc + L.out + 8), na,
-                                reinterpret_cast<uint32_t *>(sc + L.out), c->sms, s));
+    const float *src_a = a, *src_b = b;
+    // the packing kernels read rows as float4: direct reads need 16-byte alignment
+    const bool direct = c->host_direct && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+    if (!direct) {
+        SLM_CU(cudaMemcpyAsync(sc + L.raw_a, a, (size_t)na * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
+        SLM_CU(cudaMemcpyAsync(sc + L.raw_b, b, (size_t)nb * kDesc * sizeof(float), cudaMemcpyHostToDevice, s));
+        src_a = reinterpret_cast<const float *>(sc + L.raw_a);
+        src_b = reinterpret_cast<const float *>(sc + L.raw_b);
+    }
+    SLM_CU(single_exact_enqueue(sc, L, src_a, na, src_b, nb, ratio, mutual, reinterpret_cast<slm_pair *>(sc + L.out + 8),
+                                na, reinterpret_cast<uint32_t *>(sc + L.out), c->sms, s));
     const size_t bytes = 8 + sizeof(slm_pair) * (size_t)na;
     w->single_out.resize(bytes);
     SLM_CU(cudaMemcpyAsync(w->single_out.data(), sc + L.out, bytes, cudaMemcpyDeviceToHost, s));

@@ -293,3 +293,19 @@ def test_random_batches(matcher, prec, seed):
             assert np.array_equal(got[k], want), (prec, seed, mutual, k, int(u), int(v))
         plan.close()
     st.close()
+
+
+def test_single_call_input_alignment(matcher):
+    """Single FP32 calls read 16-byte-aligned host inputs where they lie (when
+    the device can read pageable memory) and copy the others first; both give
+    the reference's lists."""
+    a, b = synth.pair_800(3)
+    want = O.ratio_match_np(a, b, 0.8, True, threads=8)
+    for shift_a, shift_b in ((0, 0), (1, 0), (0, 3), (2, 2)):
+        ba = np.empty(a.size + 4, np.float32)
+        bb = np.empty(b.size + 4, np.float32)
+        ua = ba[shift_a:shift_a + a.size].reshape(a.shape)
+        ub = bb[shift_b:shift_b + b.size].reshape(b.shape)
+        ua[...] = a
+        ub[...] = b
+        assert np.array_equal(matcher.ratio_match_np(ua, ub, 0.8, True, "fp32"), want), (shift_a, shift_b)
