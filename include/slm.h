@@ -101,6 +101,20 @@ slm_status slm_ctx_destroy(slm_ctx *ctx);
 void *slm_ctx_stream(slm_ctx *ctx);
 /* Bytes currently allocated by the context and its stores/plans. */
 uint64_t slm_ctx_bytes_in_use(slm_ctx *ctx);
+/* Coalescing of concurrent single-pair calls (no reference counterpart: the
+ * reference's rayon workers call ratio_match once per pair, matching.rs:167
+ * from pipeline.rs:487-493). With max_pairs > 0, slm_ratio_match calls made
+ * with SLM_PREC_AUTO from any thread are queued; a worker thread matches up to
+ * max_pairs of them (same ratio and cross-check) in one batch once the batch
+ * is full or its oldest call has waited window_us, while a second batch
+ * gathers, and returns each caller its own list (bit-identical to the call
+ * made alone). max_pairs = 0 turns it off. Not to be called while other
+ * threads call slm_ratio_match on the context; max_pairs <= 4096,
+ * window_us <= 1000000. */
+slm_status slm_ctx_set_coalescing(slm_ctx *ctx, uint32_t window_us, uint32_t max_pairs);
+/* Counters of the coalescer since it was set: batches run, calls matched in
+ * them, the largest batch (calls). All 0 while coalescing is off. */
+slm_status slm_ctx_coalescing_stats(slm_ctx *ctx, uint64_t *batches, uint64_t *calls, uint64_t *max_batch);
 /* Self-test of the bounded device waits (no reference counterpart): one GPU
  * thread waits on a barrier that nothing completes and gives up after `polls`
  * polls (1..65536). Returns SLM_TIMEOUT, the status every timed-out kernel

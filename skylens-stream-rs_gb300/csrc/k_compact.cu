@@ -121,6 +121,28 @@ void launch_scatter_rows(const uint4 *tab, uint32_t n, const float *src, float *
     }
 }
 
+// Rows of many views, each from its own source address (host memory the
+// device can read directly, or device memory), into their padded store rows:
+// e[v] = {source address low, high 32 bits, first store row, rows}.
+__global__ void __launch_bounds__(256) gather_rows_kernel(const ScatterTab tab, float4 *__restrict__ dst) {
+    const uint4 t = tab.e[blockIdx.x];
+    constexpr uint32_t kRow4 = 128 / 4;
+    const float4 *s = reinterpret_cast<const float4 *>(((uint64_t)t.y << 32) | t.x);
+    const uint64_t n4 = (uint64_t)t.w * kRow4;
+    float4 *d = dst + (uint64_t)t.z * kRow4;
+    for (uint64_t k = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x; k < n4; k += (uint64_t)gridDim.y * blockDim.x)
+        d[k] = s[k];
+}
+
+void launch_gather_rows(const uint4 *tab, uint32_t n, float *dst, cudaStream_t s) {
+    for (uint32_t b = 0; b < n; b += kScatterMax) {
+        const uint32_t m = n - b < kScatterMax ? n - b : kScatterMax;
+        ScatterTab t;
+        for (uint32_t k = 0; k < m; ++k) t.e[k] = tab[b + k];
+        gather_rows_kernel<<<dim3(m, 8), 256, 0, s>>>(t, reinterpret_cast<float4 *>(dst));
+    }
+}
+
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s) {
     if (!n) return;
     uint64_t blocks = (n + 255) / 256;

@@ -68,6 +68,11 @@ cudaError_t record_event(cudaEvent_t e, cudaStream_t s) {
 // ------------------------------------------------------------------ context
 
 struct Workspace;
+struct Coalescer;
+// Coalescing of concurrent single-pair calls (defined with the serving code).
+void coalescer_destroy(slm_ctx *c);
+slm_status coalesce_call(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb, float ratio,
+                         int mutual, slm_pair *out, uint32_t cap, uint32_t *n_out, slm_stats *st);
 
 struct slm_ctx {
     int device = 0;
@@ -78,6 +83,7 @@ struct slm_ctx {
     // the CPU-GPU link, as on Grace-based GB300 systems): single-pair inputs are
     // then read by the packing kernels where they lie instead of being copied.
     bool host_direct = false;
+    Coalescer *coal = nullptr;  // set by slm_ctx_set_coalescing
     uint64_t budget = 0;
     std::atomic<uint64_t> used{0};
     std::mutex mu;
@@ -226,6 +232,8 @@ struct slm_plan {
 namespace slm {
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t v, cudaStream_t s);
 void launch_scatter_rows(const uint4 *tab, uint32_t n, const float *src, float *dst, cudaStream_t s);
+// Each view's rows from its own 16-byte-aligned source address: {addr lo, addr hi, store row, rows}.
+void launch_gather_rows(const uint4 *tab, uint32_t n, float *dst, cudaStream_t s);
 void launch_filter_counts(uint32_t *counts, uint32_t np, uint32_t min_matches, cudaStream_t s);
 void launch_scan_counts(const uint32_t *counts, uint32_t np, uint64_t *offsets, cudaStream_t s);
 void launch_gather(const uint2 *slots, const uint64_t *slot_off, const uint32_t *counts, const uint64_t *offsets,
@@ -783,6 +791,7 @@ extern "C" slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out) {
 extern "C" slm_status slm_ctx_destroy(slm_ctx *c) {
     if (!c) return SLM_OK;
     cudaSetDevice(c->device);
+    coalescer_destroy(c);
     cudaDeviceSynchronize();
     for (Workspace *w : c->all) {
         if (w->stream) cudaStreamDestroy(w->stream);
@@ -1333,6 +1342,7 @@ extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, c
                                       float ratio, int mutual, slm_precision prec, slm_pair *out, uint32_t cap,
                                       uint32_t *n_out, slm_stats *st) {
     SLM_TRY(check_pair_args(c, a, na, b, nb, ratio, prec));
+    const bool coalesce = prec == SLM_PREC_AUTO && c->coal;
     prec = resolve_prec(prec, (uint64_t)na * nb);
     if (!n_out || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL output");
     *n_out = 0;
@@ -1343,6 +1353,7 @@ extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, c
         return SLM_OK;
     }
     SLM_TRY(ctx_check_device(c));
+    if (coalesce) return coalesce_call(c, a, na, b, nb, ratio, mutual, out, cap, n_out, st);
     Workspace *w = nullptr;
     SLM_TRY(ws_acquire(c, &w));
     WsGuard guard{c, w};
@@ -1839,5 +1850,335 @@ extern "C" slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st
     std::lock_guard<std::mutex> g(srv->mu);
     *st = srv->stats;
     st->bytes_in_use = srv->ctx->used.load();
+    return SLM_OK;
+}
+
+// ------------------------------------------------------------- coalescing
+//
+// Concurrent single-pair calls (the reference's rayon workers call
+// ratio_match once per pair, matching.rs:167 from pipeline.rs:487-493) are
+// queued when coalescing is on: a worker thread gathers the waiting calls into
+// one batch plan (each call's two arrays become two views of the batch's
+// store), runs it on one of two slots so that one batch gathers while the
+// other runs, and hands every caller its own list. Results are those of the
+// call made alone (every precision is bit-exact).
+
+namespace {
+
+struct CoalReq {
+    const float *a = nullptr, *b = nullptr;
+    uint32_t na = 0, nb = 0;
+    float ratio = 0.f;
+    int mutual = 0;
+    slm_pair *out = nullptr;
+    uint32_t cap = 0;
+    uint32_t *n_out = nullptr;
+    slm_stats *st = nullptr;
+    slm_status status = SLM_OK;
+    std::string error;
+    bool done = false;
+    Clock::time_point t_submit;
+};
+
+struct CoalSlot {
+    Workspace w;
+    cudaEvent_t done = nullptr;
+    std::vector<CoalReq *> reqs;
+    bool busy = false;
+    // pinned host copy of a finished batch: [error word, pad, offsets (np + 1), pairs]
+    void *host = nullptr;
+    size_t host_bytes = 0;
+    ~CoalSlot() {
+        if (host) cudaFreeHost(host);
+    }
+};
+
+}  // namespace
+
+struct Coalescer {
+    slm_ctx *ctx = nullptr;
+    uint32_t window_us = 0, max_pairs = 0;
+    CoalSlot slots[2];
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<CoalReq *> pending;
+    Clock::time_point last_arrival;
+    bool stop = false;
+    uint64_t batches = 0, pairs = 0, max_batch = 0;
+};
+
+namespace {
+
+void coal_finish(Coalescer *co, CoalReq *r, slm_status s, const std::string &err) {
+    r->status = s;
+    r->error = err;
+    r->done = true;
+}
+
+// Results of a finished slot, distributed to its callers (called with co->mu held).
+void coal_collect(Coalescer *co, CoalSlot *s) {
+    slm_plan *p = &s->w.plan;
+    const uint32_t *hw = static_cast<const uint32_t *>(s->host);
+    const uint64_t *off = reinterpret_cast<const uint64_t *>(hw + 2);
+    const slm_pair *dense = reinterpret_cast<const slm_pair *>(off + p->np + 1);
+    slm_status rs = SLM_OK;
+    if (cudaEventQuery(s->done) != cudaSuccess) {
+        cudaGetLastError();
+        rs = fail(SLM_CUDA_ERROR, "batch failed on the device");
+    } else if (hw[0] == DERR_TIMEOUT_BAR || hw[0] == DERR_TIMEOUT_MMA) {
+        rs = fail(SLM_TIMEOUT, "device wait gave up (code " + std::to_string(hw[0]) + ")");
+    } else if (hw[0]) {
+        rs = fail(SLM_INTERNAL, "device invariant failed (code " + std::to_string(hw[0]) + ")");
+    }
+    const std::string err = rs == SLM_OK ? std::string() : g_last_error;
+    for (size_t k = 0; k < s->reqs.size(); ++k) {
+        CoalReq *r = s->reqs[k];
+        if (rs != SLM_OK) {
+            coal_finish(co, r, rs, err);
+            continue;
+        }
+        const uint64_t n = off[k + 1] - off[k];
+        *r->n_out = (uint32_t)n;
+        if (r->st) {
+            std::memset(r->st, 0, sizeof(*r->st));
+            r->st->pairs = 1;
+            r->st->distances = (uint64_t)r->na * r->nb;
+            r->st->matches = n;
+        }
+        if (n > r->cap) {
+            coal_finish(co, r, SLM_CAPACITY, "need " + std::to_string(n) + " pairs, have " + std::to_string(r->cap));
+            continue;
+        }
+        if (n) std::memcpy(r->out, dense + off[k], sizeof(slm_pair) * n);
+        coal_finish(co, r, SLM_OK, std::string());
+    }
+    s->reqs.clear();
+    s->busy = false;
+}
+
+// Upload, plan and launch one batch on a free slot (called with co->mu held).
+slm_status coal_issue(Coalescer *co, CoalSlot *s, std::vector<CoalReq *> &take) {
+    slm_ctx *c = co->ctx;
+    Workspace *w = &s->w;
+    uint64_t rows = 0, dist = 0;
+    for (CoalReq *r : take) {
+        rows += pad_rows(r->na) + pad_rows(r->nb);
+        dist += (uint64_t)r->na * r->nb;
+    }
+    slm_store *st = &w->store;
+    SLM_TRY(store_reserve(st, std::max<uint64_t>(rows, kTile)));
+    slm_store_clear(st);
+    std::vector<slm_pair> pr(take.size());
+    bool direct = c->host_direct;
+    for (CoalReq *r : take) direct &= ((reinterpret_cast<uintptr_t>(r->a) | reinterpret_cast<uintptr_t>(r->b)) & 15) == 0;
+    if (direct) {
+        // one kernel reads every caller's arrays where they lie (no copies by this thread)
+        std::vector<uint4> tab;
+        tab.reserve(2 * take.size());
+        auto add = [&](const float *src, uint32_t n, uint32_t *id) {
+            const uint64_t row0 = store_place(st, n, id);
+            const uint64_t adr = reinterpret_cast<uint64_t>(src);
+            if (n) tab.push_back(make_uint4((uint32_t)adr, (uint32_t)(adr >> 32), (uint32_t)row0, n));
+        };
+        for (size_t k = 0; k < take.size(); ++k) {
+            add(take[k]->a, take[k]->na, &pr[k].i);
+            add(take[k]->b, take[k]->nb, &pr[k].j);
+        }
+        launch_gather_rows(tab.data(), (uint32_t)tab.size(), st->raw.as<float>(), w->stream);
+        SLM_CU(cudaGetLastError());
+    } else {
+        for (size_t k = 0; k < take.size(); ++k) {
+            SLM_TRY(store_append(st, take[k]->a, take[k]->na, false, w->stream, &pr[k].i));
+            SLM_TRY(store_append(st, take[k]->b, take[k]->nb, false, w->stream, &pr[k].j));
+        }
+    }
+    slm_tune t{};
+    t.use_graph = 2;  // a new shape every batch: plain launches
+    SLM_TRY(plan_init(&w->plan, c, st, pr.data(), (uint32_t)pr.size(), take[0]->ratio, take[0]->mutual,
+                      resolve_prec(SLM_PREC_AUTO, dist), &t, w->stream));
+    SLM_TRY(plan_launch_on(&w->plan, w->stream, false));
+    // results come back with the batch: one pinned copy of the error word,
+    // the offsets and every slot the pairs may fill
+    slm_plan *p = &w->plan;
+    const size_t off_bytes = sizeof(uint64_t) * (p->np + 1), pair_bytes = sizeof(slm_pair) * p->n_slots;
+    const size_t need = 8 + off_bytes + pair_bytes;
+    if (need > s->host_bytes) {
+        if (s->host) cudaFreeHost(s->host);
+        s->host = nullptr;
+        s->host_bytes = 0;
+        SLM_CU(cudaHostAlloc(&s->host, need + need / 4, cudaHostAllocDefault));
+        s->host_bytes = need + need / 4;
+    }
+    unsigned char *h = static_cast<unsigned char *>(s->host);
+    SLM_CU(cudaMemcpyAsync(h, p->d_ctl.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    SLM_CU(cudaMemcpyAsync(h + 8, p->d_offsets.p, off_bytes, cudaMemcpyDeviceToHost, w->stream));
+    if (pair_bytes) SLM_CU(cudaMemcpyAsync(h + 8 + off_bytes, p->d_dense.p, pair_bytes, cudaMemcpyDeviceToHost, w->stream));
+    SLM_CU(cudaEventRecord(s->done, w->stream));
+    return SLM_OK;
+}
+
+void coal_loop(Coalescer *co) {
+    cudaSetDevice(co->ctx->device);
+    std::unique_lock<std::mutex> lk(co->mu);
+    const auto tick = std::chrono::microseconds(20);  // completion polling while a batch runs
+    const auto win = std::chrono::microseconds(co->window_us);
+    for (;;) {
+        // completions
+        bool finished = false;
+        for (CoalSlot &s : co->slots)
+            if (s.busy && cudaEventQuery(s.done) != cudaErrorNotReady) {
+                cudaGetLastError();
+                coal_collect(co, &s);
+                finished = true;
+            }
+        if (finished) co->cv_done.notify_all();
+        // admission: a free slot takes the waiting calls with the oldest call's
+        // ratio and cross-check once the batch is full, the queue has been quiet
+        // for the window (callers released together have all come back), or the
+        // oldest call has waited 8 windows
+        for (CoalSlot &s : co->slots) {
+            if (s.busy || co->pending.empty()) continue;
+            const CoalReq *first = co->pending.front();
+            const auto now = Clock::now();
+            const bool full = co->pending.size() >= co->max_pairs;
+            const bool quiet = now - co->last_arrival >= win;
+            const bool overdue = now - first->t_submit >= 8 * win;
+            if (!full && !quiet && !overdue && !co->stop) break;
+            std::vector<CoalReq *> take;
+            for (auto it = co->pending.begin(); it != co->pending.end() && take.size() < co->max_pairs;) {
+                if ((*it)->ratio == first->ratio && (*it)->mutual == first->mutual) {
+                    take.push_back(*it);
+                    it = co->pending.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            const slm_status is = coal_issue(co, &s, take);
+            if (is != SLM_OK) {
+                for (CoalReq *r : take) coal_finish(co, r, is, g_last_error);
+                co->cv_done.notify_all();
+                continue;
+            }
+            s.reqs = std::move(take);
+            s.busy = true;
+            co->batches++;
+            co->pairs += s.reqs.size();
+            co->max_batch = std::max<uint64_t>(co->max_batch, s.reqs.size());
+        }
+        const bool busy = co->slots[0].busy || co->slots[1].busy;
+        const bool slot_free = !co->slots[0].busy || !co->slots[1].busy;
+        if (co->stop && !busy && co->pending.empty()) break;
+        // sleep until a call arrives (idle), the next completion poll (a batch
+        // runs) or the moment the waiting calls may start
+        if (co->pending.empty() && !busy) {
+            co->cv_work.wait(lk, [&] { return co->stop || !co->pending.empty(); });
+            continue;
+        }
+        auto wake = Clock::now() + tick;
+        if (!co->pending.empty() && slot_free) {
+            const auto ready = std::min(co->last_arrival + win, co->pending.front()->t_submit + 8 * win);
+            wake = busy ? std::min(wake, ready) : ready;
+        }
+        const size_t npend = co->pending.size();
+        co->cv_work.wait_until(lk, wake, [&] {
+            return co->stop || (slot_free && co->pending.size() >= co->max_pairs && co->pending.size() != npend);
+        });
+    }
+}
+
+void coal_stop(slm_ctx *c) {
+    Coalescer *co = c->coal;
+    if (!co) return;
+    {
+        std::lock_guard<std::mutex> g(co->mu);
+        co->stop = true;
+    }
+    co->cv_work.notify_all();
+    if (co->worker.joinable()) co->worker.join();
+    for (CoalSlot &s : co->slots) {
+        if (s.w.stream) cudaStreamSynchronize(s.w.stream);
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.w.stream) cudaStreamDestroy(s.w.stream);
+        s.w.stream = nullptr;
+    }
+    delete co;
+    c->coal = nullptr;
+}
+
+}  // namespace
+
+void coalescer_destroy(slm_ctx *c) { coal_stop(c); }
+
+// Queues one AUTO call on the context's coalescer and waits for its result.
+slm_status coalesce_call(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb, float ratio,
+                         int mutual, slm_pair *out, uint32_t cap, uint32_t *n_out, slm_stats *st) {
+    Coalescer *co = c->coal;
+    CoalReq r;
+    r.a = a;
+    r.b = b;
+    r.na = na;
+    r.nb = nb;
+    r.ratio = ratio;
+    r.mutual = mutual;
+    r.out = out;
+    r.cap = cap;
+    r.n_out = n_out;
+    r.st = st;
+    r.t_submit = Clock::now();
+    std::unique_lock<std::mutex> lk(co->mu);
+    if (co->stop) return fail(SLM_INVALID_ARG, "context is being destroyed");
+    co->pending.push_back(&r);
+    co->last_arrival = r.t_submit;
+    co->cv_work.notify_all();
+    co->cv_done.wait(lk, [&] { return r.done; });
+    if (r.status != SLM_OK) {
+        g_last_error = r.error;
+        return r.status;
+    }
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_ctx_set_coalescing(slm_ctx *c, uint32_t window_us, uint32_t max_pairs) {
+    if (!c) return fail(SLM_INVALID_ARG, "NULL context");
+    if (max_pairs > 4096) return fail(SLM_INVALID_ARG, "max_pairs must be at most 4096");
+    if (window_us > 1000000) return fail(SLM_INVALID_ARG, "window_us must be at most 1000000");
+    SLM_TRY(ctx_check_device(c));
+    coal_stop(c);  // waits for calls in flight; a new setting starts a new worker
+    if (max_pairs == 0) return SLM_OK;
+    auto *co = new (std::nothrow) Coalescer();
+    if (!co) return fail(SLM_OOM, "host allocation failed");
+    co->ctx = c;
+    co->window_us = window_us;
+    co->max_pairs = max_pairs;
+    for (CoalSlot &s : co->slots) {
+        if (cudaStreamCreateWithFlags(&s.w.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            for (CoalSlot &q : co->slots) {
+                if (q.done) cudaEventDestroy(q.done);
+                if (q.w.stream) cudaStreamDestroy(q.w.stream);
+            }
+            delete co;
+            return fail(SLM_CUDA_ERROR, "coalescer stream or event creation failed");
+        }
+        s.w.store.ctx = c;
+        s.w.plan.ctx = c;
+        s.w.plan.st = &s.w.store;
+    }
+    c->coal = co;
+    co->worker = std::thread(coal_loop, co);
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_ctx_coalescing_stats(slm_ctx *c, uint64_t *batches, uint64_t *calls, uint64_t *max_batch) {
+    if (!c || !batches || !calls || !max_batch) return fail(SLM_INVALID_ARG, "NULL argument");
+    *batches = *calls = *max_batch = 0;
+    Coalescer *co = c->coal;
+    if (!co) return SLM_OK;
+    std::lock_guard<std::mutex> g(co->mu);
+    *batches = co->batches;
+    *calls = co->pairs;
+    *max_batch = co->max_batch;
     return SLM_OK;
 }

@@ -93,6 +93,9 @@ extern "C" {
     pub fn slm_status_str(s: SlmStatus) -> *const c_char;
     pub fn slm_last_error() -> *const c_char;
     pub fn slm_selftest_wait_timeout(ctx: *mut slm_ctx, polls: u32) -> SlmStatus;
+    pub fn slm_ctx_set_coalescing(ctx: *mut slm_ctx, window_us: u32, max_pairs: u32) -> SlmStatus;
+    pub fn slm_ctx_coalescing_stats(ctx: *mut slm_ctx, batches: *mut u64, calls: *mut u64,
+                                    max_batch: *mut u64) -> SlmStatus;
     pub fn slm_ctx_create(opts: *const slm_opts, out: *mut *mut slm_ctx) -> SlmStatus;
     pub fn slm_ctx_destroy(ctx: *mut slm_ctx) -> SlmStatus;
     pub fn slm_ctx_stream(ctx: *mut slm_ctx) -> *mut c_void;

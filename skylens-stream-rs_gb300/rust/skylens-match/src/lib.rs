@@ -73,6 +73,14 @@ fn pack<D: Descriptor>(v: &[D]) -> Vec<f32> {
     out
 }
 
+/// Batch concurrent `ratio_match` calls of the process-wide context (rayon
+/// workers calling it once per pair): up to `max_pairs` calls per batch, each
+/// waiting at most `window_us` for company; `max_pairs = 0` turns it off.
+/// Call it before the workers start. Results are unchanged (bit-exact).
+pub fn set_coalescing(window_us: u32, max_pairs: u32) {
+    check(unsafe { sys::slm_ctx_set_coalescing(ctx(), window_us, max_pairs) }, "slm_ctx_set_coalescing");
+}
+
 /// Drop-in for `skylens_core::matching::ratio_match` (exact; the BF16
 /// shortlist for large pairs, the plain FP32 kernel for small ones).
 pub fn ratio_match<D: Descriptor>(a: &[D], b: &[D], ratio: f32, mutual: bool) -> Vec<(usize, usize)> {

@@ -80,6 +80,8 @@ SIGNATURES = {
     "slm_status_str": (ctypes.c_char_p, [c_int]),
     "slm_last_error": (ctypes.c_char_p, []),
     "slm_selftest_wait_timeout": (c_int, [ctypes.c_void_p, c_u32]),
+    "slm_ctx_set_coalescing": (c_int, [ctypes.c_void_p, c_u32, c_u32]),
+    "slm_ctx_coalescing_stats": (c_int, [ctypes.c_void_p, P(c_u64), P(c_u64), P(c_u64)]),
     "slm_ctx_create": (c_int, [P(SlmOpts), P(ctypes.c_void_p)]),
     "slm_ctx_destroy": (c_int, [ctypes.c_void_p]),
     "slm_ctx_stream": (ctypes.c_void_p, [ctypes.c_void_p]),

@@ -90,6 +90,17 @@ class Matcher:
     def bytes_in_use(self) -> int:
         return int(self._L.slm_ctx_bytes_in_use(self._h))
 
+    def set_coalescing(self, window_us: int = 50, max_pairs: int = 256) -> None:
+        """slm_ctx_set_coalescing: batch concurrent AUTO ratio_match calls
+        (max_pairs = 0 turns it off)."""
+        check(self._L.slm_ctx_set_coalescing(self._h, window_us, max_pairs), "slm_ctx_set_coalescing")
+
+    def coalescing_stats(self) -> dict:
+        b, c, m = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(self._L.slm_ctx_coalescing_stats(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(m)),
+              "slm_ctx_coalescing_stats")
+        return {"batches": b.value, "calls": c.value, "max_batch": m.value}
+
     def selftest_wait_timeout(self, polls: int = 256) -> int:
         """Runs the bounded-wait self-test (slm_selftest_wait_timeout) and
         returns its status: SLM_TIMEOUT when the device wait gave up as it must."""
