@@ -60,21 +60,18 @@ __global__ void __launch_bounds__(256) pack_fp32_kernel(const float *__restrict_
     }
 }
 
-// Many views at once: one CTA per entry of a tile table
-// {first store row of the view, rows of the view, tile within the view, view}.
-__global__ void __launch_bounds__(256) pack_fp32_tiles_kernel(const uint4 *__restrict__ tab,
-                                                              const float *__restrict__ raw,
-                                                              float *__restrict__ tiled) {
-    const uint4 e = tab[blockIdx.x];
-    __shared__ float sm[32][kDesc + 1];
-    const float *src = raw + (size_t)e.x * kDesc;
-    float *dst = tiled + (size_t)(e.x / kTile + e.z) * kTileFloats;
+// Tile `tile` of the view whose rows start at store row `row0` (n rows): raw
+// rows -> tile[slot][row]. Called by all 256 threads of a CTA alike.
+SLM_DEV void pack_view_tile(const float *__restrict__ raw, float *__restrict__ tiled, uint32_t row0, uint32_t n,
+                            uint32_t tile, float (&sm)[32][kDesc + 1]) {
+    const float *src = raw + (size_t)row0 * kDesc;
+    float *dst = tiled + (size_t)(row0 / kTile + tile) * kTileFloats;
     for (int g = 0; g < 4; ++g) {
-        const uint32_t r0 = e.z * kTile + g * 32;
+        const uint32_t r0 = tile * kTile + g * 32;
         for (int q = threadIdx.x; q < 32 * 32; q += 256) {
             const int r = q >> 5, c = q & 31;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + r < e.y) v = reinterpret_cast<const float4 *>(src + (size_t)(r0 + r) * kDesc)[c];
+            if (r0 + r < n) v = reinterpret_cast<const float4 *>(src + (size_t)(r0 + r) * kDesc)[c];
             sm[r][4 * c + 0] = v.x;
             sm[r][4 * c + 1] = v.y;
             sm[r][4 * c + 2] = v.z;
@@ -88,6 +85,41 @@ __global__ void __launch_bounds__(256) pack_fp32_tiles_kernel(const uint4 *__res
         }
         __syncthreads();
     }
+}
+
+// Many views at once: one CTA per entry of a tile table
+// {first store row of the view, rows of the view, tile within the view, view}.
+__global__ void __launch_bounds__(256) pack_fp32_tiles_kernel(const uint4 *__restrict__ tab,
+                                                              const float *__restrict__ raw,
+                                                              float *__restrict__ tiled) {
+    __shared__ float sm[32][kDesc + 1];
+    const uint4 e = tab[blockIdx.x];
+    pack_view_tile(raw, tiled, e.x, e.y, e.z, sm);
+}
+
+// The FP32 tiles of both views of every routed pair of a low-precision batch
+// (the only readers of FP32 tiles on that path), packed on the device once the
+// routed pairs are known; with nothing routed every CTA returns at once. A
+// view shared by several routed pairs is packed once per pair (same values).
+__global__ void __launch_bounds__(256) pack_routed_kernel(const PairMeta *__restrict__ pairs,
+                                                          const uint32_t *__restrict__ xlist,
+                                                          const uint32_t *__restrict__ count,
+                                                          const float *__restrict__ raw, float *__restrict__ tiled) {
+    __shared__ float sm[32][kDesc + 1];
+    const uint32_t n = *count;
+    for (uint32_t k = 0; k < n; ++k) {
+        const PairMeta pm = pairs[xlist[k]];
+        const uint32_t ta = (pm.na + kTile - 1) / kTile, tb = (pm.nb + kTile - 1) / kTile;
+        for (uint32_t t = blockIdx.x; t < ta + tb; t += gridDim.x) {
+            const bool is_a = t < ta;
+            pack_view_tile(raw, tiled, is_a ? pm.a_row0 : pm.b_row0, is_a ? pm.na : pm.nb, is_a ? t : t - ta, sm);
+        }
+    }
+}
+
+void launch_pack_routed(const PairMeta *pairs, const uint32_t *xlist, const uint32_t *count, const float *raw,
+                        float *tiled, int grid, cudaStream_t s) {
+    pack_routed_kernel<<<grid, 256, 0, s>>>(pairs, xlist, count, raw, tiled);
 }
 
 void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw, float *tiled, cudaStream_t s) {

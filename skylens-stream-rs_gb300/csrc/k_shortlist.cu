@@ -1585,12 +1585,17 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     x.err = a.ctl + 1;
     x.mutual = a.mutual;
     x.x2 = 1;
+    // BF16 batches rarely route a pair: the FP32 tiles the exact kernel reads
+    // are packed here for the routed pairs' views only (FP8 batches, which
+    // route most pairs of unit descriptors, keep the store's packed tiles)
+    if (!a.fp8)
+        launch_pack_routed(a.pairs, a.xlist, a.ctl + kCtlRoutedPairs, a.raw, const_cast<float *>(a.tiled), 2 * sms, s);
     launch_exact(x, sms, s);
     sl_route_finalize_kernel<<<dim3(rgrid, a.row_blocks), 256, 0, s>>>(a);
     sl_rescore_kernel<<<5 * sms, 256, 0, s>>>(a);  // 40 warps per SM: latency-bound gathers
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
     sl_compact_kernel<<<per_block, 256, 0, s>>>(a);
-    return 8;
+    return a.fp8 ? 8 : 9;
 }
 
 }  // namespace slm

@@ -988,14 +988,16 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
     }
     p->launched = false;
     p->dump = p->tune.variant == 2 && prec != SLM_PREC_FP32;
-    // FP32 tiles serve the exact kernel of every path (low precision: routed pairs)
-    SLM_TRY(store_sync_fp32(st, stream));
+    // FP32 tiles: the whole store for FP32 and FP8 plans (FP8 routes most
+    // pairs of unit descriptors to the exact kernel); a BF16 batch packs the
+    // tiles of its few routed pairs' views itself, on the device
+    if (prec != SLM_PREC_BF16) SLM_TRY(store_sync_fp32(st, stream));
     if (prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
     return plan_build(p, pairs);
 }
 
 slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
-    SLM_TRY(store_sync_fp32(p->st, s));
+    if (p->prec != SLM_PREC_BF16) SLM_TRY(store_sync_fp32(p->st, s));
     if (p->prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
     // a store buffer the captured graph reads may have moved: capture again
     if (p->exec && (p->st->tiled.p != p->graph_tiled ||
@@ -1675,7 +1677,8 @@ void serve_loop(slm_server *srv) {
             // FP32 tiles and low-precision images of the new views, on the
             // upload stream, so every slot that waits for the upload sees them.
             {
-                slm_status ls = store_sync_fp32(srv->store, srv->ctx->stream);
+                slm_status ls = SLM_OK;
+                if (srv->opts.prec != SLM_PREC_BF16) ls = store_sync_fp32(srv->store, srv->ctx->stream);
                 if (ls == SLM_OK && srv->opts.prec != SLM_PREC_FP32)
                     ls = store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream);
                 if (ls != SLM_OK) {

@@ -100,6 +100,10 @@ void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0
 // The same for many views: tab holds one {row0, n, tile, view} per tile.
 void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw, float *tiled, cudaStream_t s);
 void launch_exact(const ExactArgs &a, int grid, cudaStream_t s);
+// FP32 tiles of both views of the routed pairs xlist[0 .. *count) of a
+// low-precision batch (count read on the device).
+void launch_pack_routed(const PairMeta *pairs, const uint32_t *xlist, const uint32_t *count, const float *raw,
+                        float *tiled, int grid, cudaStream_t s);
 // Sets kernel attributes (large shared memory) once per device; called at
 // context creation, outside any stream capture. Fails if the kernel image
 // cannot load on the device.
