@@ -420,13 +420,17 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *err = g.ctl + 1;
     volatile uint32_t *abort_flag = &S.abort_flag;
+    // the epilogue reads the b stage in pass 2 (thresholds) and for FP8 (norms, scales)
+    constexpr bool kEpReadsB = PASS == 2 || FP8;
 
     if (threadIdx.x == 0) {
         mbar_init(&S.a_full, 1);
         mbar_init(&S.a_empty, 1 + kSlEpWarps);
         for (int s = 0; s < kStg; ++s) {
             mbar_init(&S.b_full[s], 1);
-            mbar_init(&S.b_empty[s], 1 + kSlEpWarps);
+            // BF16 pass 1's epilogue reads nothing of the b stage (norms are in the
+            // product): the MMA's commit alone frees it, one use earlier
+            mbar_init(&S.b_empty[s], kEpReadsB ? 1 + kSlEpWarps : 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&S.t_full[b], 1);
@@ -598,7 +602,12 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             uint32_t ncand = 0;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
-                if (!sl_wait(&S.b_full[st], sph, abort_flag, err) || !sl_wait(&S.t_full[tb], tph, abort_flag, err)) {
+                // without the epilogue's b_empty arrivals the producer may refill a
+                // stage twice before this warp would wait on it (its parity would be
+                // ambiguous): an epilogue that does not read the stage waits on t_full
+                // only, which implies the MMA consumed the stage
+                if ((kEpReadsB && !sl_wait(&S.b_full[st], sph, abort_flag, err)) ||
+                    !sl_wait(&S.t_full[tb], tph, abort_flag, err)) {
                     ok = false;
                     break;
                 }
@@ -794,7 +803,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     }
                 }
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&S.b_empty[st]);
+                if (kEpReadsB && lane == 0) mbar_arrive(&S.b_empty[st]);
                 if (++st == kStg) st = 0, sph ^= 1;
                 tb ^= 1;
                 if (tb == 0) tph ^= 1;
