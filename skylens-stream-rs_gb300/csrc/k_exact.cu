@@ -465,10 +465,11 @@ void launch_exact(const ExactArgs &a, int grid, cudaStream_t s) {
 // bandwidth problem; larger batches run 256 (more pairs resident per SM).
 constexpr int kFinThreadsMax = 1024;
 
-__global__ void __launch_bounds__(kFinThreadsMax) finalize_kernel(FinalizeArgs g) {
-    __shared__ uint32_t warp_tot[kFinThreadsMax / 32];
-    const uint32_t nthr = blockDim.x;
-    const int nwarps = (int)(nthr >> 5);
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) finalize_kernel(FinalizeArgs g) {
+    __shared__ uint32_t warp_tot[kThreads / 32];
+    constexpr uint32_t nthr = kThreads;
+    constexpr int nwarps = kThreads / 32;
     const PairMeta pm = g.pairs[blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const float kInf = __int_as_float(0x7f800000);
@@ -481,6 +482,9 @@ __global__ void __launch_bounds__(kFinThreadsMax) finalize_kernel(FinalizeArgs g
             float d1 = kInf, d2 = kInf;
             uint32_t j1 = 0xffffffffu;
             const RowPart *pr = g.parts + (size_t)(pm.part_base + rt * pm.nchunk) * kTile + (i % kTile);
+            if constexpr (kThreads == 256) {  // many pairs: mostly one column range per row
+                for (uint32_t c = 0; c < pm.nchunk; ++c) merge_rowpart(pr[(size_t)c * kTile], d1, d2, j1);
+            } else
             for (uint32_t c0 = 0; c0 < pm.nchunk; c0 += 4) {
                 RowPart q[4];
 #pragma unroll
@@ -519,7 +523,11 @@ __global__ void __launch_bounds__(kFinThreadsMax) finalize_kernel(FinalizeArgs g
 }
 
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s) {
-    if (a.npairs) finalize_kernel<<<a.npairs, a.npairs <= kFewPairs ? kFinThreadsMax : 256, 0, s>>>(a);
+    if (!a.npairs) return;
+    if (a.npairs <= kFewPairs)
+        finalize_kernel<kFinThreadsMax><<<a.npairs, kFinThreadsMax, 0, s>>>(a);
+    else
+        finalize_kernel<256><<<a.npairs, 256, 0, s>>>(a);
 }
 
 // Self-test of the bounded waits: thread 0 waits on an mbarrier that expects

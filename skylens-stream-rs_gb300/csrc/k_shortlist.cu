@@ -914,7 +914,10 @@ SLM_DEV uint32_t pair_blocks(const PairMeta &pm) {
 // from the pass-1 partials, column thresholds from the column minima, and the
 // near-chunk counts; the last CTA of a pair to finish makes the routing
 // decision from the pair's totals.
-__global__ void __launch_bounds__(1024) sl_mid_kernel(SlArgs g) {
+// kThreads: 256 for batches of many pairs, 1024 for a few (see kFewPairs);
+// the bound sets the register budget the compiler schedules for.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) sl_mid_kernel(SlArgs g) {
     __shared__ uint32_t wide_sh, open_sh, last_sh;
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
@@ -940,9 +943,19 @@ __global__ void __launch_bounds__(1024) sl_mid_kernel(SlArgs g) {
             const uint32_t super = i / 256, r = i % 256;
             float m1 = kInf, m2 = kInf;
             uint32_t near = 0;
-            // the column ranges' partials, four independent loads per step (an
-            // absent range merges as (inf, inf), near 0)
+            // the column ranges' partials: one load per step in batches of many
+            // pairs (mostly one range per row); four independent loads per step
+            // for a few pairs split into many ranges (an absent range merges as
+            // (inf, inf), near 0)
             const size_t slot0 = (size_t)(sp.part_base + super * sp.nchunk) * 256 + r;
+            if constexpr (kThreads == 256) {
+                for (uint32_t c = 0; c < sp.nchunk; ++c) {
+                    const float2 v = g.rowpart[slot0 + (size_t)c * 256];
+                    near += g.rownear[slot0 + (size_t)c * 256];
+                    m2 = fminf(fminf(m2, v.y), fmaxf(m1, v.x));
+                    m1 = fminf(m1, v.x);
+                }
+            } else
             for (uint32_t c0 = 0; c0 < sp.nchunk; c0 += 4) {
                 float2 v[4];
                 uint32_t nr[4];
@@ -1041,7 +1054,8 @@ SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &s
 // queue exact work. A pair with more than 1/8 as many overflowed row halves
 // (counted by pass 2) as rows is routed to the exact kernel instead (one exact
 // scan per row would cost more).
-__global__ void __launch_bounds__(1024) sl_finalize_kernel(SlArgs g) {
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) sl_finalize_kernel(SlArgs g) {
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
@@ -1570,7 +1584,10 @@ int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s) {
 
 int launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
     if (!a.npairs) return 0;
-    sl_mid_kernel<<<dim3(a.npairs, a.row_blocks), a.npairs <= kFewPairs ? 1024 : 256, 0, s>>>(a);
+    if (a.npairs <= kFewPairs)
+        sl_mid_kernel<1024><<<dim3(a.npairs, a.row_blocks), 1024, 0, s>>>(a);
+    else
+        sl_mid_kernel<256><<<dim3(a.npairs, a.row_blocks), 256, 0, s>>>(a);
     return 1;
 }
 
@@ -1578,7 +1595,10 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     if (!a.npairs) return 0;
     const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
     const dim3 per_block(a.npairs, a.row_blocks);  // CTA per pair and row block
-    sl_finalize_kernel<<<per_block, a.npairs <= kFewPairs ? 1024 : 256, 0, s>>>(a);
+    if (a.npairs <= kFewPairs)
+        sl_finalize_kernel<1024><<<per_block, 1024, 0, s>>>(a);
+    else
+        sl_finalize_kernel<256><<<per_block, 256, 0, s>>>(a);
     // routed pairs: plan, exact kernel over all their rows and columns, decisions
     sl_route_plan_kernel<<<1, 1024, 0, s>>>(a);
     sl_route_apply_kernel<<<rgrid, 256, 0, s>>>(a);
