@@ -21,7 +21,11 @@
 //               one thread per row, 16 columns per tcgen05.ld. Row minima use
 //               a 3-input min tree per 16 columns; column minima use
 //               redux.sync.min.f32 per column, merged across warps in shared
-//               memory and across CTAs with one atomicMin per column and tile.
+//               memory (by the epilogue warps of sub-partitions 2 and 3) and
+//               across CTAs with one atomicMin per column and tile. Pass 2
+//               looks for row-candidate and column-window hits in groups of 4
+//               columns behind the chunk minimum. BF16 pass 1 never reads the
+//               b stage: the MMA's commit alone frees it.
 #include <cuda_fp8.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
