@@ -14,7 +14,7 @@ from skylens_match import serve, synth
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec", ["bf16", "fp32"])
+@pytest.mark.parametrize("prec", ["bf16", "fp32", "fp8"])
 def test_serving_results_same_alone_and_in_the_mix(prec):
     z = synth.zone(positions=7, n_range=(150, 900), seed=21)
     reqs = serve.zone_requests(z)
