@@ -58,7 +58,7 @@ typedef enum {
 
 /* SLM_PREC_AUTO's switch point, measured on GB300 through slm_ratio_match:
  * 2048 x 2048 descriptors FP32 0.24 ms / BF16 0.28 ms, 3072 x 3072 0.36 / 0.34 ms. */
-#define SLM_AUTO_BF16_DISTANCES 6000000ull
+#define SLM_AUTO_BF16_DISTANCES 9000000ull
 
 typedef struct {
     uint32_t i, j;
