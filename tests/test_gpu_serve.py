@@ -40,3 +40,24 @@ def test_serving_results_same_alone_and_in_the_mix(prec):
         for (u, _), a_k, m_k in zip(pairs, ra, rm):
             assert np.array_equal(a_k, m_k), (u, v)
             assert np.array_equal(a_k, O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=8)), (u, v)
+
+
+def test_serving_within_a_small_hbm_budget():
+    """Admission by free HBM: with a budget that holds the store and only a few
+    requests' batches, requests queue and run in more, smaller batches; every
+    result is still the oracle's and the device memory in use stays within
+    the budget."""
+    z = synth.zone(positions=7, n_range=(150, 900), seed=22)
+    reqs = serve.zone_requests(z)
+    total = int(z.counts.sum())
+    budget = 48 << 20
+    srv = serve.Server(total, len(z.counts), "bf16", slots=3, hbm_budget=budget)
+    res, lats, wall = serve.stream_zone(srv, z, rate=None)
+    st = srv.stats()
+    srv.close()
+    print("small budget:", st)
+    assert st["completed"] == len(reqs)
+    assert 0 < st["bytes_in_use"] <= budget
+    for (v, pairs), rv in zip(reqs, res):
+        for (u, _), m_k in zip(pairs, rv):
+            assert np.array_equal(m_k, O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=8)), (u, v)
