@@ -56,9 +56,10 @@ typedef enum {
                           batch), FP32 below, where the shortlist's fixed cost dominates */
 } slm_precision;
 
-/* SLM_PREC_AUTO's switch point, measured on GB300 through slm_ratio_match:
- * 2048 x 2048 descriptors FP32 0.24 ms / BF16 0.28 ms, 3072 x 3072 0.36 / 0.34 ms. */
-#define SLM_AUTO_BF16_DISTANCES 9000000ull
+/* SLM_PREC_AUTO's switch point, measured on GB300 through slm_ratio_match from
+ * host arrays: 3072 x 3072 descriptors FP32 0.21 ms / BF16 0.25 ms,
+ * 3584 x 3584 0.25 / 0.26 ms, 4096 x 4096 0.31 / 0.28 ms. */
+#define SLM_AUTO_BF16_DISTANCES 12000000ull
 
 typedef struct {
     uint32_t i, j;

@@ -124,14 +124,25 @@ void launch_scatter_rows(const uint4 *tab, uint32_t n, const float *src, float *
 // Rows of many views, each from its own source address (host memory the
 // device can read directly, or device memory), into their padded store rows:
 // e[v] = {source address low, high 32 bits, first store row, rows}.
+// Each thread issues four 16-byte loads before it stores any of them, so that
+// many loads are in flight: reads of host memory over the chip-to-chip link are
+// bound by their latency.
 __global__ void __launch_bounds__(256) gather_rows_kernel(const ScatterTab tab, float4 *__restrict__ dst) {
     const uint4 t = tab.e[blockIdx.x];
     constexpr uint32_t kRow4 = 128 / 4;
-    const float4 *s = reinterpret_cast<const float4 *>(((uint64_t)t.y << 32) | t.x);
+    const float4 *__restrict__ s = reinterpret_cast<const float4 *>(((uint64_t)t.y << 32) | t.x);
     const uint64_t n4 = (uint64_t)t.w * kRow4;
     float4 *d = dst + (uint64_t)t.z * kRow4;
-    for (uint64_t k = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x; k < n4; k += (uint64_t)gridDim.y * blockDim.x)
-        d[k] = s[k];
+    const uint64_t stride = (uint64_t)gridDim.y * blockDim.x;
+    for (uint64_t k = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x; k < n4; k += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k + u * stride < n4) v[u] = s[k + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k + u * stride < n4) d[k + u * stride] = v[u];
+    }
 }
 
 void launch_gather_rows(const uint4 *tab, uint32_t n, float *dst, cudaStream_t s) {
@@ -139,7 +150,7 @@ void launch_gather_rows(const uint4 *tab, uint32_t n, float *dst, cudaStream_t s
         const uint32_t m = n - b < kScatterMax ? n - b : kScatterMax;
         ScatterTab t;
         for (uint32_t k = 0; k < m; ++k) t.e[k] = tab[b + k];
-        gather_rows_kernel<<<dim3(m, 8), 256, 0, s>>>(t, reinterpret_cast<float4 *>(dst));
+        gather_rows_kernel<<<dim3(m, 16), 256, 0, s>>>(t, reinterpret_cast<float4 *>(dst));
     }
 }
 

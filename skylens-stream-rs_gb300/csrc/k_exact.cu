@@ -26,6 +26,7 @@
 // (d1 < (r*r)*d2 in f32) and the mutual check, and compacts in ascending i.
 #include <cuda_runtime.h>
 
+#include "pack.cuh"
 #include "ptx.cuh"
 #include "slm_internal.h"
 
@@ -33,31 +34,13 @@ namespace slm {
 
 // ------------------------------------------------------------------ pack
 
-// One CTA per 128-row tile: row-major rows -> tile[slot][row].
+// One CTA per 32-row group of a 128-row tile (grid tiles x 4): row-major
+// rows -> tile[slot][row]. Four CTAs per tile keep four times as many loads in
+// flight as one, which is what sets the time when src is host memory.
 __global__ void __launch_bounds__(256) pack_fp32_kernel(const float *__restrict__ src, uint32_t n,
                                                         float *__restrict__ tiled, uint32_t tile0) {
     __shared__ float sm[32][kDesc + 1];
-    const uint32_t tile = blockIdx.x;
-    float *dst = tiled + (size_t)(tile0 + tile) * kTileFloats;
-    for (int g = 0; g < 4; ++g) {
-        const uint32_t r0 = tile * kTile + g * 32;
-        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
-            const int r = e >> 5, q = e & 31;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + r < n) v = reinterpret_cast<const float4 *>(src + (size_t)(r0 + r) * kDesc)[q];
-            sm[r][4 * q + 0] = v.x;
-            sm[r][4 * q + 1] = v.y;
-            sm[r][4 * q + 2] = v.z;
-            sm[r][4 * q + 3] = v.w;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < 32 * kDesc; e += 256) {
-            const int slot = e >> 5, r = e & 31;
-            const int k = 8 * (slot & 15) + (slot >> 4);  // inverse of perm_slot
-            dst[slot * kTile + g * 32 + r] = sm[r][k];
-        }
-        __syncthreads();
-    }
+    pack_group(src, n, tiled + (size_t)(tile0 + blockIdx.x) * kTileFloats, blockIdx.x, blockIdx.y, sm);
 }
 
 // Tile `tile` of the view whose rows start at store row `row0` (n rows): raw
@@ -66,25 +49,7 @@ SLM_DEV void pack_view_tile(const float *__restrict__ raw, float *__restrict__ t
                             uint32_t tile, float (&sm)[32][kDesc + 1]) {
     const float *src = raw + (size_t)row0 * kDesc;
     float *dst = tiled + (size_t)(row0 / kTile + tile) * kTileFloats;
-    for (int g = 0; g < 4; ++g) {
-        const uint32_t r0 = tile * kTile + g * 32;
-        for (int q = threadIdx.x; q < 32 * 32; q += 256) {
-            const int r = q >> 5, c = q & 31;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + r < n) v = reinterpret_cast<const float4 *>(src + (size_t)(r0 + r) * kDesc)[c];
-            sm[r][4 * c + 0] = v.x;
-            sm[r][4 * c + 1] = v.y;
-            sm[r][4 * c + 2] = v.z;
-            sm[r][4 * c + 3] = v.w;
-        }
-        __syncthreads();
-        for (int q = threadIdx.x; q < 32 * kDesc; q += 256) {
-            const int slot = q >> 5, r = q & 31;
-            const int k = 8 * (slot & 15) + (slot >> 4);  // inverse of perm_slot
-            dst[slot * kTile + g * 32 + r] = sm[r][k];
-        }
-        __syncthreads();
-    }
+    for (int g = 0; g < 4; ++g) pack_group(src, n, dst, tile, g, sm);
 }
 
 // Many views at once: one CTA per entry of a tile table
@@ -128,7 +93,7 @@ void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw,
 
 void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0, cudaStream_t s) {
     const uint32_t tiles = (n + kTile - 1) / kTile;
-    if (tiles) pack_fp32_kernel<<<tiles, 256, 0, s>>>(src, n, tiled, tile0);
+    if (tiles) pack_fp32_kernel<<<dim3(tiles, 4), 256, 0, s>>>(src, n, tiled, tile0);
 }
 
 __global__ void fill_u64_kernel(unsigned long long *p, uint64_t n, unsigned long long v) {

@@ -29,6 +29,7 @@
 #include <mutex>
 #include <string>
 
+#include "pack.cuh"
 #include "slm.h"
 #include "slm_internal.h"
 
@@ -64,39 +65,58 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 DeviceSetup g_setup[kMaxDevices];
 
-// Writes the single pair's metadata and its work items, clears the work
-// counter, error word and match count.
-__global__ void single_setup_kernel(unsigned char *scratch, SingleLayout L, uint32_t na, uint32_t nb) {
-    Item *items = reinterpret_cast<Item *>(scratch + L.items);
-    PairMeta *meta = reinterpret_cast<PairMeta *>(scratch + L.meta);
-    uint32_t *ctl = reinterpret_cast<uint32_t *>(scratch + L.ctl);
-    uint32_t *counts = reinterpret_cast<uint32_t *>(scratch + L.counts);
-    const uint32_t chunks = L.chunks, n_items = L.rt_n * chunks;
-    for (uint32_t k = threadIdx.x; k < n_items; k += blockDim.x) {
-        const uint32_t rt = k / chunks, c = k % chunks;
-        Item it;
-        it.pair = 0;
-        it.rt = rt;
-        it.ct0 = (uint32_t)((uint64_t)L.ct_n * c / chunks);
-        it.ct1 = (uint32_t)((uint64_t)L.ct_n * (c + 1) / chunks);
-        it.part = k;  // = rt * chunks + c, the layout finalize_kernel reads
-        it.pad[0] = it.pad[1] = it.pad[2] = 0;
-        items[k] = it;
+// Everything before the exact kernel, in one launch of 4 x (row tiles of a +
+// row tiles of b) CTAs: CTA k packs 32-row group k % 4 of tile k / 4 (the
+// tiles of a, then those of b); CTA 0 also writes the pair's metadata and work
+// items and clears the work counter, error word and match count; with the
+// cross-check every CTA clears its share of the column keys.
+__global__ void __launch_bounds__(256) single_prep_kernel(unsigned char *scratch, SingleLayout L, const float *d_a,
+                                                          uint32_t na, const float *d_b, uint32_t nb, int mutual) {
+    __shared__ float sm[32][kDesc + 1];
+    if (blockIdx.x == 0) {
+        Item *items = reinterpret_cast<Item *>(scratch + L.items);
+        PairMeta *meta = reinterpret_cast<PairMeta *>(scratch + L.meta);
+        uint32_t *ctl = reinterpret_cast<uint32_t *>(scratch + L.ctl);
+        uint32_t *counts = reinterpret_cast<uint32_t *>(scratch + L.counts);
+        const uint32_t chunks = L.chunks, n_items = L.rt_n * chunks;
+        for (uint32_t k = threadIdx.x; k < n_items; k += blockDim.x) {
+            const uint32_t rt = k / chunks, c = k % chunks;
+            Item it;
+            it.pair = 0;
+            it.rt = rt;
+            it.ct0 = (uint32_t)((uint64_t)L.ct_n * c / chunks);
+            it.ct1 = (uint32_t)((uint64_t)L.ct_n * (c + 1) / chunks);
+            it.part = k;  // = rt * chunks + c, the layout finalize_kernel reads
+            it.pad[0] = it.pad[1] = it.pad[2] = 0;
+            items[k] = it;
+        }
+        if (threadIdx.x == 0) {
+            PairMeta m;
+            m.a_row0 = 0;
+            m.b_row0 = L.rt_n * kTile;
+            m.na = na;
+            m.nb = nb;
+            m.nchunk = chunks;
+            m.part_base = 0;
+            m.col_base = 0;
+            m.slot_off = 0;
+            *meta = m;
+            *counts = 0;
+        }
+        if (threadIdx.x < 16) ctl[threadIdx.x] = 0;
     }
-    if (threadIdx.x == 0) {
-        PairMeta m;
-        m.a_row0 = 0;
-        m.b_row0 = L.rt_n * kTile;
-        m.na = na;
-        m.nb = nb;
-        m.nchunk = chunks;
-        m.part_base = 0;
-        m.col_base = 0;
-        m.slot_off = 0;
-        *meta = m;
-        *counts = 0;
+    if (mutual) {
+        unsigned long long *colbest = reinterpret_cast<unsigned long long *>(scratch + L.colbest);
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x)
+            colbest[k] = ~0ull;
     }
-    if (threadIdx.x < 16) ctl[threadIdx.x] = 0;
+    float *tiled = reinterpret_cast<float *>(scratch + L.tiled);
+    const uint32_t t = blockIdx.x >> 2;
+    const int g = (int)(blockIdx.x & 3);
+    if (t < L.rt_n)
+        pack_group(d_a, na, tiled + (size_t)t * kTileFloats, t, g, sm);
+    else
+        pack_group(d_b, nb, tiled + (size_t)t * kTileFloats, t - L.rt_n, g, sm);
 }
 
 // Copies the match list to the caller's buffer (at most cap pairs) and writes
@@ -173,26 +193,22 @@ SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs) {
     L.slots = o, o += align256(sizeof(uint2) * (na ? na : 1));
     L.counts = o, o += align256(sizeof(uint32_t));
     L.ctl = o, o += align256(sizeof(uint32_t) * 16);
-    if (inputs) {  // row-major inputs and the result block [count, pad, pairs]
+    if (inputs) {  // row-major inputs, for callers whose inputs the device cannot read where they lie
         L.raw_a = o, o += align256(sizeof(float) * kDesc * (size_t)(na ? na : 1));
         L.raw_b = o, o += align256(sizeof(float) * kDesc * (size_t)(nb ? nb : 1));
-        L.out = o, o += align256(8 + sizeof(slm_pair) * (size_t)(na ? na : 1));
     }
     L.bytes = o;
     return L;
 }
 
-// The exact FP32 match of one pair (pack -> exact_kernel -> finalize -> copy)
+// The exact FP32 match of one pair (prep -> exact_kernel -> finalize -> copy)
 // over a scratch block laid out by single_layout: no metadata from the host.
 cudaError_t single_exact_enqueue(unsigned char *sc, const SingleLayout &L, const float *d_a, uint32_t na,
                                  const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
                                  uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s) {
     const uint32_t n_items = L.rt_n * L.chunks;
     float *tiled = reinterpret_cast<float *>(sc + L.tiled);
-    single_setup_kernel<<<1, 256, 0, s>>>(sc, L, na, nb);
-    if (mutual) launch_fill_u64(reinterpret_cast<unsigned long long *>(sc + L.colbest), nb, ~0ull, s);
-    launch_pack_fp32(d_a, na, tiled, 0, s);
-    launch_pack_fp32(d_b, nb, tiled, L.rt_n, s);
+    single_prep_kernel<<<4 * (L.rt_n + L.ct_n), 256, 0, s>>>(sc, L, d_a, na, d_b, nb, mutual);
     ExactArgs a{};
     a.tiled = tiled;
     a.items = reinterpret_cast<const Item *>(sc + L.items);

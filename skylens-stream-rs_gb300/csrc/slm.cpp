@@ -584,8 +584,9 @@ struct Workspace {
     cudaStream_t stream = nullptr;
     slm_store store;
     slm_plan plan;
-    DevBuf single;                   // FP32 single-pair calls: inputs, scratch and result block
-    std::vector<unsigned char> single_out;
+    DevBuf single;                   // FP32 single-pair calls: inputs and scratch
+    unsigned char *single_host = nullptr;  // their result block: pinned host memory the kernels write
+    size_t single_host_bytes = 0;
 };
 
 namespace {
@@ -795,6 +796,7 @@ extern "C" slm_status slm_ctx_destroy(slm_ctx *c) {
     cudaDeviceSynchronize();
     for (Workspace *w : c->all) {
         if (w->stream) cudaStreamDestroy(w->stream);
+        if (w->single_host) cudaFreeHost(w->single_host);
         delete w;
     }
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -1299,9 +1301,10 @@ slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float 
 
 namespace {
 
-// An FP32 single-pair call without a store or a plan: the inputs go into the
-// workspace's scratch block, the metadata is made on the device, and the
-// count and pairs come back in one copy (7 kernels, 2 uploads, 1 read-back).
+// An FP32 single-pair call without a store or a plan: the packing reads the
+// inputs where they lie (or from the workspace's scratch block after two
+// uploads), the metadata is made on the device, and the last kernel writes the
+// count and pairs into pinned host memory (4 kernels, no read-back).
 slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t na, const float *b, uint32_t nb,
                             float ratio, int mutual, slm_pair *out, uint32_t cap, uint32_t *n_out, slm_stats *st) {
     const SingleLayout L = single_layout(na, nb, c->sms, true);
@@ -1317,24 +1320,34 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
         src_a = reinterpret_cast<const float *>(sc + L.raw_a);
         src_b = reinterpret_cast<const float *>(sc + L.raw_b);
     }
-    SLM_CU(single_exact_enqueue(sc, L, src_a, na, src_b, nb, ratio, mutual, reinterpret_cast<slm_pair *>(sc + L.out + 8),
-                                na, reinterpret_cast<uint32_t *>(sc + L.out), c->sms, s));
+    // the copy kernel writes the count and the pairs straight into pinned host
+    // memory (no separate read-back); the block grows with na, with slack
     const size_t bytes = 8 + sizeof(slm_pair) * (size_t)na;
-    w->single_out.resize(bytes);
-    SLM_CU(cudaMemcpyAsync(w->single_out.data(), sc + L.out, bytes, cudaMemcpyDeviceToHost, s));
+    if (w->single_host_bytes < bytes) {
+        if (w->single_host) cudaFreeHost(w->single_host);  // the previous call has synchronised
+        w->single_host = nullptr;
+        w->single_host_bytes = 0;
+        const size_t want = bytes + bytes / 4 + 4096;
+        SLM_CU(cudaHostAlloc(reinterpret_cast<void **>(&w->single_host), want, cudaHostAllocMapped));
+        w->single_host_bytes = want;
+    }
+    unsigned char *res = nullptr;
+    SLM_CU(cudaHostGetDevicePointer(reinterpret_cast<void **>(&res), w->single_host, 0));
+    SLM_CU(single_exact_enqueue(sc, L, src_a, na, src_b, nb, ratio, mutual, reinterpret_cast<slm_pair *>(res + 8), na,
+                                reinterpret_cast<uint32_t *>(res), c->sms, s));
     SLM_CU(cudaStreamSynchronize(s));
     uint32_t n = 0;
-    std::memcpy(&n, w->single_out.data(), sizeof(n));
+    std::memcpy(&n, w->single_host, sizeof(n));
     if (n == 0xffffffffu) return fail(SLM_TIMEOUT, "device wait gave up");
     *n_out = n;
     if (st) {
         st->pairs = 1;
         st->distances = (uint64_t)na * nb;
         st->matches = n;
-        st->kernel_launches = mutual ? 7 : 6;
+        st->kernel_launches = 4;
     }
     if (n > cap) return fail(SLM_CAPACITY, "need " + std::to_string(n) + " pairs, have " + std::to_string(cap));
-    if (n) std::memcpy(out, w->single_out.data() + 8, sizeof(slm_pair) * (size_t)n);
+    if (n) std::memcpy(out, w->single_host + 8, sizeof(slm_pair) * (size_t)n);
     return SLM_OK;
 }
 

@@ -120,11 +120,11 @@ void set_last_error(const char *msg);
 // device (byte offsets; `inputs` adds room for the row-major inputs and a
 // result block [count, pad, pairs]).
 struct SingleLayout {
-    size_t tiled, items, parts, meta, colbest, slots, counts, ctl, raw_a, raw_b, out, bytes;
+    size_t tiled, items, parts, meta, colbest, slots, counts, ctl, raw_a, raw_b, bytes;
     uint32_t rt_n, ct_n, chunks;
 };
 SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs);
-// Enqueues setup, packing, exact_kernel, finalize and the copy of at most cap
+// Enqueues the setup and packing, exact_kernel, finalize and the copy of at most cap
 // pairs into d_out with the count (0xffffffff: a device wait gave up) into
 // *d_count. Returns the launch status.
 cudaError_t single_exact_enqueue(unsigned char *scratch, const SingleLayout &L, const float *d_a, uint32_t na,

@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libslm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_exact.cu", "k_compact.cu", "k_shortlist.cu", "k_noalloc.cu"]
 CPP_SOURCES = ["slm.cpp"]
-HEADERS = ["ptx.cuh", "slm_internal.h", "slm_shortlist.h"]
+HEADERS = ["pack.cuh", "ptx.cuh", "slm_internal.h", "slm_shortlist.h"]
 
 
 def _nvcc() -> str:
