@@ -34,15 +34,6 @@ namespace slm {
 
 // ------------------------------------------------------------------ pack
 
-// One CTA per 32-row group of a 128-row tile (grid tiles x 4): row-major
-// rows -> tile[slot][row]. Four CTAs per tile keep four times as many loads in
-// flight as one, which is what sets the time when src is host memory.
-__global__ void __launch_bounds__(256) pack_fp32_kernel(const float *__restrict__ src, uint32_t n,
-                                                        float *__restrict__ tiled, uint32_t tile0) {
-    __shared__ float sm[32][kDesc + 1];
-    pack_group(src, n, tiled + (size_t)(tile0 + blockIdx.x) * kTileFloats, blockIdx.x, blockIdx.y, sm);
-}
-
 // Tile `tile` of the view whose rows start at store row `row0` (n rows): raw
 // rows -> tile[slot][row]. Called by all 256 threads of a CTA alike.
 SLM_DEV void pack_view_tile(const float *__restrict__ raw, float *__restrict__ tiled, uint32_t row0, uint32_t n,
@@ -52,14 +43,16 @@ SLM_DEV void pack_view_tile(const float *__restrict__ raw, float *__restrict__ t
     for (int g = 0; g < 4; ++g) pack_group(src, n, dst, tile, g, sm);
 }
 
-// Many views at once: one CTA per entry of a tile table
-// {first store row of the view, rows of the view, tile within the view, view}.
+// Many views at once: one CTA per 32-row group (blockIdx.y) of each entry of
+// a tile table {first store row of the view, rows of the view, tile within the
+// view, view}.
 __global__ void __launch_bounds__(256) pack_fp32_tiles_kernel(const uint4 *__restrict__ tab,
                                                               const float *__restrict__ raw,
                                                               float *__restrict__ tiled) {
     __shared__ float sm[32][kDesc + 1];
     const uint4 e = tab[blockIdx.x];
-    pack_view_tile(raw, tiled, e.x, e.y, e.z, sm);
+    pack_group(raw + (size_t)e.x * kDesc, e.y, tiled + (size_t)(e.x / kTile + e.z) * kTileFloats, e.z, blockIdx.y,
+               sm);
 }
 
 // The FP32 tiles of both views of every routed pair of a low-precision batch
@@ -88,12 +81,7 @@ void launch_pack_routed(const PairMeta *pairs, const uint32_t *xlist, const uint
 }
 
 void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw, float *tiled, cudaStream_t s) {
-    if (ntiles) pack_fp32_tiles_kernel<<<ntiles, 256, 0, s>>>(tab, raw, tiled);
-}
-
-void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0, cudaStream_t s) {
-    const uint32_t tiles = (n + kTile - 1) / kTile;
-    if (tiles) pack_fp32_kernel<<<dim3(tiles, 4), 256, 0, s>>>(src, n, tiled, tile0);
+    if (ntiles) pack_fp32_tiles_kernel<<<dim3(ntiles, 4), 256, 0, s>>>(tab, raw, tiled);
 }
 
 __global__ void fill_u64_kernel(unsigned long long *p, uint64_t n, unsigned long long v) {

@@ -96,7 +96,6 @@ struct FinalizeArgs {
 
 // Pack n row-major descriptors (src, n x 128) into store tiles starting at
 // tile index `tile0` (rows beyond n within the last tile are zeroed).
-void launch_pack_fp32(const float *src, uint32_t n, float *tiled, uint32_t tile0, cudaStream_t s);
 // The same for many views: tab holds one {row0, n, tile, view} per tile.
 void launch_pack_fp32_tiles(const uint4 *tab, uint32_t ntiles, const float *raw, float *tiled, cudaStream_t s);
 void launch_exact(const ExactArgs &a, int grid, cudaStream_t s);
