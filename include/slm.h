@@ -57,9 +57,9 @@ typedef enum {
 } slm_precision;
 
 /* SLM_PREC_AUTO's switch point, measured on GB300 through slm_ratio_match from
- * host arrays: 3072 x 3072 descriptors FP32 0.21 ms / BF16 0.25 ms,
- * 3584 x 3584 0.25 / 0.26 ms, 4096 x 4096 0.31 / 0.28 ms. */
-#define SLM_AUTO_BF16_DISTANCES 12000000ull
+ * host arrays: 2500 x 2500 descriptors FP32 0.18 ms / BF16 0.19 ms,
+ * 3072 x 3072 0.21 / 0.20 ms, 4096 x 4096 0.31 / 0.22 ms. */
+#define SLM_AUTO_BF16_DISTANCES 8000000ull
 
 typedef struct {
     uint32_t i, j;

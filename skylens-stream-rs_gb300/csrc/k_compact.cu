@@ -149,8 +149,16 @@ void launch_gather_rows(const uint4 *tab, uint32_t n, float *dst, cudaStream_t s
     for (uint32_t b = 0; b < n; b += kScatterMax) {
         const uint32_t m = n - b < kScatterMax ? n - b : kScatterMax;
         ScatterTab t;
-        for (uint32_t k = 0; k < m; ++k) t.e[k] = tab[b + k];
-        gather_rows_kernel<<<dim3(m, 16), 256, 0, s>>>(t, reinterpret_cast<float4 *>(dst));
+        uint32_t rows = 0;
+        for (uint32_t k = 0; k < m; ++k) {
+            t.e[k] = tab[b + k];
+            rows = t.e[k].w > rows ? t.e[k].w : rows;
+        }
+        // CTAs per entry: one per 32 rows of the largest entry (a CTA's four
+        // loads per thread cover 32 rows), between 16 and 64
+        uint32_t per = (rows + 31) / 32;
+        per = per < 16 ? 16 : (per > 64 ? 64 : per);
+        gather_rows_kernel<<<dim3(m, per), 256, 0, s>>>(t, reinterpret_cast<float4 *>(dst));
     }
 }
 

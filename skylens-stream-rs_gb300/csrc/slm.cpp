@@ -671,16 +671,41 @@ slm_status store_append(slm_store *st, const float *desc, uint32_t n, bool devic
     return SLM_OK;
 }
 
-slm_status check_status_word(slm_plan *p) {
-    uint32_t err = 0;
-    SLM_CU(cudaMemcpy(&err, p->d_ctl.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+// Appends `count` views whose rows the device reads where they lie (host
+// memory it can read directly, or device memory) with one gather launch.
+slm_status store_append_direct(slm_store *st, size_t count, const float *const *src, const uint32_t *n, uint32_t *ids,
+                               cudaStream_t s) {
+    uint64_t padded = 0;
+    for (size_t k = 0; k < count; ++k) padded += pad_rows(n[k]);
+    SLM_TRY(store_check_room(st, count, padded));
+    std::vector<uint4> tab;
+    tab.reserve(count);
+    for (size_t k = 0; k < count; ++k) {
+        const uint64_t row0 = store_place(st, n[k], ids ? &ids[k] : nullptr);
+        const uint64_t adr = reinterpret_cast<uint64_t>(src[k]);
+        if (n[k]) tab.push_back(make_uint4((uint32_t)adr, (uint32_t)(adr >> 32), (uint32_t)row0, n[k]));
+    }
+    launch_gather_rows(tab.data(), (uint32_t)tab.size(), st->raw.as<float>(), s);
+    SLM_CU(cudaGetLastError());
+    return SLM_OK;
+}
+
+// The host status for a plan's error word.
+slm_status status_of_word(uint32_t err) {
     if (err == DERR_TIMEOUT_BAR || err == DERR_TIMEOUT_MMA)
         return fail(SLM_TIMEOUT, "device wait gave up (code " + std::to_string(err) + ")");
     if (err) return fail(SLM_INTERNAL, "device invariant failed (code " + std::to_string(err) + ")");
     return SLM_OK;
 }
 
-slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
+slm_status check_status_word(slm_plan *p) {
+    uint32_t err = 0;
+    SLM_CU(cudaMemcpy(&err, p->d_ctl.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return status_of_word(err);
+}
+
+// ctl: a host copy of the plan's 16 control words, or null to read them.
+slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches, const uint32_t *ctl = nullptr) {
     if (!st) return SLM_OK;
     std::memset(st, 0, sizeof(*st));
     st->pairs = p->np;
@@ -689,7 +714,10 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches) {
     st->kernel_launches = p->kernels;
     if (p->prec != SLM_PREC_FP32 && p->launched) {
         uint32_t w[16];
-        SLM_CU(cudaMemcpy(w, p->d_ctl.p, sizeof(w), cudaMemcpyDeviceToHost));
+        if (ctl)
+            std::memcpy(w, ctl, sizeof(w));
+        else
+            SLM_CU(cudaMemcpy(w, p->d_ctl.p, sizeof(w), cudaMemcpyDeviceToHost));
         st->rows_rescored = w[kCtlRescored];
         st->rows_recomputed = (uint64_t)w[kCtlQueueRows] + w[kCtlRoutedRows];
         st->cols_recomputed = (uint64_t)w[kCtlQueueCols] + w[kCtlRoutedCols];
@@ -1272,8 +1300,15 @@ slm_status single_pair_enqueue(slm_ctx *c, Workspace *w, const float *a, uint32_
     const uint64_t rows = pad_rows(na) + pad_rows(nb);
     SLM_TRY(store_reserve(st, std::max<uint64_t>(rows, kTile)));
     slm_store_clear(st);
-    SLM_TRY(store_append(st, a, na, device_src, w->stream, nullptr));
-    SLM_TRY(store_append(st, b, nb, device_src, w->stream, nullptr));
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+    if ((device_src || c->host_direct) && aligned) {  // one gather launch reads both where they lie
+        const float *src[2] = {a, b};
+        const uint32_t n[2] = {na, nb};
+        SLM_TRY(store_append_direct(st, 2, src, n, nullptr, w->stream));
+    } else {
+        SLM_TRY(store_append(st, a, na, false, w->stream, nullptr));
+        SLM_TRY(store_append(st, b, nb, false, w->stream, nullptr));
+    }
     const slm_pair pr{0, 1};
     slm_tune t{};
     t.use_graph = 2;  // one-off shapes: plain launches, no graph
@@ -1301,6 +1336,19 @@ slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float 
 
 namespace {
 
+// The workspace's pinned, mapped host block of at least `bytes` (grown with
+// slack; the previous call on the workspace has synchronised).
+slm_status ws_host_block(Workspace *w, size_t bytes) {
+    if (w->single_host_bytes >= bytes) return SLM_OK;
+    if (w->single_host) cudaFreeHost(w->single_host);
+    w->single_host = nullptr;
+    w->single_host_bytes = 0;
+    const size_t want = bytes + bytes / 4 + 4096;
+    SLM_CU(cudaHostAlloc(reinterpret_cast<void **>(&w->single_host), want, cudaHostAllocMapped));
+    w->single_host_bytes = want;
+    return SLM_OK;
+}
+
 // An FP32 single-pair call without a store or a plan: the packing reads the
 // inputs where they lie (or from the workspace's scratch block after two
 // uploads), the metadata is made on the device, and the last kernel writes the
@@ -1321,16 +1369,8 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
         src_b = reinterpret_cast<const float *>(sc + L.raw_b);
     }
     // the copy kernel writes the count and the pairs straight into pinned host
-    // memory (no separate read-back); the block grows with na, with slack
-    const size_t bytes = 8 + sizeof(slm_pair) * (size_t)na;
-    if (w->single_host_bytes < bytes) {
-        if (w->single_host) cudaFreeHost(w->single_host);  // the previous call has synchronised
-        w->single_host = nullptr;
-        w->single_host_bytes = 0;
-        const size_t want = bytes + bytes / 4 + 4096;
-        SLM_CU(cudaHostAlloc(reinterpret_cast<void **>(&w->single_host), want, cudaHostAllocMapped));
-        w->single_host_bytes = want;
-    }
+    // memory (no separate read-back)
+    SLM_TRY(ws_host_block(w, 8 + sizeof(slm_pair) * (size_t)na));
     unsigned char *res = nullptr;
     SLM_CU(cudaHostGetDevicePointer(reinterpret_cast<void **>(&res), w->single_host, 0));
     SLM_CU(single_exact_enqueue(sc, L, src_a, na, src_b, nb, ratio, mutual, reinterpret_cast<slm_pair *>(res + 8), na,
@@ -1375,15 +1415,25 @@ extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, c
     if (prec == SLM_PREC_FP32) return single_pair_fp32(c, w, a, na, b, nb, ratio, mutual, out, cap, n_out, st);
     SLM_TRY(single_pair_enqueue(c, w, a, na, b, nb, ratio, mutual, prec, false));
     slm_plan *p = &w->plan;
+    // the control words, the offsets and every slot the pairs may fill come
+    // back with the launch into pinned memory: one synchronisation per call
+    const size_t pair_bytes = sizeof(slm_pair) * p->n_slots;
+    SLM_TRY(ws_host_block(w, 80 + pair_bytes));
+    unsigned char *h = w->single_host;
+    SLM_CU(cudaMemcpyAsync(h, p->d_ctl.p, 64, cudaMemcpyDeviceToHost, w->stream));
+    SLM_CU(cudaMemcpyAsync(h + 64, p->d_offsets.p, 16, cudaMemcpyDeviceToHost, w->stream));
+    if (pair_bytes) SLM_CU(cudaMemcpyAsync(h + 80, p->d_dense.p, pair_bytes, cudaMemcpyDeviceToHost, w->stream));
     SLM_CU(cudaStreamSynchronize(w->stream));
-    SLM_TRY(check_status_word(p));
-    uint64_t off[2] = {0, 0};
-    SLM_CU(cudaMemcpy(off, p->d_offsets.p, sizeof(off), cudaMemcpyDeviceToHost));
+    uint32_t ctl[16];
+    std::memcpy(ctl, h, sizeof(ctl));
+    SLM_TRY(status_of_word(ctl[1]));
+    uint64_t off[2];
+    std::memcpy(off, h + 64, sizeof(off));
     const uint64_t total = off[1];
     *n_out = (uint32_t)total;
-    SLM_TRY(fill_stats(p, st, total));
+    SLM_TRY(fill_stats(p, st, total, ctl));
     if (total > cap) return fail(SLM_CAPACITY, "need " + std::to_string(total) + " pairs, have " + std::to_string(cap));
-    if (total) SLM_CU(cudaMemcpy(out, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost));
+    if (total) std::memcpy(out, h + 80, sizeof(slm_pair) * total);
     return SLM_OK;
 }
 
@@ -1990,19 +2040,14 @@ slm_status coal_issue(Coalescer *co, CoalSlot *s, std::vector<CoalReq *> &take) 
     for (CoalReq *r : take) direct &= ((reinterpret_cast<uintptr_t>(r->a) | reinterpret_cast<uintptr_t>(r->b)) & 15) == 0;
     if (direct) {
         // one kernel reads every caller's arrays where they lie (no copies by this thread)
-        std::vector<uint4> tab;
-        tab.reserve(2 * take.size());
-        auto add = [&](const float *src, uint32_t n, uint32_t *id) {
-            const uint64_t row0 = store_place(st, n, id);
-            const uint64_t adr = reinterpret_cast<uint64_t>(src);
-            if (n) tab.push_back(make_uint4((uint32_t)adr, (uint32_t)(adr >> 32), (uint32_t)row0, n));
-        };
+        std::vector<const float *> src(2 * take.size());
+        std::vector<uint32_t> n(2 * take.size()), ids(2 * take.size());
         for (size_t k = 0; k < take.size(); ++k) {
-            add(take[k]->a, take[k]->na, &pr[k].i);
-            add(take[k]->b, take[k]->nb, &pr[k].j);
+            src[2 * k] = take[k]->a, n[2 * k] = take[k]->na;
+            src[2 * k + 1] = take[k]->b, n[2 * k + 1] = take[k]->nb;
         }
-        launch_gather_rows(tab.data(), (uint32_t)tab.size(), st->raw.as<float>(), w->stream);
-        SLM_CU(cudaGetLastError());
+        SLM_TRY(store_append_direct(st, src.size(), src.data(), n.data(), ids.data(), w->stream));
+        for (size_t k = 0; k < take.size(); ++k) pr[k] = slm_pair{ids[2 * k], ids[2 * k + 1]};
     } else {
         for (size_t k = 0; k < take.size(); ++k) {
             SLM_TRY(store_append(st, take[k]->a, take[k]->na, false, w->stream, &pr[k].i));

@@ -19,7 +19,7 @@ pub const SLM_PREC_BF16: SlmPrecision = 1;
 pub const SLM_PREC_FP8: SlmPrecision = 2;
 /// BF16 from SLM_AUTO_BF16_DISTANCES distances (one call or batch), FP32 below.
 pub const SLM_PREC_AUTO: SlmPrecision = 3;
-pub const SLM_AUTO_BF16_DISTANCES: u64 = 12_000_000;
+pub const SLM_AUTO_BF16_DISTANCES: u64 = 8_000_000;
 
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default, PartialEq, Eq)]

@@ -15,7 +15,7 @@ P = ctypes.POINTER
 c_u32, c_u64, c_f32, c_int = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_int
 
 SLM_OK, SLM_INVALID_ARG, SLM_CAPACITY, SLM_OOM, SLM_CUDA_ERROR, SLM_TIMEOUT, SLM_NO_DEVICE, SLM_INTERNAL = range(8)
-PRECISIONS = {"fp32": 0, "bf16": 1, "fp8": 2, "auto": 3}  # auto: BF16 from 12M distances per call or batch
+PRECISIONS = {"fp32": 0, "bf16": 1, "fp8": 2, "auto": 3}  # auto: BF16 from 8M distances per call or batch
 
 
 class SlmPair(ctypes.Structure):

@@ -239,7 +239,8 @@ def test_autotuned_plan(matcher, prec):
 
 def test_auto_precision(matcher):
     """SLM_PREC_AUTO: the plain FP32 kernel below SLM_AUTO_BF16_DISTANCES, the
-    BF16 shortlist from there up (5 and 15 kernels per launch); exact both ways."""
+    BF16 shortlist from there up (4 kernels per call, and more than 10);
+    exact both ways."""
     for n, path in ((800, "fp32"), (3500, "bf16")):
         a, b = synth.pair_large(n, 0.5, 0.05, seed=n)
         got = matcher.ratio_match_np(a, b, 0.8, True, "auto")
