@@ -153,20 +153,25 @@ def test_batch_with_repeated_and_reversed_pairs(matcher, prec):
 
 
 def test_device_entry_point(matcher, prec):
+    """Device arrays: 16-byte aligned ones are gathered where they lie, the
+    others (here 4 or 8 bytes past an aligned address) copied first."""
     torch = pytest.importorskip("torch")
     a, b = synth.pair_800(1)
-    da = torch.from_numpy(a).cuda()
-    db = torch.from_numpy(b).cuda()
-    out = torch.zeros((800, 2), dtype=torch.int32, device="cuda")
-    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
-    torch.cuda.synchronize()  # inputs are ready before the library stream reads them
-    matcher.ratio_match_device(da.data_ptr(), 800, db.data_ptr(), 800, 0.8, True, prec, out.data_ptr(), 800,
-                               cnt.data_ptr())
-    torch.cuda.ExternalStream(matcher.stream).synchronize()
-    n = int(cnt.item())
     ref = O.ratio_match_np(a, b, 0.8, True, threads=4)
-    assert n == len(ref)
-    assert np.array_equal(out[:n].cpu().numpy().astype(np.uint32), ref)
+    for shift in (0, 1, 2):
+        da = torch.zeros(a.size + 4, dtype=torch.float32, device="cuda")
+        db = torch.zeros(b.size + 4, dtype=torch.float32, device="cuda")
+        da[shift:shift + a.size] = torch.from_numpy(a.reshape(-1)).cuda()
+        db[shift:shift + b.size] = torch.from_numpy(b.reshape(-1)).cuda()
+        out = torch.zeros((800, 2), dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()  # inputs are ready before the library stream reads them
+        matcher.ratio_match_device(da.data_ptr() + 4 * shift, 800, db.data_ptr() + 4 * shift, 800, 0.8, True, prec,
+                                   out.data_ptr(), 800, cnt.data_ptr())
+        torch.cuda.ExternalStream(matcher.stream).synchronize()
+        n = int(cnt.item())
+        assert n == len(ref), shift
+        assert np.array_equal(out[:n].cpu().numpy().astype(np.uint32), ref), shift
 
 
 def plan_rm(matcher, prec, variant):
@@ -296,10 +301,10 @@ def test_random_batches(matcher, prec, seed):
     st.close()
 
 
-def test_single_call_input_alignment(matcher):
-    """Single FP32 calls read 16-byte-aligned host inputs where they lie (when
-    the device can read pageable memory) and copy the others first; both give
-    the reference's lists."""
+def test_single_call_input_alignment(matcher, prec):
+    """Single calls read 16-byte-aligned host inputs where they lie (when the
+    device can read pageable memory) and copy the others first; both give the
+    reference's lists."""
     a, b = synth.pair_800(3)
     want = O.ratio_match_np(a, b, 0.8, True, threads=8)
     for shift_a, shift_b in ((0, 0), (1, 0), (0, 3), (2, 2)):
@@ -309,4 +314,4 @@ def test_single_call_input_alignment(matcher):
         ub = bb[shift_b:shift_b + b.size].reshape(b.shape)
         ua[...] = a
         ub[...] = b
-        assert np.array_equal(matcher.ratio_match_np(ua, ub, 0.8, True, "fp32"), want), (shift_a, shift_b)
+        assert np.array_equal(matcher.ratio_match_np(ua, ub, 0.8, True, prec), want), (shift_a, shift_b)
