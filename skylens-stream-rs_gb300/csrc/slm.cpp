@@ -6,6 +6,7 @@
 // points (the ratio_match drop-in) run through a pool of workspaces so that
 // concurrent host threads (rayon workers in the reference) never share one.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -113,6 +114,15 @@ struct slm_ctx {
         cudaFree(p);
         used.fetch_sub(bytes);
     }
+};
+
+// A named range on the calling thread for profilers that read NVTX (nsys,
+// ncu's range filters); without such a tool attached the calls return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
 // Device buffer owned by a context, grown on demand.
@@ -883,6 +893,7 @@ extern "C" slm_status slm_store_destroy(slm_store *st) {
 }
 
 extern "C" slm_status slm_store_add_view(slm_store *st, const float *desc, uint32_t n, uint32_t *view_id) {
+    NvtxRange range_("slm_store_add_view");
     if (!st || (!desc && n)) return fail(SLM_INVALID_ARG, "NULL argument");
     SLM_TRY(ctx_check_device(st->ctx));
     return store_append(st, desc, n, false, st->ctx->stream, view_id);
@@ -894,6 +905,7 @@ extern "C" slm_status slm_store_add_view(slm_store *st, const float *desc, uint3
 // its own call overhead). All views are checked for room before any is added.
 extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets,
                                           const uint32_t *counts, uint32_t nviews, uint32_t *ids) {
+    NvtxRange range_("slm_store_add_views");
     if (!st || (!desc && nviews) || (nviews && (!offsets || !counts))) return fail(SLM_INVALID_ARG, "NULL argument");
     SLM_TRY(ctx_check_device(st->ctx));
     uint64_t lo = ~0ull, hi = 0, padded = 0;
@@ -1082,6 +1094,7 @@ uint64_t tune_key(const slm_store *st, const slm_pair *pairs, uint32_t np, int m
 
 extern "C" slm_status slm_autotune(slm_ctx *c, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                                    int mutual, slm_precision prec, slm_tune *best, float *best_ms) {
+    NvtxRange range_("slm_autotune");
     if (!c || !st || (np && !pairs)) return fail(SLM_INVALID_ARG, "NULL argument");
     if (!prec_valid(prec)) return fail(SLM_INVALID_ARG, "unknown precision");
     SLM_TRY(validate_ratio(ratio));
@@ -1182,12 +1195,14 @@ extern "C" slm_status slm_plan_destroy(slm_plan *p) {
 }
 
 extern "C" slm_status slm_plan_launch(slm_plan *p) {
+    NvtxRange range_("slm_plan_launch");
     if (!p) return fail(SLM_INVALID_ARG, "NULL plan");
     SLM_TRY(ctx_check_device(p->ctx));
     return plan_launch_on(p, p->stream, p->tune.use_graph != 2);
 }
 
 extern "C" slm_status slm_plan_results(slm_plan *p, slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *st) {
+    NvtxRange range_("slm_plan_results");
     if (!p || !offsets || (cap && !out)) return fail(SLM_INVALID_ARG, "NULL argument");
     if (!p->launched) return fail(SLM_INVALID_ARG, "plan was not launched");
     SLM_TRY(ctx_check_device(p->ctx));
@@ -1244,6 +1259,7 @@ extern "C" slm_status slm_match_pairs(slm_ctx *c, slm_store *st, const uint64_t 
                                       uint32_t min_matches, slm_pair *pairs_out, uint64_t pairs_cap,
                                       uint64_t *n_pairs, slm_pair *out, uint64_t cap, uint64_t *offsets,
                                       slm_stats *stats) {
+    NvtxRange range_("slm_match_pairs");
     if (!c || !st || (nv && !views) || !n_pairs || (pairs_cap && (!pairs_out || !offsets)))
         return fail(SLM_INVALID_ARG, "NULL argument");
     if (nv > st->row0.size())
@@ -1396,6 +1412,7 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
 extern "C" slm_status slm_ratio_match(slm_ctx *c, const float *a, uint32_t na, const float *b, uint32_t nb,
                                       float ratio, int mutual, slm_precision prec, slm_pair *out, uint32_t cap,
                                       uint32_t *n_out, slm_stats *st) {
+    NvtxRange range_("slm_ratio_match");
     SLM_TRY(check_pair_args(c, a, na, b, nb, ratio, prec));
     const bool coalesce = prec == SLM_PREC_AUTO && c->coal;
     prec = resolve_prec(prec, (uint64_t)na * nb);
@@ -1445,6 +1462,7 @@ void launch_copy_pairs(const uint2 *src, const uint64_t *total, slm_pair *dst, u
 extern "C" slm_status slm_ratio_match_device(slm_ctx *c, const float *d_a, uint32_t na, const float *d_b, uint32_t nb,
                                              float ratio, int mutual, slm_precision prec, slm_pair *d_out,
                                              uint32_t cap, uint32_t *d_count) {
+    NvtxRange range_("slm_ratio_match_device");
     SLM_TRY(check_pair_args(c, d_a, na, d_b, nb, ratio, prec));
     prec = resolve_prec(prec, (uint64_t)na * nb);
     if (!d_count || (cap && !d_out)) return fail(SLM_INVALID_ARG, "NULL output");

@@ -80,5 +80,44 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+SAN_LIB = os.path.join(OUT, "asan", "libslm.so")
+
+
+def build_sanitized(verbose: bool = False) -> str:
+    """libslm with its host C++ (the context, stores, plans, autotuner, serving
+    and coalescing threads) under AddressSanitizer and UBSan, the CUDA
+    translation units as in build(). Load it through SLM_LIB_PATH with the
+    sanitizer runtimes preloaded, e.g.
+
+        LD_PRELOAD=$(gcc -print-file-name=libasan.so):$(gcc -print-file-name=libubsan.so) \\
+        ASAN_OPTIONS=detect_leaks=0:protect_shadow_gap=0 SLM_LIB_PATH=<this path> \\
+        python -m pytest tests -m gpu
+
+    (leak detection off: the Python interpreter itself is not instrumented;
+    protect_shadow_gap=0: the CUDA driver maps memory where ASan would
+    otherwise reserve its shadow gap)."""
+    build(verbose=verbose)  # the CUDA objects
+    d = os.path.dirname(SAN_LIB)
+    os.makedirs(d, exist_ok=True)
+    cuda = os.path.dirname(os.path.dirname(_nvcc()))
+    obj = os.path.join(d, "slm.cpp.o")
+    cmds = [["g++", "-std=c++17", "-O1", "-g", "-fPIC", "-fno-omit-frame-pointer", "-fsanitize=address,undefined",
+             "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(cuda, "include"), "-c",
+             os.path.join(CSRC, "slm.cpp"), "-o", obj],
+            ["g++", "-shared", "-fsanitize=address,undefined", "-o", SAN_LIB, obj,
+             *[os.path.join(OUT, s + ".o") for s in CU_SOURCES],
+             "-L", os.path.join(cuda, "lib64"), "-lcudart_static", "-ldl", "-lpthread", "-lrt"]]
+    for cmd in cmds:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError(f"sanitized libslm build failed: {' '.join(cmd)}\n{r.stderr}")
+    return SAN_LIB
+
+
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--sanitize" in sys.argv:
+        print(build_sanitized(verbose="-v" in sys.argv))
+    else:
+        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
