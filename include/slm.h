@@ -45,7 +45,8 @@ typedef enum {
     SLM_CUDA_ERROR = 4,  /* a CUDA runtime call failed (see slm_last_error) */
     SLM_TIMEOUT = 5,     /* a bounded device-side wait gave up */
     SLM_NO_DEVICE = 6,   /* no CUDA device / device is not sm_103 */
-    SLM_INTERNAL = 7     /* invariant violated inside the library */
+    SLM_INTERNAL = 7,    /* invariant violated inside the library */
+    SLM_CANCELLED = 8    /* a serving request withdrawn by slm_server_cancel */
 } slm_status;
 
 typedef enum {
@@ -323,6 +324,13 @@ slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, con
 slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t timeout_ms, slm_pair *out, uint64_t cap,
                            uint64_t *offsets, double *latency_ms);
 slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st);
+/* Withdraw a submitted request's matching. Not yet admitted: its pairs are
+ * dropped (its view is still added to the store, so later submissions may
+ * name it). Admitted (its batch on the GPU): the batch runs to completion and
+ * the request's results are discarded. Already finished: its results are
+ * discarded. slm_server_wait then returns SLM_CANCELLED for the ticket and
+ * releases it; other requests are unaffected. */
+slm_status slm_server_cancel(slm_server *srv, uint64_t ticket);
 
 #ifdef __cplusplus
 }

@@ -163,6 +163,7 @@ extern "C" const char *slm_status_str(slm_status s) {
         case SLM_TIMEOUT: return "SLM_TIMEOUT";
         case SLM_NO_DEVICE: return "SLM_NO_DEVICE";
         case SLM_INTERNAL: return "SLM_INTERNAL";
+        case SLM_CANCELLED: return "SLM_CANCELLED";
     }
     return "SLM_UNKNOWN";
 }
@@ -1615,6 +1616,7 @@ struct ServeRequest {
     std::vector<uint64_t> offsets;   // np + 1
     Clock::time_point t_submit, t_done;
     bool uploaded = false, done = false;
+    bool cancelled = false;          // slm_server_cancel: results are not kept
     slm_status status = SLM_OK;
     std::string error;
 };
@@ -1707,8 +1709,9 @@ void serve_loop(slm_server *srv) {
             const slm_status rs = slm_plan_results(&s->plan, out.data(), out.size(), off.data(), &st);
             uint32_t k = 0;
             for (ServeRequest *r : s->reqs) {
-                if (rs != SLM_OK) {
-                    serve_fail_request(r, rs);
+                if (rs != SLM_OK || r->cancelled) {
+                    if (r->cancelled) g_last_error = "request cancelled";
+                    serve_fail_request(r, r->cancelled ? SLM_CANCELLED : rs);
                     k += (uint32_t)r->pairs.size();
                     continue;
                 }
@@ -1746,6 +1749,13 @@ void serve_loop(slm_server *srv) {
                     }
                     r->uploaded = true;
                     std::vector<float>().swap(r->desc);
+                }
+                if (r->cancelled) {  // its view stays in the store; its pairs are dropped
+                    srv->pending.pop_front();
+                    g_last_error = "request cancelled";
+                    serve_fail_request(r, SLM_CANCELLED);
+                    srv->cv_done.notify_all();
+                    continue;
                 }
                 std::vector<slm_pair> trial = pairs;
                 trial.insert(trial.end(), r->pairs.begin(), r->pairs.end());
@@ -1926,6 +1936,23 @@ extern "C" slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
     srv->reqs.erase(it);
     delete r;
+    return SLM_OK;
+}
+
+extern "C" slm_status slm_server_cancel(slm_server *srv, uint64_t ticket) {
+    if (!srv) return fail(SLM_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return fail(SLM_INVALID_ARG, "unknown ticket");
+    ServeRequest *r = it->second;
+    r->cancelled = true;
+    if (r->done && r->status == SLM_OK) {  // finished: drop the results
+        r->status = SLM_CANCELLED;
+        r->error = "request cancelled";
+        std::vector<slm_pair>().swap(r->matches);
+        std::vector<uint64_t>().swap(r->offsets);
+    }
+    srv->cv_work.notify_all();
     return SLM_OK;
 }
 

@@ -12,6 +12,7 @@ pub const SLM_CUDA_ERROR: SlmStatus = 4;
 pub const SLM_TIMEOUT: SlmStatus = 5;
 pub const SLM_NO_DEVICE: SlmStatus = 6;
 pub const SLM_INTERNAL: SlmStatus = 7;
+pub const SLM_CANCELLED: SlmStatus = 8;
 
 pub type SlmPrecision = c_int;
 pub const SLM_PREC_FP32: SlmPrecision = 0;

@@ -14,7 +14,8 @@ from . import buildlib as _build
 P = ctypes.POINTER
 c_u32, c_u64, c_f32, c_int = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_int
 
-SLM_OK, SLM_INVALID_ARG, SLM_CAPACITY, SLM_OOM, SLM_CUDA_ERROR, SLM_TIMEOUT, SLM_NO_DEVICE, SLM_INTERNAL = range(8)
+(SLM_OK, SLM_INVALID_ARG, SLM_CAPACITY, SLM_OOM, SLM_CUDA_ERROR, SLM_TIMEOUT, SLM_NO_DEVICE, SLM_INTERNAL,
+ SLM_CANCELLED) = range(9)
 PRECISIONS = {"fp32": 0, "bf16": 1, "fp8": 2, "auto": 3}  # auto: BF16 from 8M distances per call or batch
 
 
@@ -70,7 +71,7 @@ class SlmError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str):
         self.status = status
         names = ["SLM_OK", "SLM_INVALID_ARG", "SLM_CAPACITY", "SLM_OOM", "SLM_CUDA_ERROR", "SLM_TIMEOUT",
-                 "SLM_NO_DEVICE", "SLM_INTERNAL"]
+                 "SLM_NO_DEVICE", "SLM_INTERNAL", "SLM_CANCELLED"]
         name = names[status] if 0 <= status < len(names) else str(status)
         super().__init__(f"{where}: {name}: {detail}")
 
@@ -117,6 +118,7 @@ SIGNATURES = {
     "slm_server_wait": (c_int, [ctypes.c_void_p, c_u64, c_u32, P(SlmPair), c_u64, P(c_u64),
                                 P(ctypes.c_double)]),
     "slm_server_stats_get": (c_int, [ctypes.c_void_p, P(SlmServerStats)]),
+    "slm_server_cancel": (c_int, [ctypes.c_void_p, c_u64]),
     "slm_autotune": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int, P(SlmTune),
                              P(c_f32)]),
     "slm_match_batch": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(SlmPair), c_u32, c_f32, c_int, c_int,

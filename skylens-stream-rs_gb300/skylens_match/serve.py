@@ -61,6 +61,11 @@ class Server:
         flat = np.frombuffer(out, dtype=np.uint32, count=2 * int(off[-1])).reshape(-1, 2)
         return [flat[int(off[k]):int(off[k + 1])].copy() for k in range(np_)], lat.value
 
+    def cancel(self, ticket: int) -> None:
+        """slm_server_cancel: the request's pairs are dropped (or its results
+        discarded); wait() on the ticket then raises SlmError(SLM_CANCELLED)."""
+        check(self._L.slm_server_cancel(self._h, ticket), "slm_server_cancel")
+
     def stats(self) -> dict:
         s = SlmServerStats()
         check(self._L.slm_server_stats_get(self._h, ctypes.byref(s)), "slm_server_stats_get")

@@ -61,3 +61,34 @@ def test_serving_within_a_small_hbm_budget():
     for (v, pairs), rv in zip(reqs, res):
         for (u, _), m_k in zip(pairs, rv):
             assert np.array_equal(m_k, O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=8)), (u, v)
+
+
+def test_cancelled_requests_and_the_rest():
+    """slm_server_cancel on every third request of a burst (some still queued,
+    some already on the GPU): those tickets report SLM_CANCELLED; every other
+    request, including those that match against a cancelled request's view,
+    still gets the oracle's lists."""
+    from skylens_match import _lib
+    z = synth.zone(positions=7, n_range=(150, 900), seed=23)
+    reqs = serve.zone_requests(z)
+    total = int(z.counts.sum())
+    srv = serve.Server(total, len(z.counts), "bf16", slots=2, max_batch_pairs=6)
+    tickets = [srv.submit(z.view(v), pairs)[1] for v, pairs in reqs]
+    cancelled = set(range(0, len(tickets), 3))
+    for k in sorted(cancelled):
+        srv.cancel(tickets[k])
+    with pytest.raises(_lib.SlmError):
+        srv.cancel(10 ** 9)  # unknown ticket
+    for k, ((v, pairs), t) in enumerate(zip(reqs, tickets)):
+        if k in cancelled:
+            with pytest.raises(_lib.SlmError) as e:
+                srv.wait(t, cap=int(z.counts[v]) * max(1, len(pairs)))
+            assert e.value.status == _lib.SLM_CANCELLED
+            continue
+        res, _ = srv.wait(t, cap=int(z.counts[v]) * max(1, len(pairs)))
+        for (u, _), m_k in zip(pairs, res):
+            assert np.array_equal(m_k, O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=8)), (u, v)
+    st = srv.stats()
+    srv.close()
+    print("cancel:", st)
+    assert st["submitted"] == len(reqs)
