@@ -61,3 +61,22 @@ def test_one_batch(matcher, cases, prec):
         assert np.array_equal(got[k], want[True]), (len(a), len(b), prec)
     plan.close()
     st.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_repeated_launches_give_identical_bytes(matcher, cases, prec):
+    """Candidate slots and column counters are filled by atomics in whatever
+    order the CTAs run; the compacted lists must not depend on it: five
+    launches of one plan (rows split over many work items among its pairs)
+    return the same bytes."""
+    st = matcher.store(sum(len(a) + len(b) for a, b, _ in cases), 2 * len(cases))
+    pairs = [(st.add_view(a), st.add_view(b)) for a, b, _ in cases]
+    plan = st.plan(pairs, 0.8, True, prec)
+    plan.launch()
+    first = plan.results()
+    for _ in range(4):
+        plan.launch()
+        again = plan.results()
+        assert np.array_equal(again[0], first[0]) and np.array_equal(again[1], first[1])
+    plan.close()
+    st.close()
