@@ -1354,10 +1354,14 @@ slm_status check_pair_args(slm_ctx *c, const float *a, uint32_t na, const float 
 namespace {
 
 // The workspace's pinned, mapped host block of at least `bytes` (grown with
-// slack; the previous call on the workspace has synchronised).
+// slack). The old block is freed only once the workspace's stream is idle: a
+// call that failed after enqueuing work may have left a copy into it pending.
 slm_status ws_host_block(Workspace *w, size_t bytes) {
     if (w->single_host_bytes >= bytes) return SLM_OK;
-    if (w->single_host) cudaFreeHost(w->single_host);
+    if (w->single_host) {
+        cudaStreamSynchronize(w->stream);
+        cudaFreeHost(w->single_host);
+    }
     w->single_host = nullptr;
     w->single_host_bytes = 0;
     const size_t want = bytes + bytes / 4 + 4096;
