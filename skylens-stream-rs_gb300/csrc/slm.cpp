@@ -2114,7 +2114,10 @@ slm_status coal_issue(Coalescer *co, CoalSlot *s, std::vector<CoalReq *> &take) 
     const size_t off_bytes = sizeof(uint64_t) * (p->np + 1), pair_bytes = sizeof(slm_pair) * p->n_slots;
     const size_t need = 8 + off_bytes + pair_bytes;
     if (need > s->host_bytes) {
-        if (s->host) cudaFreeHost(s->host);
+        if (s->host) {
+            cudaStreamSynchronize(w->stream);  // a failed earlier batch may have left copies pending
+            cudaFreeHost(s->host);
+        }
         s->host = nullptr;
         s->host_bytes = 0;
         SLM_CU(cudaHostAlloc(&s->host, need + need / 4, cudaHostAllocDefault));
