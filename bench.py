@@ -429,13 +429,17 @@ def main():
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
     ms = float(np.mean(step_ms))
-    ms, _, value = reduce_over_ranks(ms, len(z.pairs), dist, device="cuda" if dist else None)
+    rdev = "cuda" if dist else None
+    ms_local = ms
+    ms, _, value = reduce_over_ranks(ms, len(z.pairs), dist, device=rdev)
+    # distances over all ranks (each rank's zone has its own seed) per job time
+    _, _, dist_rate = reduce_over_ranks(ms_local, z.distances, dist, device=rdev)
 
     fp32 = None
     if plan_fp32 is not plan:
         f_ms, f_kern = timed(plan_fp32, max(1, args.fp32_steps), 1)
-        fms = float(np.mean(f_ms))
-        fp32 = {"value": len(z.pairs) / (fms / 1e3), "unit": "image pairs/s", "ms_per_step": fms,
+        fms, _, fval = reduce_over_ranks(float(np.mean(f_ms)), len(z.pairs), dist, device=rdev)
+        fp32 = {"value": fval, "unit": "image pairs/s", "ms_per_step": fms,
                 "kernel_ms": float(np.mean([k[0] for k in f_kern]))}
 
     # ---- the run pipeline's own pair set (pipeline.rs:485-496): scheduled_pairs with
@@ -511,12 +515,14 @@ def main():
             total = read(k - 1)
         total = read(args.steps - 1)
         e2e_s = (time.perf_counter() - t0) / args.steps
+        # job time = the slowest rank's, work = every rank's pairs
+        e2e_ms, _, e2e_value = reduce_over_ranks(1e3 * e2e_s, len(z.pairs), dist, device=rdev)
         out_bytes = total * 8 + lanes[0][3].nbytes
         for st_, pl_, _, _ in lanes[1:]:
             pl_.close()
             st_.close()
         m2.close()
-        e2e = {"value": ws * len(z.pairs) / e2e_s, "unit": "image pairs/s", "ms_per_step": 1e3 * e2e_s,
+        e2e = {"value": e2e_value, "unit": "image pairs/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(z.desc.nbytes), "d2h_bytes_per_step": int(out_bytes),
                "pipeline": "2 contexts: a batch's upload overlaps the previous batch's kernels"}
 
@@ -581,7 +587,7 @@ def main():
                        "distances": dist_n, "descriptors": n_rows, "ratio": 0.8, "mutual": True,
                        "l2": "flushed between steps (512 MiB write, outside the events)",
                        "parallelism": f"replicas{ws}"},
-            "distances_per_s": ws * dist_n / (ms / 1e3),
+            "distances_per_s": dist_rate,
             "bit_exact": {"ok": bit_exact, "pairs_checked": int(nverify), "mismatched_pairs": int(mism)},
             "fp32_plain": fp32, "scheduled": sched,
             "kernel_ms": kms, "stats": stats_main,
