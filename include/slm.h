@@ -320,7 +320,8 @@ slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, con
 /* Wait up to timeout_ms (0: poll) for a ticket. SLM_TIMEOUT if not done yet.
  * On completion copies pair k's matches to out[offsets[k] .. offsets[k+1])
  * (offsets has np+1 entries) and the request's latency (submit -> results on
- * the host) to *latency_ms; the ticket is then released. */
+ * the host) to *latency_ms; the ticket is then released. At most one thread
+ * waits on a given ticket at a time. */
 slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t timeout_ms, slm_pair *out, uint64_t cap,
                            uint64_t *offsets, double *latency_ms);
 slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st);
