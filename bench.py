@@ -15,9 +15,9 @@ one planned batch replayed from a CUDA graph.
          steps outside the events.
   e2e    the same through the C ABI with host buffers: every step re-uploads
          all views from pinned host memory (slm_store_add_views), runs the
-         batch and reads the match lists back (slm_plan_results); two
+         batch and reads the match lists back (slm_plan_results); three
          contexts take the steps in turn, so one step's copies overlap the
-         previous step's kernels.
+         kernels of the two steps before it.
 The match lists of the main arm are checked against the oracle (bit-exact) on
 a sample of pairs before timing. `--impl reference` times the CPU restatement
 of the reference (oracle/, all host threads) on a bounded sample.
@@ -472,59 +472,70 @@ def main():
     e2e = None
     out_bytes = 0
     if not args.no_e2e:
-        # Two contexts (two library streams), each with its own store and plan,
-        # take the batches in turn: batch k's upload and launch are issued before
-        # batch k-1's match lists are read back, so the copies of one batch
-        # overlap the kernels of the other. Every step still uploads all views
-        # from pinned host memory and reads its match lists back into pinned
-        # host buffers (slm_plan_results).
-        m2 = sm.Matcher(device=dev)
-        store2 = m2.store(n_rows, len(z.counts))
-        store2.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
+        # Three contexts (three library streams), each with its own store and
+        # plan, take the batches in turn: batch k's upload and launch are issued
+        # before batch k-2's match lists are read back, so the copies of one
+        # batch overlap the kernels of the two before it. Every step still
+        # uploads all views from pinned host memory (one copy per view, copy
+        # engines only) and reads its match lists back into pinned host buffers
+        # (slm_plan_results).
+        NL = 3
         tp = tuned[prec]
-        plan2 = store2.plan(z.pairs, 0.8, True, prec, items_per_sm=tp["items_per_sm"], shortlist_k=tp["shortlist_k"],
-                            use_graph=1, variant=tp["variant"], row_tiles=tp["row_tiles"])
+        extra = []
         lanes = []
-        for st_, pl_ in ((store, plan), (store2, plan2)):
+        for q in range(NL):
+            if q == 0:
+                st_, pl_ = store, plan
+            else:
+                mq = sm.Matcher(device=dev)
+                st_ = mq.store(n_rows, len(z.counts))
+                st_.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
+                pl_ = st_.plan(z.pairs, 0.8, True, prec, items_per_sm=tp["items_per_sm"],
+                               shortlist_k=tp["shortlist_k"], use_graph=1, variant=tp["variant"],
+                               row_tiles=tp["row_tiles"])
+                extra.append((mq, st_, pl_))
             lanes.append((st_, pl_,
                           torch.empty((max(pl_.total_rows, 1), 2), dtype=torch.int32).pin_memory().numpy().view(np.uint32),
                           torch.empty(len(z.pairs) + 1, dtype=torch.int64).pin_memory().numpy().view(np.uint64)))
 
         def issue(k):
-            st_, pl_ = lanes[k % 2][:2]
+            st_, pl_ = lanes[k % NL][:2]
             st_.clear()
             st_.add_views_ptr(pinned.data_ptr(), z.offsets, z.counts)
             pl_.launch()
 
         def read(k):
-            _, pl_, o_, f_ = lanes[k % 2]
+            _, pl_, o_, f_ = lanes[k % NL]
             return pl_.results_into(o_, f_)
 
-        for k in range(4):  # warm-up: both lanes, graphs captured
-            issue(k)
-            if k:
-                read(k - 1)
-        total = read(3)
+        def run(first, n):
+            """Steps first .. first+n-1, at most NL-1 in flight; returns the last total."""
+            tot = 0
+            for k in range(first, first + n):
+                issue(k)
+                if k - first >= NL - 1:
+                    tot = read(k - NL + 1)
+            for k in range(max(first, first + n - NL + 1), first + n):
+                tot = read(k)
+            return tot
+
+        run(0, 2 * NL)  # warm-up: every lane, graphs captured
         ref_pr, ref_of = plan.results()
         for _, _, o_, f_ in lanes:
             assert int(f_[-1]) == int(ref_of[-1]) and np.array_equal(o_[:int(f_[-1])], ref_pr)
         t0 = time.perf_counter()
-        issue(0)
-        for k in range(1, args.steps):
-            issue(k)
-            total = read(k - 1)
-        total = read(args.steps - 1)
+        total = run(0, args.steps)
         e2e_s = (time.perf_counter() - t0) / args.steps
         # job time = the slowest rank's, work = every rank's pairs
         e2e_ms, _, e2e_value = reduce_over_ranks(1e3 * e2e_s, len(z.pairs), dist, device=rdev)
         out_bytes = total * 8 + lanes[0][3].nbytes
-        for st_, pl_, _, _ in lanes[1:]:
+        for mq, st_, pl_ in extra:
             pl_.close()
             st_.close()
-        m2.close()
+            mq.close()
         e2e = {"value": e2e_value, "unit": "image pairs/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(z.desc.nbytes), "d2h_bytes_per_step": int(out_bytes),
-               "pipeline": "2 contexts: a batch's upload overlaps the previous batch's kernels"}
+               "pipeline": f"{NL} contexts: a batch's upload overlaps the kernels of the {NL - 1} before it"}
 
     # ---- roofline of the dominant kernel
     pk, pk_kind = peaks()

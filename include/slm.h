@@ -194,8 +194,11 @@ slm_status slm_store_destroy(slm_store *st);
  * for the kernels (asynchronous on the context stream; desc must stay valid
  * until the next synchronising call). Returns its id in *view_id. */
 slm_status slm_store_add_view(slm_store *st, const float *desc, uint32_t n, uint32_t *view_id);
-/* Append many views from one host buffer: view v has counts[v] rows starting
- * at row offsets[v] of desc. ids[v] receives its id. */
+/* Append many views from one buffer: view v has counts[v] rows starting at
+ * row offsets[v] of desc. ids[v] receives its id. desc may be pageable host
+ * memory (one copy and a scatter kernel), pinned host memory or device memory
+ * (one copy per view, copy engines only; up to 4096 views per call).
+ * Asynchronous on the context stream like slm_store_add_view. */
 slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets, const uint32_t *counts,
                                uint32_t nviews, uint32_t *ids);
 /* Forget every view (capacity is kept). */

@@ -904,6 +904,10 @@ extern "C" slm_status slm_store_add_view(slm_store *st, const float *desc, uint3
 // span into a staging buffer, then one kernel launch per 1024 views scatters
 // them into their padded store rows (instead of one copy per view, each with
 // its own call overhead). All views are checked for room before any is added.
+// Views per slm_store_add_views call copied one by one (pinned or device
+// sources); above this, a staging copy and a scatter kernel.
+constexpr uint32_t kDirectViewCopies = 4096;
+
 extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, const uint64_t *offsets,
                                           const uint32_t *counts, uint32_t nviews, uint32_t *ids) {
     NvtxRange range_("slm_store_add_views");
@@ -918,6 +922,25 @@ extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, cons
     }
     SLM_TRY(store_check_room(st, nviews, padded));
     cudaStream_t s = st->ctx->stream;
+    // Pinned or device sources: one copy per view straight into its padded
+    // store rows (copy engines only). A staging copy plus a scatter kernel
+    // would need SMs, which a batch running on another stream may hold.
+    cudaPointerAttributes pa{};
+    const bool direct_copies = nviews <= kDirectViewCopies && cudaPointerGetAttributes(&pa, desc) == cudaSuccess &&
+                               (pa.type == cudaMemoryTypeHost || pa.type == cudaMemoryTypeDevice);
+    cudaGetLastError();
+    if (direct_copies) {
+        const cudaMemcpyKind kind = pa.type == cudaMemoryTypeDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        for (uint32_t v = 0; v < nviews; ++v) {
+            uint32_t id = 0;
+            const uint64_t row0 = store_place(st, counts[v], &id);
+            if (ids) ids[v] = id;
+            if (counts[v])
+                SLM_CU(cudaMemcpyAsync(st->raw.as<float>() + row0 * kDesc, desc + offsets[v] * kDesc,
+                                       (size_t)counts[v] * kDesc * sizeof(float), kind, s));
+        }
+        return SLM_OK;
+    }
     if (hi > lo) {
         SLM_TRY(st->staging.ensure(st->ctx, (size_t)(hi - lo) * kDesc * sizeof(float)));
         SLM_CU(cudaMemcpyAsync(st->staging.p, desc + lo * kDesc, (size_t)(hi - lo) * kDesc * sizeof(float),

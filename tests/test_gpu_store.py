@@ -1,7 +1,8 @@
 """GPU: the descriptor store's batched upload (slm_store_add_views).
 
-Many views come from one host buffer through one host-to-device copy and a
-scatter kernel into padded store rows. Views may be empty, listed out of
+Many views come from one host buffer: from pageable memory through one
+host-to-device copy and a scatter kernel into padded store rows; from pinned
+or device memory by one copy per view. Views may be empty, listed out of
 buffer order, leave gaps in the buffer or share rows; a batch that does not
 fit is refused whole, leaving the store as it was.
 """
@@ -15,14 +16,23 @@ from skylens_match import synth
 pytestmark = pytest.mark.gpu
 
 
-def test_add_views_layouts(matcher):
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "device"])
+def test_add_views_layouts(matcher, memory):
     rng = np.random.Generator(np.random.PCG64(41))
     buf = synth.sift_like(rng, 1000)
     # (offset, count) per view: out of order, a gap (rows 600-699 unused), an
     # empty view, one view that overlaps another, a single row
     spec = [(700, 300), (0, 250), (250, 0), (250, 350), (100, 200), (999, 1)]
     st = matcher.store(sum(c for _, c in spec), len(spec))
-    ids = st.add_views_packed(buf, [o for o, _ in spec], [c for _, c in spec])
+    if memory == "pageable":
+        ids = st.add_views_packed(buf, [o for o, _ in spec], [c for _, c in spec])
+    else:
+        torch = pytest.importorskip("torch")
+        t = torch.from_numpy(buf)
+        t = t.pin_memory() if memory == "pinned" else t.cuda()
+        torch.cuda.synchronize()
+        ids = st.add_views_ptr(t.data_ptr(), [o for o, _ in spec], [c for _, c in spec])
+        st._keep_tensor = t  # the copies are asynchronous
     assert ids == list(range(len(spec)))
     views = [buf[o:o + c] for o, c in spec]
     pairs = [(u, v) for u in range(len(spec)) for v in range(len(spec)) if u != v]
