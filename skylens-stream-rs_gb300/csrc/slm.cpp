@@ -944,7 +944,7 @@ extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, cons
     if (hi > lo) {
         SLM_TRY(st->staging.ensure(st->ctx, (size_t)(hi - lo) * kDesc * sizeof(float)));
         SLM_CU(cudaMemcpyAsync(st->staging.p, desc + lo * kDesc, (size_t)(hi - lo) * kDesc * sizeof(float),
-                               cudaMemcpyHostToDevice, s));
+                               cudaMemcpyDefault, s));  // host or device source (unified addressing)
     }
     std::vector<uint4> tab;  // {first staging row, first store row, rows, 0}
     tab.reserve(nviews);
