@@ -64,3 +64,34 @@ def test_add_views_refused_whole(matcher):
     assert np.array_equal(got[1], O.ratio_match_np(buf[200:], buf[:100], 0.8, True, threads=4))
     plan.close()
     st.close()
+
+
+@pytest.mark.parametrize("memory", ["pageable", "device"])
+def test_more_views_than_one_copy_each(matcher, memory):
+    """Above 4096 views per call the upload is one staging copy and a scatter
+    kernel, also from device memory."""
+    rng = np.random.Generator(np.random.PCG64(43))
+    counts = rng.integers(1, 4, size=5000).astype(np.uint32)
+    offsets = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
+    buf = synth.sift_like(rng, int(counts.sum()))
+    st = matcher.store(int(counts.sum()), len(counts))
+    if memory == "pageable":
+        ids = st.add_views_packed(buf, offsets, counts)
+    else:
+        torch = pytest.importorskip("torch")
+        t = torch.from_numpy(buf).cuda()
+        torch.cuda.synchronize()
+        ids = st.add_views_ptr(t.data_ptr(), offsets, counts)
+        st._keep_tensor = t
+    assert ids == list(range(len(counts)))
+    # random pairs of these 1-3 row views (a one-row b view has no second neighbour: an empty list)
+    pairs = [(int(u), int(v)) for u, v in rng.integers(0, len(counts), size=(64, 2))]
+    plan = st.plan(pairs, 0.8, True, "fp32")
+    plan.launch()
+    got = plan.per_pair()
+    for k, (u, v) in enumerate(pairs):
+        a = buf[int(offsets[u]):int(offsets[u]) + int(counts[u])]
+        b = buf[int(offsets[v]):int(offsets[v]) + int(counts[v])]
+        assert np.array_equal(got[k], O.ratio_match_np(a, b, 0.8, True, threads=2)), (u, v)
+    plan.close()
+    st.close()
