@@ -196,7 +196,10 @@ class DescriptorStore:
         return ids.tolist()
 
     def add_views_ptr(self, host_ptr: int, offsets, counts) -> list[int]:
-        """Like add_views_packed for a raw host pointer (e.g. a pinned torch tensor)."""
+        """Like add_views_packed for a raw pointer to pinned host or device memory
+        (e.g. a torch tensor): one asynchronous copy per view, so the buffer must
+        stay alive and unchanged until the next synchronising call (a plan's
+        results, or the context stream's synchronisation)."""
         off = np.ascontiguousarray(offsets, dtype=np.uint64)
         cnt = np.ascontiguousarray(counts, dtype=np.uint32)
         ids = np.empty(len(cnt), np.uint32)
