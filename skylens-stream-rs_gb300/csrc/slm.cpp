@@ -923,7 +923,8 @@ extern "C" slm_status slm_store_add_views(slm_store *st, const float *desc, cons
     SLM_TRY(store_check_room(st, nviews, padded));
     cudaStream_t s = st->ctx->stream;
     // Pinned or device sources: one copy per view straight into its padded
-    // store rows (copy engines only). A staging copy plus a scatter kernel
+    // store rows. From pinned host memory these run on the copy engines; a
+    // staging copy followed by a scatter kernel or by device-to-device copies
     // would need SMs, which a batch running on another stream may hold.
     cudaPointerAttributes pa{};
     const bool direct_copies = nviews <= kDirectViewCopies && cudaPointerGetAttributes(&pa, desc) == cudaSuccess &&
