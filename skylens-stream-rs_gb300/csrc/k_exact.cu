@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinalizeArgs g) {
         base += tot;
         __syncthreads();
     }
-    if (tid == 0) g.counts[blockIdx.x] = base;
+    if (tid == 0) g.counts[blockIdx.x] = (g.err && *g.err) ? 0xffffffffu : base;
 }
 
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s) {

@@ -201,7 +201,7 @@ SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs) {
     return L;
 }
 
-// The exact FP32 match of one pair (prep -> exact_kernel -> finalize -> copy)
+// The exact FP32 match of one pair (prep -> exact_kernel -> finalize [-> copy])
 // over a scratch block laid out by single_layout: no metadata from the host.
 cudaError_t single_exact_enqueue(unsigned char *sc, const SingleLayout &L, const float *d_a, uint32_t na,
                                  const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
@@ -228,10 +228,19 @@ cudaError_t single_exact_enqueue(unsigned char *sc, const SingleLayout &L, const
     f.colbest = a.colbest;
     f.ratio2 = ratio * ratio;
     f.mutual = a.mutual;
-    f.slots = reinterpret_cast<uint2 *>(sc + L.slots);
-    f.counts = reinterpret_cast<uint32_t *>(sc + L.counts);
-    launch_finalize(f, s);
-    single_copy_kernel<<<16, 256, 0, s>>>(sc, L, d_out, cap, d_count);
+    if (cap >= na) {
+        // room for every possible match: finalize writes the list and the
+        // count (or the error mark) straight into the caller's buffers
+        f.slots = reinterpret_cast<uint2 *>(d_out);
+        f.counts = d_count;
+        f.err = a.err;
+        launch_finalize(f, s);
+    } else {
+        f.slots = reinterpret_cast<uint2 *>(sc + L.slots);
+        f.counts = reinterpret_cast<uint32_t *>(sc + L.counts);
+        launch_finalize(f, s);
+        single_copy_kernel<<<16, 256, 0, s>>>(sc, L, d_out, cap, d_count);
+    }
     return cudaGetLastError();
 }
 

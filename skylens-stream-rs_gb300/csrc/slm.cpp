@@ -1396,8 +1396,8 @@ slm_status ws_host_block(Workspace *w, size_t bytes) {
 
 // An FP32 single-pair call without a store or a plan: the packing reads the
 // inputs where they lie (or from the workspace's scratch block after two
-// uploads), the metadata is made on the device, and the last kernel writes the
-// count and pairs into pinned host memory (4 kernels, no read-back).
+// uploads), the metadata is made on the device, and the finalize kernel writes
+// the pairs and their count into pinned host memory (3 kernels, no read-back).
 slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t na, const float *b, uint32_t nb,
                             float ratio, int mutual, slm_pair *out, uint32_t cap, uint32_t *n_out, slm_stats *st) {
     const SingleLayout L = single_layout(na, nb, c->sms, true);
@@ -1413,8 +1413,8 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
         src_a = reinterpret_cast<const float *>(sc + L.raw_a);
         src_b = reinterpret_cast<const float *>(sc + L.raw_b);
     }
-    // the copy kernel writes the count and the pairs straight into pinned host
-    // memory (no separate read-back)
+    // finalize writes the count and the pairs straight into pinned host memory
+    // (no separate read-back)
     SLM_TRY(ws_host_block(w, 8 + sizeof(slm_pair) * (size_t)na));
     unsigned char *res = nullptr;
     SLM_CU(cudaHostGetDevicePointer(reinterpret_cast<void **>(&res), w->single_host, 0));
@@ -1429,7 +1429,7 @@ slm_status single_pair_fp32(slm_ctx *c, Workspace *w, const float *a, uint32_t n
         st->pairs = 1;
         st->distances = (uint64_t)na * nb;
         st->matches = n;
-        st->kernel_launches = 4;
+        st->kernel_launches = 3;
     }
     if (n > cap) return fail(SLM_CAPACITY, "need " + std::to_string(n) + " pairs, have " + std::to_string(cap));
     if (n) std::memcpy(out, w->single_host + 8, sizeof(slm_pair) * (size_t)n);

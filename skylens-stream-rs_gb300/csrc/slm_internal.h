@@ -92,6 +92,7 @@ struct FinalizeArgs {
     int mutual;
     uint2 *slots;                // output (i, j) slots
     uint32_t *counts;            // per-pair match count
+    const uint32_t *err;         // if set: a count of 0xffffffff when this error word is set
 };
 
 // Pack n row-major descriptors (src, n x 128) into store tiles starting at
@@ -116,16 +117,16 @@ void launch_fill_u64(unsigned long long *p, uint64_t n, unsigned long long v, cu
 void set_last_error(const char *msg);
 
 // Scratch layout of one exact FP32 pair match with its metadata made on the
-// device (byte offsets; `inputs` adds room for the row-major inputs and a
-// result block [count, pad, pairs]).
+// device (byte offsets; `inputs` adds room for copies of the row-major inputs).
 struct SingleLayout {
     size_t tiled, items, parts, meta, colbest, slots, counts, ctl, raw_a, raw_b, bytes;
     uint32_t rt_n, ct_n, chunks;
 };
 SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs);
-// Enqueues the setup and packing, exact_kernel, finalize and the copy of at most cap
-// pairs into d_out with the count (0xffffffff: a device wait gave up) into
-// *d_count. Returns the launch status.
+// Enqueues the setup and packing, exact_kernel and finalize, which leave at
+// most cap pairs in d_out and the count (0xffffffff: a device wait gave up) in
+// *d_count (directly when cap >= na, else through a copy kernel). Returns the
+// launch status.
 cudaError_t single_exact_enqueue(unsigned char *scratch, const SingleLayout &L, const float *d_a, uint32_t na,
                                  const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
                                  uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s);

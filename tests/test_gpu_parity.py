@@ -244,7 +244,7 @@ def test_autotuned_plan(matcher, prec):
 
 def test_auto_precision(matcher):
     """SLM_PREC_AUTO: the plain FP32 kernel below SLM_AUTO_BF16_DISTANCES, the
-    BF16 shortlist from there up (4 kernels per call, and more than 10);
+    BF16 shortlist from there up (3 kernels per call, and more than 10);
     exact both ways."""
     for n, path in ((800, "fp32"), (3500, "bf16")):
         a, b = synth.pair_large(n, 0.5, 0.05, seed=n)
