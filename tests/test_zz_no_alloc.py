@@ -56,7 +56,22 @@ def test_noalloc_equals_allocating_entry_point_twice():
         assert n == n_ref
         got = out[:n].cpu().numpy().astype(np.uint32)
         assert np.array_equal(got, ref_out[:n_ref].cpu().numpy().astype(np.uint32))
-        assert np.array_equal(got, O.ratio_match_np(a, b, 0.8, True, threads=8))
+        want = O.ratio_match_np(a, b, 0.8, True, threads=8)
+        assert np.array_equal(got, want)
+        # an output buffer smaller than na: the first `cap` pairs and the full count
+        cap = max(1, len(want) // 3)
+        small = torch.full((cap + 1, 2), -1, dtype=torch.int32, device="cuda")
+        cnt.zero_()
+        torch.cuda.synchronize()
+        st = L.slm_ratio_match_device_noalloc(ctypes.c_void_p(da.data_ptr()), na, ctypes.c_void_p(db.data_ptr()), nb,
+                                              ctypes.c_float(0.8), 1, ctypes.c_void_p(small.data_ptr()), cap,
+                                              ctypes.c_void_p(cnt.data_ptr()), ctypes.c_void_p(m.stream))
+        _lib.check(st, "slm_ratio_match_device_noalloc (small output)")
+        stream.synchronize()
+        assert int(cnt.item()) == len(want)
+        sm_out = small.cpu().numpy()
+        assert np.array_equal(sm_out[:cap].astype(np.uint32), want[:cap])
+        assert (sm_out[cap] == -1).all()  # nothing written past cap
     m.close()
 
 
