@@ -153,7 +153,9 @@ slm_status slm_ratio_match_device(slm_ctx *ctx, const float *d_a, uint32_t na, c
  * must be 16-byte aligned. The first call on a device sets that device up
  * (make it before any stream capture). Calls share the array: calls that
  * overlap on the GPU race. *d_count receives the match count (0xffffffff if a
- * bounded device wait gave up); at most cap pairs are written to d_out. */
+ * bounded device wait gave up; d_out's first cap pairs are then unspecified);
+ * at most cap pairs are written to d_out, which needs only slm_pair's own
+ * 4-byte alignment. */
 #define SLM_NOALLOC_MAX_DESCS 4096
 slm_status slm_ratio_match_device_noalloc(const float *d_a, uint32_t na, const float *d_b, uint32_t nb, float ratio,
                                           int mutual, slm_pair *d_out, uint32_t cap, uint32_t *d_count,

@@ -228,7 +228,7 @@ cudaError_t single_exact_enqueue(unsigned char *sc, const SingleLayout &L, const
     f.colbest = a.colbest;
     f.ratio2 = ratio * ratio;
     f.mutual = a.mutual;
-    if (cap >= na) {
+    if (single_direct_output(d_out, cap, na)) {
         // room for every possible match: finalize writes the list and the
         // count (or the error mark) straight into the caller's buffers
         f.slots = reinterpret_cast<uint2 *>(d_out);

@@ -123,10 +123,18 @@ struct SingleLayout {
     uint32_t rt_n, ct_n, chunks;
 };
 SingleLayout single_layout(uint32_t na, uint32_t nb, int sms, bool inputs);
+// Whether finalize may write the match list straight into d_out: there must be
+// room for every possible match (cap >= na), and finalize stores each pair as
+// one 8-byte vector, while slm_pair itself only needs 4-byte alignment. Any
+// other d_out gets the list through single_copy_kernel, which stores the two
+// fields separately.
+inline bool single_direct_output(const slm_pair *d_out, uint32_t cap, uint32_t na) {
+    return cap >= na && (reinterpret_cast<uintptr_t>(d_out) & 7u) == 0;
+}
 // Enqueues the setup and packing, exact_kernel and finalize, which leave at
 // most cap pairs in d_out and the count (0xffffffff: a device wait gave up) in
-// *d_count (directly when cap >= na, else through a copy kernel). Returns the
-// launch status.
+// *d_count (directly when single_direct_output holds, else through a copy
+// kernel). Returns the launch status.
 cudaError_t single_exact_enqueue(unsigned char *scratch, const SingleLayout &L, const float *d_a, uint32_t na,
                                  const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
                                  uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s);
