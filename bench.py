@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
     ap.add_argument("--no-scheduled", action="store_true",
                     help="skip the scheduled_pairs(PairSchedule::default()) batch with the < 20 filter")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' sub-records (single pairs 800 / 8192 / 32768, serving)")
+    ap.add_argument("--config-rates", default="50,burst", help="serving arrival rates in the default run's sub-record")
     return ap.parse_args()
 
 
@@ -163,6 +166,19 @@ def peaks():
         "fallback"
 
 
+L2_NOTE = ("zone store 141 MB (raw f32) > 129 MB L2; the GPU arm also flushes L2 (512 MiB write) between steps, "
+           "outside the timed events")
+ORACLE_FLAGS = "gcc -O3 -std=c11 -ffp-contract=off -fno-fast-math -fPIC (portable: no -march/-mcpu=native)"
+
+
+def workload_config(z, seed: int, ws: int = 1) -> dict:
+    """The workload as both arms report it (the GPU arm's precision and tuned
+    settings are top-level keys of its line)."""
+    return {"workload": WORKLOAD, "views": len(z.counts), "pairs": int(len(z.pairs)), "distances": int(z.distances),
+            "descriptors": int(z.counts.sum()), "ratio": 0.8, "mutual": True, "seed": seed, "l2": L2_NOTE,
+            "parallelism": f"replicas{ws}"}
+
+
 def cpu_baseline(z, budget_s: float, threads: int):
     """The oracle's blocked ratio_match (64-row blocks over `threads` host threads,
     pairs serial as in benches/pipeline.rs:247-253) on pairs in a fixed order until
@@ -200,47 +216,51 @@ def run_reference(args):
         npairs.append(n)
     wall = time.perf_counter() - t0
     value = float(np.mean(rates))
+    sample = {"pairs_per_step": int(np.mean(npairs)), "of_pairs": int(len(z.pairs)),
+              "seconds_per_step": per_step,
+              "order": "a fixed random permutation of the zone's pairs (PCG64 seed 123); each step starts at its "
+                       "first pair and runs until the step's time budget is used"}
     line = {"metric": METRIC, "value": value, "unit": "image pairs/s", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "views": len(z.counts), "pairs": int(len(z.pairs)),
-                       "distances": z.distances, "sample": "pairs in a fixed random order, each step "
-                       f"~{per_step:.1f}s of CPU time ({int(np.mean(npairs))} pairs/step)"},
+            "config": workload_config(z, args.seed, ws),
             "distances_per_s": float(np.mean(drates)),
             "cpu_baseline": {"value": value, "unit": "image pairs/s", "cores": threads, "kind": "port",
-                             "sample": f"{int(np.mean(npairs))} of {len(z.pairs)} zone pairs per step"},
+                             "sample": f"{int(np.mean(npairs))} of {len(z.pairs)} zone pairs per step",
+                             "sample_detail": sample, "compiler": ORACLE_FLAGS},
             "e2e": {"value": value, "unit": "image pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serve(args):
+def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32")) -> dict:
     """Serving: zones of 48 positions x 3 cameras, n ~ log-uniform[500, 4000],
-    views arriving as a Poisson process; each view is matched against its
-    candidate_pairs partners already on the device."""
+    views arriving as a Poisson process (or all at once: 'burst'); each view is
+    matched against its candidate_pairs partners already on the device.
+    Latency = submit -> match lists on the host; every 9th request's lists are
+    checked against the oracle."""
     import oracle as O
     from skylens_match import serve
-    z = serve.serving_zone(48, seed=args.seed + 2)
+    z = serve.serving_zone(48, seed=seed + 2)
     reqs = serve.zone_requests(z)
     out = {"metric": "serving: image pairs/s and p50/p99 request latency (view arrival -> match lists on host)",
            "config": {"workload": "serve_zone144", "views": len(z.counts), "pairs": int(len(z.pairs)),
-                      "n": "log-uniform [500, 4000]", "arrivals": "Poisson"}, "runs": []}
+                      "n": "log-uniform [500, 4000]", "arrivals": "Poisson", "slots": 3}, "runs": []}
     check = {}
-    for prec in ("bf16", "fp32"):
-        for rate in [None if r == "burst" else float(r) for r in args.rates.split(",")]:
+    for prec in prec_list:
+        for rate in [None if r == "burst" else float(r) for r in rates.split(",")]:
             srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
             res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
             st = srv.stats()
             srv.close()
             npairs = sum(len(p) for _, p in reqs)
-            # bit-exactness against the oracle on a sample of requests
             mism = 0
             for k in range(0, len(reqs), 9):
                 v, pairs = reqs[k]
                 for (u, _), got in zip(pairs, res[k]):
                     key = (u, v)
                     if key not in check:
-                        check[key] = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=os.cpu_count() or 1)
+                        check[key] = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=threads)
                     mism += not np.array_equal(got, check[key])
             out["runs"].append({"precision": prec, "rate_views_per_s": rate if rate else "burst",
                                 "p50_ms": float(np.percentile(lats, 50)),
@@ -249,29 +269,35 @@ def run_serve(args):
                                 "max_batch_requests": st["max_batch_requests"], "max_inflight": st["max_inflight"],
                                 "bit_exact_sample_mismatches": int(mism)})
             print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
+    return out
+
+
+def run_serve(args):
+    out = serve_configs(args.seed, args.rates, os.cpu_count() or 1)
     print(json.dumps(out), flush=True)
     if args.json_out:
         open(args.json_out, "w").write(json.dumps(out) + "\n")
     return 0
 
 
-def run_pairs(args):
+def pair_configs(m, steps: int, threads: int) -> list:
     """Single-pair configurations: 800 x 800, 8192 x 8192 (BF16 vs FP32), and
-    32768 x 32768 (FP8 E4M3 shortlist); bit-exactness against the oracle,
-    distance-estimate error against FP64, rows settled exactly."""
+    32768 x 32768 (FP8 E4M3 shortlist), each in every precision through a
+    one-pair plan: device time by CUDA events (median of `steps` launches),
+    bit-exactness of the whole list against the oracle, distance-estimate
+    error against FP64 on a 1024 x 1024 block, and the rows settled exactly."""
     import torch
 
     import oracle as O
-    import skylens_match as sm
     from skylens_match import synth
-    m = sm.Matcher()
     ext = torch.cuda.ExternalStream(m.stream)
     pk, _ = peaks()
-    cases = [("pair800", synth.pair_800(0)), ("pair8192", synth.pair_large(8192, 0.5, 0.05, seed=2)),
-             ("pair32768", synth.pair_fp8(32768, seed=4))]
+    cases = [("pair800", lambda: synth.pair_800(0)), ("pair8192", lambda: synth.pair_large(8192, 0.5, 0.05, seed=2)),
+             ("pair32768", lambda: synth.pair_fp8(32768, seed=4))]
     out = []
-    for name, (a, b) in cases:
-        ref = O.ratio_match_np(a, b, 0.8, True, threads=os.cpu_count() or 1)
+    for name, make in cases:
+        a, b = make()
+        ref = O.ratio_match_np(a, b, 0.8, True, threads=threads)
         st = m.store(len(a) + len(b), 2)
         st.add_view(a)
         st.add_view(b)
@@ -281,7 +307,7 @@ def run_pairs(args):
             plan.launch()
             got, _ = plan.results()
             times = []
-            for _ in range(max(1, args.steps)):
+            for _ in range(max(1, steps)):
                 with torch.cuda.stream(ext):
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
@@ -326,8 +352,17 @@ def run_pairs(args):
             p.close()
         st2.close()
         st.close()
-        print(json.dumps(row), flush=True)
+        print(json.dumps(row), file=sys.stderr, flush=True)
         out.append(row)
+    return out
+
+
+def run_pairs(args):
+    import skylens_match as sm
+    m = sm.Matcher()
+    out = pair_configs(m, args.steps, os.cpu_count() or 1)
+    for r in out:
+        print(json.dumps(r), flush=True)
     if args.json_out:
         open(args.json_out, "w").write("\n".join(json.dumps(r) for r in out) + "\n")
     m.close()
@@ -582,7 +617,7 @@ def main():
         cpu = {"value": med, "unit": "image pairs/s", "cores": cores, "kind": "port",
                "sample": f"{int(np.median([x[2] for x in runs]))} of {len(z.pairs)} zone pairs in a fixed random "
                          f"order per repeat (~{args.cpu_seconds / 3:.0f} s), 3 repeats",
-               "median": med, "min": float(min(x[0] for x in runs)),
+               "median": med, "min": float(min(x[0] for x in runs)), "compiler": ORACLE_FLAGS,
                "distances_per_s": float(np.median([x[1] for x in runs])),
                "one_thread": {"median": float(np.median([x[0] for x in one])), "min": float(min(x[0] for x in one)),
                               "unit": "image pairs/s",
@@ -593,11 +628,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp8": "e4m3"}[prec],
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": prec, "tuned": tuned, "views": len(z.counts),
-                       "pairs": int(len(z.pairs)),
-                       "distances": dist_n, "descriptors": n_rows, "ratio": 0.8, "mutual": True,
-                       "l2": "flushed between steps (512 MiB write, outside the events)",
-                       "parallelism": f"replicas{ws}"},
+            "config": workload_config(z, args.seed + rank, ws), "precision": prec, "tuned": tuned,
             "distances_per_s": dist_rate,
             "bit_exact": {"ok": bit_exact, "pairs_checked": int(nverify), "mismatched_pairs": int(mism)},
             "fp32_plain": fp32, "scheduled": sched,
@@ -605,6 +636,13 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(stats_main.get("kernel_launches", 0)) * args.steps,
             "clocks": clk, "wall_s_timed": t_wall}
+    if rank == 0 and ws == 1 and not args.no_configs:
+        # the other configurations, bounded (about half a minute): single pairs
+        # in every precision and the serving workload at one rate and in a burst
+        t_c = time.perf_counter()
+        line["configs"] = {"pairs": pair_configs(m, 3, os.cpu_count() or 1),
+                           "serve": serve_configs(args.seed, args.config_rates, os.cpu_count() or 1)}
+        line["configs"]["wall_s"] = time.perf_counter() - t_c
     if rank == 0:
         s = json.dumps(line)
         print(s, flush=True)
