@@ -502,6 +502,14 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         // ---------------------------------------------------------- MMA issue
         constexpr uint32_t idesc = umma_idesc(FP8);
         constexpr uint32_t idesc_neg = umma_idesc(FP8, true);
+        // Every operand tile has a fixed shared-memory address for the whole
+        // kernel: the descriptors are made once, and a tile, stage or K step
+        // adds its byte offset / 16 to the 14-bit start-address field (all
+        // shared addresses lie below 256 KiB, so the field never carries).
+        constexpr uint32_t kOp16 = kOp >> 4;
+        const uint64_t adesc0 = umma_desc(smem_u32(S.A[0])), bdesc0 = umma_desc(smem_u32(S.B[0]));
+        const uint64_t aext0 = umma_desc_plain(smem_u32(S.A[0]) + kBf16TileBytes, 128, 384);
+        const uint64_t bext0 = umma_desc_plain(smem_u32(S.B[0]) + kBf16TileBytes + 128, 128, 384);
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
@@ -516,22 +524,24 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                 }
                 tc_fence_after();
                 if (lane == 0) {
-                    for (uint32_t a = 0; a < item.nat; ++a) {
+                    const uint64_t bd = bdesc0 + (uint64_t)(st * kOp16);
+#pragma unroll
+                    for (uint32_t a = 0; a < 2; ++a) {
+                        if (a >= item.nat) break;
                         const uint32_t d_tmem = tmem + (tb * 2 + a) * 128;
-                        const uint32_t abase = smem_u32(S.A[a]), bbase = smem_u32(S.B[st]);
+                        const uint64_t ad = adesc0 + (uint64_t)(a * kOp16);
                         if constexpr (FP8) {
 #pragma unroll
                             for (int k = 0; k < 4; ++k)  // K = 32 e4m3 = 32 bytes per step
-                                mma_f8(d_tmem, umma_desc(abase + k * 32), umma_desc(bbase + k * 32), idesc, k > 0);
+                                mma_f8(d_tmem, ad + 2 * k, bd + 2 * k, idesc, k > 0);
                         } else {
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {  // K = 16 bf16 = 32 bytes per step; -a.b
-                                const uint32_t off = (k >> 2) * 16384 + (k & 3) * 32;
-                                mma_f16(d_tmem, umma_desc(abase + off), umma_desc(bbase + off), idesc_neg, k > 0);
+                                const uint32_t off16 = (k >> 2) * (16384 >> 4) + (k & 3) * 2;
+                                mma_f16(d_tmem, ad + off16, bd + off16, idesc_neg, k > 0);
                             }
                             // + (|a|^2 + |b|^2) / 2: A from kc0, B from kc1 of the norm extension
-                            mma_f16(d_tmem, umma_desc_plain(abase + kBf16TileBytes, 128, 384),
-                                    umma_desc_plain(bbase + kBf16TileBytes + 128, 128, 384), idesc, true);
+                            mma_f16(d_tmem, aext0 + (uint64_t)(a * kOp16), bext0 + (uint64_t)(st * kOp16), idesc, true);
                         }
                     }
                     mma_commit(&S.b_empty[st]);
