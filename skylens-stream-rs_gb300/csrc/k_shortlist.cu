@@ -147,6 +147,19 @@ SLM_DEV void st_pair_if(uint2 *p, uint32_t a, uint32_t b, bool pred) {
         : "memory");
 }
 
+// One record (4 values, first column) when pred holds, without a branch.
+SLM_DEV void st_rec_if(float4 *p, uint32_t *pj, float a, float b, float c, float d, uint32_t j, bool pred) {
+    asm volatile(
+        "{\n"
+        ".reg .pred q;\n"
+        "setp.ne.u32 q, %6, 0;\n"
+        "@q st.global.v4.f32 [%0], {%2, %3, %4, %5};\n"
+        "@q st.global.u32 [%1], %7;\n"
+        "}\n" ::"l"(p),
+        "l"(pj), "f"(a), "f"(b), "f"(c), "f"(d), "r"((uint32_t)pred), "r"(j)
+        : "memory");
+}
+
 // Minimum of 16 values, and with the minima of its two groups of 8.
 SLM_DEV float min16(const float (&d)[16]) {
     const float a = min3f(d[0], d[1], d[2]), b = min3f(d[3], d[4], d[5]), c = min3f(d[6], d[7], d[8]);
@@ -610,9 +623,10 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             // row's shortlist size that pair routing uses
             const float w2 = 2.f * sp.eps;
             uint32_t near = 0;
-            const bool own_row = sp.nchunk == 1;
-            const uint32_t ridx = sp.rbase + i;
-            uint2 *cand = g.rowcand + (size_t)ridx * kSlRowSlots + h * kSlHalfSlots;
+            // pass 2: the records of this row and of the item's column range
+            // (exactly one item writes them: plain stores, a running count)
+            const uint32_t crow = PASS == 2 ? sl_cand_row(sp, pm.na, (mypart - sp.part_base) % sp.nchunk, i) : 0;
+            const uint32_t rec0 = crow * kSlRowRecs + h * kSlHalfRecs;
             uint32_t ncand = 0;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
@@ -631,10 +645,9 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     const uint32_t tcol = tmem + lane_addr + (tb * 2 + at) * 128 + h * 64;
                     // chunks of 16 columns, two per iteration: loads double-buffered,
                     // the body kept at two copies (instruction-cache footprint)
-                    auto chunk = [&](const uint32_t (&vc)[16], int c) {
+                    auto chunk = [&](const uint32_t (&vc)[16], int c, const ulonglong2 (&tt)[4]) {
                         const uint32_t cb = h * 64 + c * 16;   // column within the tile
                         const uint32_t j0 = t * kTile + cb;    // column within the pair
-                        if (j0 >= pm.nb) return;               // padding only (warp-uniform)
                         float d[16];
                         if constexpr (FP8) {
                             const float4 *bn4 = reinterpret_cast<const float4 *>(&S.bnorm[st][cb]);
@@ -690,95 +703,72 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 if (lane == 0) cp[k4] = o;
                             }
                         } else {
-                            {
-                                // rows certain to have no match carry thr_i = -inf: no hit
-                                float g4[4];
-                                const float cm = min16q(d, g4);
-                                if (cm <= thr_i) {
-                                    if (own_row) {
-                                        // the item owns the whole row: predicated stores, running count
+                            // both tests' group minima first (independent chains), then
+                            // the rare bodies. Row candidates: d~ <= T (rows certain to
+                            // have no match carry T = -inf); column window: d~ <= c1 + 2 eps,
+                            // x = d - thr in the accumulator domain (the sign is exact)
+                            float x[16];
 #pragma unroll
-                                        for (int qq = 0; qq < 4; ++qq) {
-                                            if (g4[qq] <= thr_i) {
+                            for (int k4 = 0; k4 < 4; ++k4) {
+                                u64x x0, x1;
+                                if constexpr (FP8) {
+                                    x0 = f2_sub(f2_pack(d[4 * k4], d[4 * k4 + 1]), tt[k4].x);
+                                    x1 = f2_sub(f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]), tt[k4].y);
+                                } else {
+                                    const u64x mhalf = f2_pack(-0.5f, -0.5f);
+                                    x0 = f2_fma(tt[k4].x, mhalf, f2_pack(d[4 * k4], d[4 * k4 + 1]));
+                                    x1 = f2_fma(tt[k4].y, mhalf, f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]));
+                                }
+                                x[4 * k4 + 0] = f2_lo(x0);
+                                x[4 * k4 + 1] = f2_hi(x0);
+                                x[4 * k4 + 2] = f2_lo(x1);
+                                x[4 * k4 + 3] = f2_hi(x1);
+                            }
+                            float gr[4], gc[4];
+                            const float cm = min16q(d, gr);
+                            const float xm = rvalid ? min16q(x, gc) : kInf;
+                            if (cm <= thr_i) {
+                                // a hit group: one record of its 4 values (accumulator domain)
 #pragma unroll
-                                                for (int k = 4 * qq; k < 4 * qq + 4; ++k) {
-                                                    const bool hit = d[k] <= thr_i;
-                                                    st_pair_if(cand + min(ncand, (uint32_t)kSlHalfSlots - 1), j0 + k,
-                                                               __float_as_uint(kDom * d[k]), hit && ncand < kSlHalfSlots);
-                                                    ncand += hit ? 1u : 0u;
-                                                }
-                                            }
-                                        }
-                                    } else {
-                                        // rows shared with other items: slots by atomics, 8 values per
-                                        // group (a path the zone's pairs rarely take: kept small)
-#pragma unroll
-                                        for (int qq = 0; qq < 2; ++qq) {
-                                            if (fminf(g4[2 * qq], g4[2 * qq + 1]) <= thr_i) {
-#pragma unroll
-                                                for (int k = 8 * qq; k < 8 * qq + 8; ++k) {
-                                                    // once the count passed the capacity, the row is
-                                                    // settled by an exact scan: no more slots needed
-                                                    if (d[k] <= thr_i && ncand <= kSlHalfSlots) {
-                                                        const uint32_t sl = atomicAdd(&g.rowcnt[2 * ridx + h], 1u);
-                                                        if (sl < kSlHalfSlots)
-                                                            cand[sl] = make_uint2(j0 + k, __float_as_uint(kDom * d[k]));
-                                                        else if (sl == kSlHalfSlots)  // this half overflowed just now
-                                                            atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
-                                                        ncand = sl + 1;
-                                                    }
-                                                }
-                                            }
-                                        }
+                                for (int qq = 0; qq < 4; ++qq) {
+                                    if (gr[qq] <= thr_i) {
+                                        const uint32_t sl = rec0 + min(ncand, (uint32_t)kSlHalfRecs - 1);
+                                        st_rec_if(g.rowrec + sl, g.rowrecj + sl, d[4 * qq], d[4 * qq + 1], d[4 * qq + 2],
+                                                  d[4 * qq + 3], j0 + 4 * qq, ncand < kSlHalfRecs);
+                                        ++ncand;
                                     }
                                 }
                             }
-                            if (rvalid) {
-                                const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(
-                                    two && at == 1 ? &S.bthr2[st][cb] : &S.bthr[st][cb]);
-                                float x[16];
+                            if (xm <= 0.f) {
+                                uint32_t *cc = g.colcnt + sp.cbase + j0;
 #pragma unroll
-                                for (int k4 = 0; k4 < 4; ++k4) {
-                                    // x = d - thr in the accumulator domain (the sign is exact)
-                                    const ulonglong2 tt = bt2[k4];
-                                    u64x x0, x1;
-                                    if constexpr (FP8) {
-                                        x0 = f2_sub(f2_pack(d[4 * k4], d[4 * k4 + 1]), tt.x);
-                                        x1 = f2_sub(f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]), tt.y);
-                                    } else {
-                                        const u64x mhalf = f2_pack(-0.5f, -0.5f);
-                                        x0 = f2_fma(tt.x, mhalf, f2_pack(d[4 * k4], d[4 * k4 + 1]));
-                                        x1 = f2_fma(tt.y, mhalf, f2_pack(d[4 * k4 + 2], d[4 * k4 + 3]));
+                                for (int qq = 0; qq < 4; ++qq)
+                                    if (gc[qq] <= 0.f) {
+#pragma unroll
+                                        for (int k = 4 * qq; k < 4 * qq + 4; ++k) red_add1_le0(cc + k, x[k]);
                                     }
-                                    x[4 * k4 + 0] = f2_lo(x0);
-                                    x[4 * k4 + 1] = f2_hi(x0);
-                                    x[4 * k4 + 2] = f2_lo(x1);
-                                    x[4 * k4 + 3] = f2_hi(x1);
-                                }
-                                float g4[4];
-                                const float xm = min16q(x, g4);
-                                if (xm <= 0.f) {
-                                    uint32_t *cc = g.colcnt + sp.cbase + j0;
-#pragma unroll
-                                    for (int qq = 0; qq < 4; ++qq)
-                                        if (g4[qq] <= 0.f) {
-#pragma unroll
-                                            for (int k = 4 * qq; k < 4 * qq + 4; ++k) red_add1_le0(cc + k, x[k]);
-                                        }
-                                }
                             }
                         }
                     };
-                    uint32_t v0[16], v1[16];
-                    tmem_ld16(tcol, v0);
+                    // one chunk of 16 columns per TMEM load, one copy of the body: the
+                    // epilogue is bound by its instruction stream (measured: a second
+                    // copy of the body to overlap the next load with this chunk, or
+                    // four loads in flight, ran slower), and the other epilogue warps
+                    // of the sub-partition cover the load's latency
+                    const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(
+                        two && at == 1 ? &S.bthr2[st][h * 64] : &S.bthr[st][h * 64]);
 #pragma unroll 1
-                    for (int c = 0; c < 4; c += 2) {
-                        tmem_wait_ld16(v0);
-                        tmem_ld16(tcol + (c + 1) * 16, v1);
-                        chunk(v0, c);
-                        tmem_wait_ld16(v1);
-                        if (c + 2 < 4) tmem_ld16(tcol + (c + 2) * 16, v0);
-                        chunk(v1, c + 1);
+                    for (int c = 0; c < 4; ++c) {
+                        if (t * kTile + h * 64 + c * 16 >= pm.nb) break;  // padding only (warp-uniform)
+                        ulonglong2 tt[4];  // pass 2: the chunk's column thresholds, read before the wait
+                        if constexpr (PASS == 2) {
+#pragma unroll
+                            for (int k4 = 0; k4 < 4; ++k4) tt[k4] = bt2[c * 4 + k4];
+                        }
+                        uint32_t v[16];
+                        tmem_ld16(tcol + c * 16, v);
+                        tmem_wait_ld16(v);
+                        chunk(v, c, tt);
                     }
                 }
                 tc_fence_before();
@@ -843,9 +833,11 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     g.rownear[slot] = near + S.rownear[r];
                 }
             } else {
-                if (own_row && rvalid && thr_i > -kInf) {
-                    g.rowcnt[2 * ridx + h] = ncand;
-                    if (ncand > kSlHalfSlots) atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
+                if (rvalid && thr_i > -kInf) {
+                    g.rowcnt[2 * crow + h] = ncand;
+                    // a wide shortlist (more than half the records): the pair's bound may be
+                    // too loose for its distances (routing estimate of finalize)
+                    if (ncand > kSlHalfRecs / 2) atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
                 }
             }
         }
@@ -1065,11 +1057,11 @@ SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &s
 }
 
 // One thread per row (CTA per pair and row block): decide from the bounds, or
-// queue exact work. A pair with more than 1/8 as many overflowed row halves
-// (counted by pass 2) as rows is routed to the exact kernel instead (one exact
-// scan per row would cost more).
+// queue exact work. A pair with more than 1/8 as many wide row halves
+// (counted by pass 2) as rows is routed to the exact kernel instead (exact
+// rescoring of long shortlists or scans per row would cost more).
 template <int kThreads>
-__global__ void __launch_bounds__(kThreads) sl_finalize_kernel(SlArgs g) {
+__global__ void __launch_bounds__(kThreads, 1) sl_finalize_kernel(SlArgs g) {
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
@@ -1089,36 +1081,48 @@ __global__ void __launch_bounds__(kThreads) sl_finalize_kernel(SlArgs g) {
         const uint32_t ridx = sp.rbase + i;
         uint32_t dec = kDecNone;
         if (g.rowthr[ridx] > -kInf) {
-            const uint32_t n0 = g.rowcnt[2 * ridx], n1 = g.rowcnt[2 * ridx + 1];
-            const uint32_t n = n0 + n1;
-            if (n0 > kSlHalfSlots || n1 > kSlHalfSlots) {
-                push_scan(g, p, 0, i, 0);
-                dec = kDecPending;
-            } else {
-                const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
-                float a1 = kInf, a2 = kInf;
-                uint32_t j1 = 0xffffffffu;
-                // four entries per step, loaded before they are used (independent loads)
-                for (uint32_t k0 = 0; k0 < n; k0 += 4) {
-                    uint2 e[4];
+            // the row's records: two column halves per column range of the pair.
+            // S = the records' columns with d~ <= T (values above T, and the NaN of
+            // padding columns, are not in S); a half with more hit groups than
+            // records overflowed and the row is scanned exactly instead
+            const float T = g.rowthr[ridx];
+            const float dom = g.fp8 ? 1.f : 2.f;
+            float a1 = kInf, a2 = kInf;
+            uint32_t j1 = 0xffffffffu, n = 0;
+            bool over = false;
+            for (uint32_t l = 0; l < 2 * sp.nchunk; ++l) {
+                const uint32_t cr = sl_cand_row(sp, pm.na, l >> 1, i);
+                const uint32_t nl = g.rowcnt[2 * cr + (l & 1)];
+                over |= nl > kSlHalfRecs;
+                const uint32_t b0 = cr * kSlRowRecs + (l & 1) * kSlHalfRecs;
+                // two records per step, loaded before they are used
+                for (uint32_t r = 0; r < nl && r < kSlHalfRecs; r += 2) {
+                    const bool two = r + 1 < nl && r + 1 < kSlHalfRecs;
+                    const float4 v0 = g.rowrec[b0 + r];
+                    const uint32_t jb0 = g.rowrecj[b0 + r];
+                    const float4 v1 = two ? g.rowrec[b0 + r + 1] : make_float4(kInf, kInf, kInf, kInf);
+                    const uint32_t jb1 = two ? g.rowrecj[b0 + r + 1] : 0u;
+                    const float vs[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t k = k0 + q;
-                        e[q] = k < n ? S[k < n0 ? k : kSlHalfSlots + (k - n0)] : make_uint2(0xffffffffu, 0x7f800000u);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (k0 + q >= n) break;
-                        const float v = __uint_as_float(e[q].y);
-                        if (v < a1 || (v == a1 && e[q].x < j1)) {
+                    for (int q = 0; q < 8; ++q) {
+                        const float v = dom * vs[q];
+                        const uint32_t j = (q < 4 ? jb0 : jb1) + (q & 3);
+                        if (!(v <= T)) continue;
+                        ++n;
+                        if (v < a1 || (v == a1 && j < j1)) {
                             a2 = a1;
                             a1 = v;
-                            j1 = e[q].x;
+                            j1 = j;
                         } else if (v < a2) {
                             a2 = v;
                         }
                     }
                 }
+            }
+            if (over) {
+                push_scan(g, p, 0, i, 0);
+                dec = kDecPending;
+            } else {
                 // S holds every column with d~ <= T, T >= (second smallest d~) + 2 eps,
                 // so the exact two smallest distances are among S. With fewer than
                 // two finite entries the exact second best is infinite
@@ -1174,37 +1178,60 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
         const PairMeta pm = g.pairs[qe.pair];
         const SlPair sp = g.spairs[qe.pair];
         const uint32_t ridx = sp.rbase + qe.i;
-        const uint32_t n0 = g.rowcnt[2 * ridx], n = n0 + g.rowcnt[2 * ridx + 1];
-        const uint2 *S = g.rowcand + (size_t)ridx * kSlRowSlots;
-        // entry k of S: slots [0, n0) of the first half, then the second half
-        auto slot = [&](uint32_t k) { return k < n0 ? k : kSlHalfSlots + (k - n0); };
         const float *a = g.raw + (size_t)(pm.a_row0 + qe.i) * kDesc;
         const float *B = g.raw + (size_t)pm.b_row0 * kDesc;
         float e1 = kInf, e2 = kInf, ad = kInf, maxerr = 0.f;
         uint32_t ej = 0xffffffffu;
-        for (uint32_t k0 = 0; k0 < n; k0 += 4) {
-            const uint32_t k = k0 + grp;
-            const uint2 ent = S[slot(k < n ? k : k0)];
-            const float d = dist8(a, B + (size_t)ent.x * kDesc);
-            // every lane merges the 4 results in slot order
+        // S = the records' columns with d~ <= T, four entries at a time: lane group
+        // grp computes queued entry grp, every lane merges the results in order
+        const float T = g.rowthr[ridx];
+        const float dom = g.fp8 ? 1.f : 2.f;
+        uint32_t qj = 0, nq = 0;  // this lane group's queued column (0: a valid placeholder)
+        float qv = kInf;
+        auto flush = [&](uint32_t cnt) {
+            const float d = dist8(a, B + (size_t)qj * kDesc);
 #pragma unroll
             for (uint32_t q = 0; q < 4; ++q) {
                 const float dq = __shfl_sync(0xffffffffu, d, q * 8);
-                const uint2 eq = S[slot(k0 + q < n ? k0 + q : k0)];
-                if (k0 + q < n) {
-                    const float approx = __uint_as_float(eq.y);
+                const uint32_t jq = __shfl_sync(0xffffffffu, qj, q * 8);
+                const float approx = __shfl_sync(0xffffffffu, qv, q * 8);
+                if (q < cnt) {
                     maxerr = fmaxf(maxerr, fabsf(dq - approx));
-                    if (dq < e1 || (dq == e1 && eq.x < ej)) {
+                    if (dq < e1 || (dq == e1 && jq < ej)) {
                         e2 = e1;
                         e1 = dq;
-                        ej = eq.x;
+                        ej = jq;
                         ad = approx;
                     } else if (dq < e2) {
                         e2 = dq;
                     }
                 }
             }
+        };
+        for (uint32_t l = 0; l < 2 * sp.nchunk; ++l) {
+            const uint32_t cr = sl_cand_row(sp, pm.na, l >> 1, qe.i);
+            const uint32_t nl = g.rowcnt[2 * cr + (l & 1)];
+            const uint32_t b0 = cr * kSlRowRecs + (l & 1) * kSlHalfRecs;
+            for (uint32_t r = 0; r < nl; ++r) {
+                const float4 v4 = g.rowrec[b0 + r];
+                const uint32_t jb = g.rowrecj[b0 + r];
+                const float vs[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) {
+                    const float v = dom * vs[q];
+                    if (!(v <= T)) continue;  // warp-uniform: every lane reads the same record
+                    if (grp == nq) {
+                        qj = jb + q;
+                        qv = v;
+                    }
+                    if (++nq == 4) {
+                        flush(4);
+                        nq = 0;
+                    }
+                }
+            }
         }
+        if (nq) flush(nq);
         if (lane == 0) {
             ++w_rows;
             if (maxerr == maxerr) w_err = fmaxf(w_err, maxerr);

@@ -215,9 +215,9 @@ struct slm_plan {
     // shortlist path
     std::vector<SlItem> sitems;
     std::vector<SlPair> spairs;
-    uint64_t rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0, row_blocks_total = 0;
+    uint64_t rows_pad = 0, cand_rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0, row_blocks_total = 0;
     uint32_t row_blocks = 1;  // the most row blocks of any pair
-    DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowcand, d_colcnt,
+    DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowrec, d_rowrecj, d_colcnt,
         d_rowdec, d_queue, d_rqueue, d_dump, d_xlist, d_xitems, d_xparts, d_blkcnt, d_pairctl;
     bool dump = false;
     uint32_t min_matches = 0;        // pairs with fewer matches report none
@@ -305,7 +305,7 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     if (supers && supers < want) split = (uint32_t)((want + supers - 1) / supers);
     p->sitems.clear();
     p->spairs.assign(p->np, SlPair{});
-    uint64_t rb = 0, cb = 0, part = 0, row_tiles = 0, blk = 0;
+    uint64_t rb = 0, cb = 0, part = 0, row_tiles = 0, blk = 0, crb = 0;
     p->row_blocks = 1;
     for (uint32_t k = 0; k < p->np; ++k) {
         const PairMeta &m = p->meta[k];
@@ -320,9 +320,11 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
         sp.view_a = pairs[k].i;
         sp.view_b = pairs[k].j;
         const uint32_t rt_n = (m.na + kTile - 1) / kTile, ct_n = (m.nb + kTile - 1) / kTile;
-        const uint32_t chunks = std::max(1u, std::min(split, ct_n));
+        const uint32_t chunks = std::max(1u, std::min(std::min(split, ct_n), kSlMaxRanges));
         sp.nchunk = chunks;
         sp.part_base = (uint32_t)part;
+        sp.crbase = (uint32_t)crb;
+        crb += pad_rows(m.na) * chunks;  // one pair of S lists per row and column range
         if (m.na && m.nb) {
             // row_tiles == 1: one 128-row a tile per item (M = 128 per CTA)
             const uint32_t per = p->tune.row_tiles == 1 ? 1u : 2u;
@@ -347,7 +349,8 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
         rb += pad_rows(m.na);
         cb += pad_rows(m.nb);
     }
-    if (rb >= (1ull << 32) || cb >= (1ull << 32)) return fail(SLM_CAPACITY, "batch too large for one plan");
+    if (rb >= (1ull << 32) || cb >= (1ull << 32) || crb >= (1ull << 31))
+        return fail(SLM_CAPACITY, "batch too large for one plan");
     // The last row tile of a pair with an odd tile count makes a one-tile item,
     // which leaves half of the epilogue warps idle. Two such tiles of pairs
     // with the same b view and column range share one item.
@@ -381,6 +384,7 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
         return (uint64_t)(x.ct1 - x.ct0) * x.nat > (uint64_t)(y.ct1 - y.ct0) * y.nat;
     });
     p->rows_pad = rb + 2 * kTile;
+    p->cand_rows_pad = crb + 2 * kTile;
     p->cols_pad = cb + kTile;
     p->sl_parts = std::max<uint64_t>(part, 1);
     p->queue_cap = std::max<uint64_t>(p->n_slots, 1) + 64;
@@ -401,8 +405,9 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     SLM_TRY(p->d_colmin.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowthr.ensure(c, sizeof(float) * p->rows_pad));
     SLM_TRY(p->d_colthr.ensure(c, sizeof(float) * p->cols_pad));
-    SLM_TRY(p->d_rowcnt.ensure(c, 2 * sizeof(uint32_t) * p->rows_pad));
-    SLM_TRY(p->d_rowcand.ensure(c, sizeof(uint2) * kSlRowSlots * p->rows_pad));
+    SLM_TRY(p->d_rowcnt.ensure(c, 2 * sizeof(uint32_t) * p->cand_rows_pad));
+    SLM_TRY(p->d_rowrec.ensure(c, sizeof(float4) * kSlRowRecs * p->cand_rows_pad));
+    SLM_TRY(p->d_rowrecj.ensure(c, sizeof(uint32_t) * kSlRowRecs * p->cand_rows_pad));
     SLM_TRY(p->d_colcnt.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowdec.ensure(c, sizeof(uint32_t) * p->rows_pad));
     SLM_TRY(p->d_queue.ensure(c, sizeof(SlQueue) * p->queue_cap));
@@ -477,7 +482,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
     if (p->prec != SLM_PREC_FP32) {
         slm_store *st = p->st;
         launch_fill_u32(p->d_colmin.as<uint32_t>(), p->cols_pad, 0xff800000u, s);  // encodes +inf
-        SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, 2 * sizeof(uint32_t) * p->rows_pad, s));
+        SLM_CU(cudaMemsetAsync(p->d_rowcnt.p, 0, 2 * sizeof(uint32_t) * p->cand_rows_pad, s));
         SLM_CU(cudaMemsetAsync(p->d_colcnt.p, 0, sizeof(uint32_t) * p->cols_pad, s));
         SLM_CU(cudaMemsetAsync(p->d_pairctl.p, 0, 4 * sizeof(uint32_t) * p->np, s));
         SLM_CU(cudaMemsetAsync(p->d_counts.p, 0, sizeof(uint32_t) * p->np, s));  // compact adds its blocks
@@ -498,7 +503,8 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.rowthr = p->d_rowthr.as<float>();
         a.colthr = p->d_colthr.as<float>();
         a.rowcnt = p->d_rowcnt.as<uint32_t>();
-        a.rowcand = p->d_rowcand.as<uint2>();
+        a.rowrec = p->d_rowrec.as<float4>();
+        a.rowrecj = p->d_rowrecj.as<uint32_t>();
         a.colcnt = p->d_colcnt.as<uint32_t>();
         a.rowdec = p->d_rowdec.as<uint32_t>();
         a.queue = p->d_queue.as<SlQueue>();
@@ -1682,19 +1688,29 @@ namespace {
 // Scratch a batch needs (matches plan_build_shortlist's and plan_build's
 // allocations; used for admission).
 uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, slm_precision prec) {
-    uint64_t rows = 0, cols = 0, na = 0, items = 0;
+    uint64_t rows = 0, cols = 0, na = 0, items = 0, supers = 0, cand_rows = 0;
+    for (const slm_pair &p : pairs) {
+        const uint64_t a = p.i < st->n.size() ? st->n[p.i] : 0, b = p.j < st->n.size() ? st->n[p.j] : 0;
+        if (b) supers += (a + 2 * kTile - 1) / (2 * kTile);
+    }
+    // column ranges per pair as plan_build_shortlist splits them (default items per SM)
+    const uint64_t want = (uint64_t)std::max(1, st->ctx->sms) * 3;
+    const uint64_t split = supers && supers < want ? (want + supers - 1) / supers : 1;
     for (const slm_pair &p : pairs) {
         const uint64_t a = p.i < st->n.size() ? st->n[p.i] : 0, b = p.j < st->n.size() ? st->n[p.j] : 0;
         rows += pad_rows(a);
         cols += pad_rows(b);
         na += a;
         items += (pad_rows(a) / kTile + 1) * 4;
+        cand_rows += pad_rows(a) *
+                     std::max<uint64_t>(1, std::min<uint64_t>(std::min<uint64_t>(split, pad_rows(b) / kTile), kSlMaxRanges));
     }
     uint64_t bytes = 64 + pairs.size() * (sizeof(PairMeta) + 16 + 8) + na * 16 + cols * 8;
     if (prec == SLM_PREC_FP32)
         bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
     else
-        bytes += rows * (5 * 4 + kSlRowSlots * 8) + cols * 12 + na * 2 * sizeof(SlQueue) + items * 256 * 12 +
+        bytes += rows * 3 * 4 + cand_rows * (2 * 4 + kSlRowRecs * 20) + cols * 12 + na * 2 * sizeof(SlQueue) +
+                 items * 256 * 12 +
                  pairs.size() * (4 + 16) + (rows / kSlRowBlock + pairs.size()) * 4 +
                  (rows / kTile + 4ull * (uint64_t)std::max(1, st->ctx->sms)) * (sizeof(Item) + sizeof(RowPart) * kTile);
     return bytes + bytes / 4;  // DevBuf growth slack

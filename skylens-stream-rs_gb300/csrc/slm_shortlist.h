@@ -14,9 +14,11 @@
 //   mid                per row: threshold T = m2' + 2 eps, or "certain no
 //                      match" when m1 - eps >= r^2 (m2' + eps); per column:
 //                      threshold c1 + 2 eps.
-//   pass 2  (tcgen05)  recomputes d~; appends (j, d~) with d~ <= T to the row's
-//                      candidate list S and counts, per column, the rows with
-//                      d~ <= c1 + 2 eps (|C|).
+//   pass 2  (tcgen05)  recomputes d~; for every group of 4 consecutive
+//                      columns holding a d~ <= T, appends the group (its first
+//                      column and its 4 values) to the row's records; S = the
+//                      records' columns with d~ <= T. Counts, per column, the
+//                      rows with d~ <= c1 + 2 eps (|C|).
 //   finalize           per row, from S: certain outcomes from the bounds; the
 //                      mutual check from |C| (a row above the column window
 //                      loses, the only row inside it wins). Everything else is
@@ -36,7 +38,8 @@
 //     a minimum within 2 eps above the running row minimum; pass 2 skips
 //     routed pairs;
 //   - after pass 2 (finalize): more than 1/8 as many row halves as rows
-//     overflowed S (pass 2 counts them).
+//     had a wide shortlist, more than kSlHalfRecs / 2 hit groups of one
+//     column range (pass 2 counts them).
 // The routed pairs' exact work items are planned on the device (route_plan,
 // route_apply), run by exact_kernel, and route_finalize writes their rows'
 // decisions; the results stay bit-exact whichever way a pair goes.
@@ -47,8 +50,18 @@
 
 namespace slm {
 
-constexpr int kSlHalfSlots = 16;   // S capacity per row and column half
-constexpr int kSlRowSlots = 2 * kSlHalfSlots;
+// Pass 2 keeps, per row, column range and column half, up to kSlHalfRecs
+// records of 4 consecutive columns (the group's first column and its 4 d~
+// values): one vector store per hit group. A half with more hit groups
+// overflows and the row is settled by an exact scan.
+constexpr int kSlHalfRecs = 16;
+constexpr int kSlRowRecs = 2 * kSlHalfRecs;
+// Routing estimate of a row's shortlist size (in columns).
+constexpr int kSlRowSlots = 32;
+// A pair's columns split into at most this many ranges (items that share its
+// rows); each range keeps its own records per row, so their memory is
+// (rows x ranges) x kSlRowRecs records.
+constexpr uint32_t kSlMaxRanges = 4;
 constexpr int kSlStages = 4;       // b-tile ring depth (FP8; BF16 tiles are larger: 3)
 constexpr int kSlEpWarps = 16;     // epilogue warps
 constexpr int kSlThreads = 32 * (2 + kSlEpWarps);  // producer, MMA, epilogue
@@ -102,7 +115,16 @@ struct SlPair {
     uint32_t xchunk;   // routed: column chunks per 128-row tile
     uint32_t xpart;    // routed: first exact work item (= first RowPart block)
     uint32_t blk;      // first entry of the pair's row blocks in SlArgs::blkcnt
+    uint32_t crbase;   // first candidate row: the records of row i and column range c at
+                       // crbase + c * (na padded to 128) + i (sl_cand_row)
 };
+
+// Candidate row of pair row i in column range c. Each range of a pair's
+// columns (an item's ct0..ct1) keeps its own records per row, so exactly one
+// item writes them and pass 2 needs no atomics for its slots.
+__host__ __device__ inline uint32_t sl_cand_row(const SlPair &sp, uint32_t na, uint32_t c, uint32_t i) {
+    return sp.crbase + c * ((na + kTile - 1) / kTile * kTile) + i;
+}
 
 // The per-pair kernels after pass 1 (mid, finalize, compact, route_finalize)
 // run one CTA per pair and block of this many rows (and columns), so that a
@@ -148,8 +170,9 @@ struct SlArgs {
     uint32_t *colmin;            // pass 1: order-preserving encoding of c1
     float *rowthr;               // mid -> pass 2
     float *colthr;               // mid -> pass 2
-    uint32_t *rowcnt;            // pass 2: two counters per row (column halves)
-    uint2 *rowcand;              // (j, bits(d~))
+    uint32_t *rowcnt;            // pass 2: records per candidate row and column half
+    float4 *rowrec;              // pass 2: a record's 4 d~ values (BF16: d~ / 2), kSlRowRecs per candidate row
+    uint32_t *rowrecj;           // the record's first column
     uint32_t *colcnt;            // |C| per column
     uint32_t *rowdec;            // finalize / rescore / scan
     SlQueue *queue;              // scan queue

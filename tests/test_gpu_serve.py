@@ -50,7 +50,10 @@ def test_serving_within_a_small_hbm_budget():
     z = synth.zone(positions=7, n_range=(150, 900), seed=22)
     reqs = serve.zone_requests(z)
     total = int(z.counts.sum())
-    budget = 48 << 20
+    # store (~12 MB) plus about one batch per slot: a one-request batch of this
+    # zone splits its pairs' columns into up to 4 ranges, each with its own
+    # candidate records per row (about 17 MB of scratch)
+    budget = 96 << 20
     srv = serve.Server(total, len(z.counts), "bf16", slots=3, hbm_budget=budget)
     res, lats, wall = serve.stream_zone(srv, z, rate=None)
     st = srv.stats()
