@@ -122,16 +122,23 @@ SLM_DEV void tmem_wait_ld16(uint32_t (&r)[16]) {
                  : "memory");
 }
 
-// atomicAdd(p, 1) when x <= 0 (not for NaN), without a branch (no return
-// value); the comparison sits in the same block as the predicated red.
-SLM_DEV void red_add1_le0(uint32_t *p, float x) {
+// Column-window counts of 4 consecutive columns (16-byte aligned): adds 1.0
+// to each column whose x <= 0 (not for NaN) with one vector reduction, issued
+// only when pred holds (the group has a hit), without a branch. The counts are
+// f32: exact far beyond any row count (2^24).
+SLM_DEV void red_add4_le0(float *p, float x0, float x1, float x2, float x3, bool pred) {
     asm volatile(
         "{\n"
         ".reg .pred q;\n"
-        "setp.le.f32 q, %1, 0f00000000;\n"
-        "@q red.relaxed.gpu.global.add.u32 [%0], 1;\n"
+        ".reg .f32 a, b, c, d;\n"
+        "set.le.f32.f32 a, %1, 0f00000000;\n"
+        "set.le.f32.f32 b, %2, 0f00000000;\n"
+        "set.le.f32.f32 c, %3, 0f00000000;\n"
+        "set.le.f32.f32 d, %4, 0f00000000;\n"
+        "setp.ne.u32 q, %5, 0;\n"
+        "@q red.relaxed.gpu.global.add.v4.f32 [%0], {a, b, c, d};\n"
         "}\n" ::"l"(p),
-        "f"(x)
+        "f"(x0), "f"(x1), "f"(x2), "f"(x3), "r"((uint32_t)pred)
         : "memory");
 }
 
@@ -732,21 +739,20 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
 #pragma unroll
                                 for (int qq = 0; qq < 4; ++qq) {
                                     if (gr[qq] <= thr_i) {
-                                        const uint32_t sl = rec0 + min(ncand, (uint32_t)kSlHalfRecs - 1);
-                                        st_rec_if(g.rowrec + sl, g.rowrecj + sl, d[4 * qq], d[4 * qq + 1], d[4 * qq + 2],
-                                                  d[4 * qq + 3], j0 + 4 * qq, ncand < kSlHalfRecs);
+                                        // past the capacity the store is predicated off (no access)
+                                        st_rec_if(g.rowrec + (rec0 + ncand), g.rowrecj + (rec0 + ncand), d[4 * qq],
+                                                  d[4 * qq + 1], d[4 * qq + 2], d[4 * qq + 3], j0 + 4 * qq,
+                                                  ncand < kSlHalfRecs);
                                         ++ncand;
                                     }
                                 }
                             }
                             if (xm <= 0.f) {
-                                uint32_t *cc = g.colcnt + sp.cbase + j0;
+                                float *cc = g.colcnt + sp.cbase + j0;
 #pragma unroll
                                 for (int qq = 0; qq < 4; ++qq)
-                                    if (gc[qq] <= 0.f) {
-#pragma unroll
-                                        for (int k = 4 * qq; k < 4 * qq + 4; ++k) red_add1_le0(cc + k, x[k]);
-                                    }
+                                    red_add4_le0(cc + 4 * qq, x[4 * qq], x[4 * qq + 1], x[4 * qq + 2], x[4 * qq + 3],
+                                                 gc[qq] <= 0.f);
                             }
                         }
                     };
@@ -1051,7 +1057,7 @@ SLM_DEV void push_scan(const SlArgs &g, uint32_t pair, uint32_t kind, uint32_t i
 SLM_DEV uint32_t mutual_from_counts(const SlArgs &g, uint32_t p, const SlPair &sp, uint32_t i, uint32_t j, float dij) {
     const uint32_t cidx = sp.cbase + j;
     if (!(dij <= g.colthr[cidx])) return kDecNone;
-    if (g.colcnt[cidx] == 1) return j;
+    if (g.colcnt[cidx] == 1.f) return j;
     push_scan(g, p, 1, i, j);
     return kDecPending;
 }

@@ -505,7 +505,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.rowcnt = p->d_rowcnt.as<uint32_t>();
         a.rowrec = p->d_rowrec.as<float4>();
         a.rowrecj = p->d_rowrecj.as<uint32_t>();
-        a.colcnt = p->d_colcnt.as<uint32_t>();
+        a.colcnt = p->d_colcnt.as<float>();
         a.rowdec = p->d_rowdec.as<uint32_t>();
         a.queue = p->d_queue.as<SlQueue>();
         a.rqueue = p->d_rqueue.as<SlQueue>();

@@ -173,7 +173,7 @@ struct SlArgs {
     uint32_t *rowcnt;            // pass 2: records per candidate row and column half
     float4 *rowrec;              // pass 2: a record's 4 d~ values (BF16: d~ / 2), kSlRowRecs per candidate row
     uint32_t *rowrecj;           // the record's first column
-    uint32_t *colcnt;            // |C| per column
+    float *colcnt;               // |C| per column (f32 counts: exact below 2^24)
     uint32_t *rowdec;            // finalize / rescore / scan
     SlQueue *queue;              // scan queue
     SlQueue *rqueue;             // rescore queue
