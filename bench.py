@@ -332,6 +332,8 @@ def pair_configs(m, steps: int, threads: int) -> list:
                                        "rows_recomputed_frac": s["rows_recomputed"] / len(a),
                                        "cols_recomputed": s["cols_recomputed"],
                                        "pairs_routed": s["pairs_routed"],
+                                       "pairs_rescued": s["pairs_rescued"],
+                                       "settled_frac": settled_frac(s, len(a), prec),
                                        "pass_ms": [float(x) for x in s["pass_ms"]],
                                        "max_err_rescored_vs_f32": s["max_abs_err"]}
             plan.close()
@@ -355,6 +357,17 @@ def pair_configs(m, steps: int, threads: int) -> list:
         print(json.dumps(row), file=sys.stderr, flush=True)
         out.append(row)
     return out
+
+
+def settled_frac(s, na, prec):
+    """Fractions of a single pair's rows settled by each tier: by the FP8 bound,
+    by the BF16 bound (BF16 pairs, and FP8 pairs rescued by the BF16 passes),
+    or with exact FP32 arithmetic (rescored, scanned, or routed whole)."""
+    if prec == "fp32" or na == 0:
+        return {"fp8_bound": 0.0, "bf16_bound": 0.0, "exact": 1.0}
+    exact = min(1.0, (s["rows_rescored"] + s["rows_recomputed"]) / na)
+    bf16 = prec == "bf16" or s["pairs_rescued"] > 0
+    return {"fp8_bound": 0.0 if bf16 else 1.0 - exact, "bf16_bound": 1.0 - exact if bf16 else 0.0, "exact": exact}
 
 
 def run_pairs(args):

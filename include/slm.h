@@ -80,6 +80,9 @@ typedef struct {
     float pass_ms[2];           /* BF16/FP8: tensor-core passes 1 and 2; FP32: [0] = exact kernel */
     uint64_t pairs_routed;      /* BF16/FP8: pairs whose error bound was too loose to certify
                                    their rows, matched whole by the exact FP32 kernel */
+    uint64_t pairs_rescued;     /* FP8: pairs whose FP8 bound was too loose for their distances,
+                                   settled by the BF16 shortlist passes instead */
+    uint64_t rows_rescued;      /* FP8: rows of those pairs */
 } slm_stats;
 
 typedef struct slm_ctx slm_ctx;

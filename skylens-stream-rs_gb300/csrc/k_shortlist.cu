@@ -421,10 +421,17 @@ SLM_DEV bool sl_wait(uint64_t *bar, uint32_t parity, volatile uint32_t *abort_fl
 // Items of two pairs (odd row-tile counts sharing a b view).
 SLM_DEV bool item_two_pairs(const SlItem &it) { return it.nat == 2 && it.pair[1] != it.pair[0]; }
 
-// Pass 2 skips an item when every pair it serves was routed to the exact
-// kernel (all roles read the same flags: mid wrote them).
-SLM_DEV bool item_routed(const SlArgs &g, const SlItem &it) {
-    return g.spairs[it.pair[0]].routed && (it.nat == 1 || g.spairs[it.pair[1]].routed);
+// Whether a pass works on a pair: tier 0's pass 1 on every pair, otherwise
+// the pairs of the tier (sl_pair_on).
+template <int PASS>
+SLM_DEV bool pass_pair_on(const SlArgs &g, const SlPair &sp) {
+    return (PASS == 1 && !g.tier) || sl_pair_on(g, sp);
+}
+// A pass skips an item when none of its pairs is on (all roles read the same
+// flags: earlier kernels wrote them).
+template <int PASS>
+SLM_DEV bool item_off(const SlArgs &g, const SlItem &it) {
+    return !pass_pair_on<PASS>(g, g.spairs[it.pair[0]]) && (it.nat == 1 || !pass_pair_on<PASS>(g, g.spairs[it.pair[1]]));
 }
 
 // One CTA of kSlThreads per SM. Warps are spread over the SM's four
@@ -479,7 +486,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             uint32_t st = 0, sph = 0, iter = 0;  // iter: items processed (routed pairs skip pass 2)
             for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
                 const SlItem item = g.items[it];
-                if (PASS == 2 && item_routed(g, item)) continue;
+                if (item_off<PASS>(g, item)) continue;
                 if (iter > 0 && !sl_wait(&S.a_empty, (iter - 1) & 1, abort_flag, err)) break;
                 const bool two = item_two_pairs(item);
                 const PairMeta pm = g.pairs[item.pair[0]];  // both pairs have this b view
@@ -533,7 +540,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         uint32_t st = 0, sph = 0, tb = 0, tph = 0, iter = 0;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
-            if (PASS == 2 && item_routed(g, item)) continue;
+            if (item_off<PASS>(g, item)) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
             ++iter;
             bool ok = true;
@@ -597,7 +604,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
         constexpr float kDom = FP8 ? 1.f : 2.f;
         for (uint32_t it = blockIdx.x; it < g.n_items; it += gridDim.x) {
             const SlItem item = g.items[it];
-            if (PASS == 2 && item_routed(g, item)) continue;
+            if (item_off<PASS>(g, item)) continue;
             if (!sl_wait(&S.a_full, iter & 1, abort_flag, err)) break;
             ++iter;
             const bool two = item_two_pairs(item);
@@ -611,7 +618,10 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             const uint32_t na0 = g.pairs[item.pair[0]].na, na1 = two ? g.pairs[item.pair[1]].na : na0;
             const uint32_t cb0 = g.spairs[item.pair[0]].cbase, cb1 = two ? g.spairs[item.pair[1]].cbase : cb0;
             // warp-uniform: the warp's a tile exists and its pair is still open
-            const bool active = at < (int)item.nat && !(PASS == 2 && sp.routed);
+            const bool active = at < (int)item.nat && pass_pair_on<PASS>(g, sp);
+            // pass 1: whether each pair of the item is on (column-minimum merge)
+            const bool on0 = pass_pair_on<PASS>(g, g.spairs[item.pair[0]]);
+            const bool on1 = two ? pass_pair_on<PASS>(g, g.spairs[item.pair[1]]) : on0;
             const uint32_t rt = mine1 ? item.rt[1] : item.rt[0];
             const uint32_t mypart = mine1 ? item.part[1] : item.part[0];
             // warp-uniform: this lane quarter holds at least one row of the pair
@@ -809,7 +819,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                 m = fminf(m, S.colpart[tb][cmb][col]);
                         }
                         const uint32_t j = t * kTile + col;
-                        if (j < pm.nb && m < kInf) atomicMin(&g.colmin[(grp ? cb1 : cb0) + j], f2ord(kDom * m));
+                        if (j < pm.nb && m < kInf && (grp ? on1 : on0))
+                            atomicMin(&g.colmin[(grp ? cb1 : cb0) + j], f2ord(kDom * m));
                     }
                 }
                 __syncwarp();
@@ -862,11 +873,10 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
 // Per pair, before pass 1: the error bound eps from the two views'
 // statistics. A pair with non-finite or huge inputs cannot be certified and is
 // routed to the exact kernel.
-__global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= g.npairs) return;
-    const PairMeta pm = g.pairs[p];
-    SlPair &sp = g.spairs[p];
+// The per-pair error bound of this launch's precision (g.fp8) from the two
+// views' statistics; false when the pair cannot be certified (non-finite or
+// huge inputs).
+SLM_DEV bool pair_eps(const SlArgs &g, const SlPair &sp, float *eps_out) {
     const ViewStat va = g.vstats[sp.view_a], vb = g.vstats[sp.view_b];
     const double A = __uint_as_float(va.nmax), B = __uint_as_float(vb.nmax);
     const double Ra = __uint_as_float(va.rho), Rb = __uint_as_float(vb.rho);
@@ -881,10 +891,48 @@ __global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
     // better than 2^-11 relative to that magnitude, doubled with d~
     if (!g.fp8) eps += 5e-4 * (A * A + B * B);
     if (!(eps < 1e30)) unsafe = true;
-    sp.eps = unsafe ? __int_as_float(0x7f800000) : (float)(eps * (1.0 + 1e-6));
+    *eps_out = unsafe ? __int_as_float(0x7f800000) : (float)(eps * (1.0 + 1e-6));
+    return !unsafe;
+}
+
+__global__ void __launch_bounds__(256) sl_eps_kernel(SlArgs g) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= g.npairs) return;
+    const PairMeta pm = g.pairs[p];
+    SlPair &sp = g.spairs[p];
+    float eps;
+    const bool unsafe = !pair_eps(g, sp, &eps);
+    sp.eps = eps;
     sp.unsafe = unsafe ? 1u : 0u;
     sp.routed = (unsafe && pm.na && pm.nb) ? 1u : 0u;
+    sp.rescued = 0;
     if (sp.routed) atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+}
+
+// Tier 1 (the BF16 rescue of an FP8 plan), one CTA per pair and block of
+// kSlRowBlock columns: for each rescued pair, the BF16 bound (block 0), its
+// column minima back to +inf and its per-pair counters back to 0 (tier 0's
+// pass 1 and mid wrote them; its pass 2 skipped the pair, so the records and
+// window counts are still clear).
+__global__ void __launch_bounds__(256) sl_rescue_prep_kernel(SlArgs g) {
+    const uint32_t p = blockIdx.x, blk = blockIdx.y;
+    const PairMeta pm = g.pairs[p];
+    const SlPair sp = g.spairs[p];
+    if (!sl_pair_on(g, sp)) return;  // block-uniform
+    const uint32_t nb_pad = (pm.nb + kTile - 1) / kTile * kTile;
+    const uint32_t c0 = blk * kSlRowBlock, c1 = min(c0 + kSlRowBlock, nb_pad);
+    for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) g.colmin[sp.cbase + j] = 0xff800000u;  // +inf
+    if (blk == 0 && threadIdx.x < 4) g.pairctl[4 * (size_t)p + threadIdx.x] = 0;
+    if (blk == 0 && threadIdx.x == 0) {
+        float eps;
+        if (!pair_eps(g, sp, &eps)) {  // cannot happen after tier 0 (unsafe pairs are routed there)
+            g.spairs[p].routed = 1;
+            atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+        }
+        g.spairs[p].eps = eps;
+        atomicAdd(&g.ctl[kCtlRescuedPairs], 1u);
+        atomicAdd(&g.ctl[kCtlRescuedRows], pm.na);
+    }
 }
 
 // ------------------------------------------------------- certified tests
@@ -935,7 +983,7 @@ __global__ void __launch_bounds__(kThreads) sl_mid_kernel(SlArgs g) {
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
     const uint32_t nblk = pair_blocks(pm);
-    if (sp.routed || blk >= nblk) return;  // block-uniform
+    if (!sl_pair_on(g, sp) || blk >= nblk) return;  // block-uniform
     const float kInf = __int_as_float(0x7f800000);
     if (threadIdx.x == 0) wide_sh = open_sh = 0;
     __syncthreads();
@@ -1020,10 +1068,15 @@ __global__ void __launch_bounds__(kThreads) sl_mid_kernel(SlArgs g) {
         const uint32_t w = atomicAdd(const_cast<uint32_t *>(&pc[kPcWide]), 0u);
         const uint32_t o = atomicAdd(const_cast<uint32_t *>(&pc[kPcOpen]), 0u);
         // more than 1/8 of the undecided rows are expected to overflow their
-        // shortlist: settle the whole pair with the exact kernel
+        // shortlist: settle the whole pair with the BF16 passes (tier 0 of an
+        // FP8 plan) or with the exact kernel
         if (w * 8 > o && o) {
-            g.spairs[p].routed = 1;
-            atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+            if (g.rescue) {
+                g.spairs[p].rescued = 1;
+            } else {
+                g.spairs[p].routed = 1;
+                atomicAdd(&g.ctl[kCtlRouteMarks], 1u);
+            }
         }
     }
 }
@@ -1071,7 +1124,8 @@ __global__ void __launch_bounds__(kThreads, 1) sl_finalize_kernel(SlArgs g) {
     const uint32_t p = blockIdx.x, blk = blockIdx.y;
     const PairMeta pm = g.pairs[p];
     const SlPair sp = g.spairs[p];
-    if (sp.routed || blk * kSlRowBlock >= pm.na) return;  // block-uniform: route_finalize decides its rows
+    // block-uniform: route_finalize decides routed pairs' rows, the other tier its own pairs'
+    if (!sl_pair_on(g, sp) || blk * kSlRowBlock >= pm.na) return;
     const float kInf = __int_as_float(0x7f800000);
     const float eps = sp.eps;
     // every CTA of the pair reads the same total (written by the previous kernel)
@@ -1191,7 +1245,8 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
         // S = the records' columns with d~ <= T, four entries at a time: lane group
         // grp computes queued entry grp, every lane merges the results in order
         const float T = g.rowthr[ridx];
-        const float dom = g.fp8 ? 1.f : 2.f;
+        // records of FP8 pairs hold d~, those of BF16 (and rescued) pairs d~ / 2
+        const float dom = g.fp8 && !sp.rescued ? 1.f : 2.f;
         uint32_t qj = 0, nq = 0;  // this lane group's queued column (0: a valid placeholder)
         float qv = kInf;
         auto flush = [&](uint32_t cnt) {
@@ -1638,14 +1693,26 @@ int launch_shortlist_mid(const SlArgs &a, cudaStream_t s) {
     return 1;
 }
 
-int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
+int launch_shortlist_finalize(const SlArgs &a, cudaStream_t s) {
     if (!a.npairs) return 0;
-    const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
     const dim3 per_block(a.npairs, a.row_blocks);  // CTA per pair and row block
     if (a.npairs <= kFewPairs)
         sl_finalize_kernel<1024><<<per_block, 1024, 0, s>>>(a);
     else
         sl_finalize_kernel<256><<<per_block, 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_shortlist_rescue_prep(const SlArgs &a, cudaStream_t s) {
+    if (!a.npairs) return 0;
+    sl_rescue_prep_kernel<<<dim3(a.npairs, a.row_blocks), 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
+    if (!a.npairs) return 0;
+    const unsigned rgrid = (unsigned)(a.npairs < (uint32_t)(4 * sms) ? a.npairs : (uint32_t)(4 * sms));
+    const dim3 per_block(a.npairs, a.row_blocks);  // CTA per pair and row block
     // routed pairs: plan, exact kernel over all their rows and columns, decisions
     sl_route_plan_kernel<<<1, 1024, 0, s>>>(a);
     sl_route_apply_kernel<<<rgrid, 256, 0, s>>>(a);
@@ -1671,7 +1738,7 @@ int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s) {
     sl_rescore_kernel<<<5 * sms, 256, 0, s>>>(a);  // 40 warps per SM: latency-bound gathers
     sl_scan_kernel<<<2 * sms, 256, 0, s>>>(a);
     sl_compact_kernel<<<per_block, 256, 0, s>>>(a);
-    return a.fp8 ? 8 : 9;
+    return a.fp8 ? 7 : 8;
 }
 
 }  // namespace slm

@@ -183,17 +183,20 @@ struct slm_store {
     std::vector<uint32_t> row0, n;
     uint64_t rows_used = 0;
     uint64_t version = 0;   // bumps when views are added or cleared
-    // Low-precision operand images for the shortlist path, rebuilt lazily
-    // when the views change (lowp_version != version) or the format changes.
-    int lowp_fp8 = -1;
-    uint64_t lowp_version = ~0ull;
-    uint64_t epoch = 0, lowp_epoch = ~0ull;  // epoch bumps on clear
-    size_t lowp_views = 0;                   // views whose images are built
+    uint64_t epoch = 0;                      // bumps on clear
+    // Low-precision operand images for the shortlist path, [0] BF16 and [1]
+    // FP8 (an FP8 plan also reads the BF16 image: pairs the FP8 bound cannot
+    // settle are rescued by the BF16 passes). Each is built lazily: only the
+    // views appended since its last build, all of them after a clear.
+    struct LowpImage {
+        uint64_t version = ~0ull, epoch = ~0ull;
+        size_t views = 0;                    // views whose images are built
+        DevBuf optiles, norms, qscale, vstats;
+    } lowp[2];
     uint64_t fp32_epoch = ~0ull;             // FP32 tiles, built lazily the same way
     size_t fp32_views = 0;
     DevBuf tiletab;                          // {row0, n, tile, view} per tile to pack
     DevBuf staging;                          // slm_store_add_views: the host rows, before the scatter
-    DevBuf optiles, norms, qscale, vstats;
 };
 
 // ---------------------------------------------------------------------- plan
@@ -226,7 +229,7 @@ struct slm_plan {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the main kernel(s)
     cudaEvent_t evp[3] = {nullptr, nullptr, nullptr};  // shortlist: after pass 1, mid, pass 2
     uint64_t kernels = 0;                      // kernels per launch
-    void *graph_optiles = nullptr;             // store buffers the captured graph reads
+    void *graph_optiles[2] = {nullptr, nullptr};  // store buffers the captured graph reads
     void *graph_tiled = nullptr;
     bool launched = false;
     ~slm_plan() {
@@ -487,11 +490,12 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         SLM_CU(cudaMemsetAsync(p->d_pairctl.p, 0, 4 * sizeof(uint32_t) * p->np, s));
         SLM_CU(cudaMemsetAsync(p->d_counts.p, 0, sizeof(uint32_t) * p->np, s));  // compact adds its blocks
         SlArgs a{};
-        a.optiles = st->optiles.as<uint8_t>();
-        a.norms = st->norms.as<float>();
+        const slm_store::LowpImage &im = st->lowp[p->prec == SLM_PREC_FP8 ? 1 : 0];
+        a.optiles = im.optiles.as<uint8_t>();
+        a.norms = im.norms.as<float>();
         a.raw = st->raw.as<float>();
-        a.qscale = p->prec == SLM_PREC_FP8 ? st->qscale.as<float>() : nullptr;
-        a.vstats = st->vstats.as<ViewStat>();
+        a.qscale = p->prec == SLM_PREC_FP8 ? im.qscale.as<float>() : nullptr;
+        a.vstats = im.vstats.as<ViewStat>();
         a.pairs = p->d_meta.as<PairMeta>();
         a.spairs = p->d_spairs.as<SlPair>();
         a.npairs = p->np;
@@ -527,6 +531,8 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.xparts = p->d_xparts.as<RowPart>();
         a.colbest = p->d_colbest.as<unsigned long long>();
         a.want_items = 4u * (uint32_t)std::max(1, p->ctx->sms);
+        a.rescue = p->prec == SLM_PREC_FP8 ? 1u : 0u;
+        a.tier = 0;
         int nk = 1;  // the colmin fill
         SLM_CU(record_event(p->ev0, s));
         nk += launch_shortlist_eps(a, s);
@@ -536,6 +542,26 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         SLM_CU(record_event(p->evp[1], s));
         nk += launch_shortlist_pass(a, 2, p->ctx->sms, s);
         SLM_CU(record_event(p->evp[2], s));
+        nk += launch_shortlist_finalize(a, s);
+        if (a.rescue) {
+            // tier 1: the BF16 passes over the pairs FP8 could not settle (their
+            // kernels return at once when no pair was rescued)
+            SlArgs b = a;
+            const slm_store::LowpImage &bi = st->lowp[0];
+            b.optiles = bi.optiles.as<uint8_t>();
+            b.norms = bi.norms.as<float>();
+            b.qscale = nullptr;
+            b.vstats = bi.vstats.as<ViewStat>();
+            b.fp8 = 0;
+            b.dump = nullptr;
+            b.rescue = 0;
+            b.tier = 1;
+            nk += launch_shortlist_rescue_prep(b, s);
+            nk += launch_shortlist_pass(b, 1, p->ctx->sms, s);
+            nk += launch_shortlist_mid(b, s);
+            nk += launch_shortlist_pass(b, 2, p->ctx->sms, s);
+            nk += launch_shortlist_finalize(b, s);
+        }
         nk += launch_shortlist_tail(a, p->ctx->sms, s);
         SLM_CU(record_event(p->ev1, s));
         p->kernels = (uint64_t)nk + 2;  // + scan_counts, gather
@@ -739,6 +765,8 @@ slm_status fill_stats(slm_plan *p, slm_stats *st, uint64_t matches, const uint32
         st->rows_recomputed = (uint64_t)w[kCtlQueueRows] + w[kCtlRoutedRows];
         st->cols_recomputed = (uint64_t)w[kCtlQueueCols] + w[kCtlRoutedCols];
         st->pairs_routed = w[kCtlRoutedPairs];
+        st->pairs_rescued = w[kCtlRescuedPairs];
+        st->rows_rescued = w[kCtlRescuedRows];
         float e;
         std::memcpy(&e, &w[kCtlMaxErr], sizeof(e));
         st->max_abs_err = e;
@@ -1010,32 +1038,39 @@ slm_status store_sync_fp32(slm_store *st, cudaStream_t s) {
     return SLM_OK;
 }
 
-// Build the store's low-precision operand images: only the views appended
-// since the last build, unless the store was cleared or the format changed.
+// Build one of the store's low-precision operand images: only the views
+// appended since its last build, unless the store was cleared.
 slm_status store_sync_lowp(slm_store *st, bool fp8, cudaStream_t s) {
-    if (st->lowp_version == st->version && st->lowp_fp8 == (int)fp8) return SLM_OK;
+    slm_store::LowpImage &im = st->lowp[fp8 ? 1 : 0];
+    if (im.version == st->version) return SLM_OK;
     slm_ctx *c = st->ctx;
     const uint64_t tiles = std::max<uint64_t>(st->max_rows / kTile, 1);
     const size_t tb = fp8 ? kFp8TileBytes : kBf16TileStride;
-    const bool fresh = st->lowp_fp8 != (int)fp8 || st->lowp_epoch != st->epoch;
-    size_t first = fresh ? 0 : st->lowp_views;
-    SLM_TRY(st->optiles.ensure(c, tiles * tb));
-    SLM_TRY(st->norms.ensure(c, tiles * kTile * sizeof(float)));
-    if (fp8) SLM_TRY(st->qscale.ensure(c, tiles * kTile * sizeof(float)));
+    size_t first = im.epoch != st->epoch ? 0 : im.views;
+    SLM_TRY(im.optiles.ensure(c, tiles * tb));
+    SLM_TRY(im.norms.ensure(c, tiles * kTile * sizeof(float)));
+    if (fp8) SLM_TRY(im.qscale.ensure(c, tiles * kTile * sizeof(float)));
     const size_t nv = std::max<size_t>({st->row0.size(), (size_t)st->max_views, 1});
-    if (st->vstats.bytes < nv * sizeof(ViewStat)) first = 0;  // grows: statistics are rebuilt
-    SLM_TRY(st->vstats.ensure(c, nv * sizeof(ViewStat)));
+    if (im.vstats.bytes < nv * sizeof(ViewStat)) first = 0;  // grows: statistics are rebuilt
+    SLM_TRY(im.vstats.ensure(c, nv * sizeof(ViewStat)));
     if (first < st->row0.size())
-        SLM_CU(cudaMemsetAsync(st->vstats.as<ViewStat>() + first, 0, (st->row0.size() - first) * sizeof(ViewStat), s));
+        SLM_CU(cudaMemsetAsync(im.vstats.as<ViewStat>() + first, 0, (st->row0.size() - first) * sizeof(ViewStat), s));
     uint32_t nt = 0;
     SLM_TRY(upload_tiletab(st, first, st->row0.size(), s, &nt));
-    launch_pack_lowp(st->tiletab.as<uint4>(), nt, st->raw.as<float>(), fp8 ? 1 : 0, st->optiles.as<uint8_t>(),
-                     st->norms.as<float>(), st->qscale.as<float>(), st->vstats.as<ViewStat>(), s);
+    launch_pack_lowp(st->tiletab.as<uint4>(), nt, st->raw.as<float>(), fp8 ? 1 : 0, im.optiles.as<uint8_t>(),
+                     im.norms.as<float>(), im.qscale.as<float>(), im.vstats.as<ViewStat>(), s);
     SLM_CU(cudaGetLastError());
-    st->lowp_version = st->version;
-    st->lowp_fp8 = fp8 ? 1 : 0;
-    st->lowp_epoch = st->epoch;
-    st->lowp_views = st->row0.size();
+    im.version = st->version;
+    im.epoch = st->epoch;
+    im.views = st->row0.size();
+    return SLM_OK;
+}
+
+// The images a plan of this precision reads: BF16 for BF16 plans, both for
+// FP8 plans (the BF16 passes rescue the pairs the FP8 bound cannot settle).
+slm_status store_sync_plan_images(slm_store *st, slm_precision prec, cudaStream_t s) {
+    if (prec == SLM_PREC_BF16 || prec == SLM_PREC_FP8) SLM_TRY(store_sync_lowp(st, false, s));
+    if (prec == SLM_PREC_FP8) SLM_TRY(store_sync_lowp(st, true, s));
     return SLM_OK;
 }
 
@@ -1065,21 +1100,22 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
     // pairs of unit descriptors to the exact kernel); a BF16 batch packs the
     // tiles of its few routed pairs' views itself, on the device
     if (prec != SLM_PREC_BF16) SLM_TRY(store_sync_fp32(st, stream));
-    if (prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(st, prec == SLM_PREC_FP8, stream));
+    SLM_TRY(store_sync_plan_images(st, prec, stream));
     return plan_build(p, pairs);
 }
 
 slm_status plan_launch_on(slm_plan *p, cudaStream_t s, bool use_graph) {
     if (p->prec != SLM_PREC_BF16) SLM_TRY(store_sync_fp32(p->st, s));
-    if (p->prec != SLM_PREC_FP32) SLM_TRY(store_sync_lowp(p->st, p->prec == SLM_PREC_FP8, s));
+    SLM_TRY(store_sync_plan_images(p->st, p->prec, s));
     // a store buffer the captured graph reads may have moved: capture again
-    if (p->exec && (p->st->tiled.p != p->graph_tiled ||
-                    (p->prec != SLM_PREC_FP32 && p->st->optiles.p != p->graph_optiles))) {
+    if (p->exec && (p->st->tiled.p != p->graph_tiled || p->st->lowp[0].optiles.p != p->graph_optiles[0] ||
+                    p->st->lowp[1].optiles.p != p->graph_optiles[1])) {
         cudaGraphExecDestroy(p->exec);
         p->exec = nullptr;
     }
     p->graph_tiled = p->st->tiled.p;
-    p->graph_optiles = p->st->optiles.p;
+    p->graph_optiles[0] = p->st->lowp[0].optiles.p;
+    p->graph_optiles[1] = p->st->lowp[1].optiles.p;
     if (!p->ev0) SLM_CU(cudaEventCreate(&p->ev0));
     if (!p->ev1) SLM_CU(cudaEventCreate(&p->ev1));
     for (cudaEvent_t &e : p->evp)
@@ -1814,8 +1850,7 @@ void serve_loop(slm_server *srv) {
             {
                 slm_status ls = SLM_OK;
                 if (srv->opts.prec != SLM_PREC_BF16) ls = store_sync_fp32(srv->store, srv->ctx->stream);
-                if (ls == SLM_OK && srv->opts.prec != SLM_PREC_FP32)
-                    ls = store_sync_lowp(srv->store, srv->opts.prec == SLM_PREC_FP8, srv->ctx->stream);
+                if (ls == SLM_OK) ls = store_sync_plan_images(srv->store, srv->opts.prec, srv->ctx->stream);
                 if (ls != SLM_OK) {
                     for (ServeRequest *r : take) serve_fail_request(r, ls);
                     srv->cv_done.notify_all();

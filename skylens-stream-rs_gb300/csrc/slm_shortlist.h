@@ -115,6 +115,7 @@ struct SlPair {
     uint32_t xchunk;   // routed: column chunks per 128-row tile
     uint32_t xpart;    // routed: first exact work item (= first RowPart block)
     uint32_t blk;      // first entry of the pair's row blocks in SlArgs::blkcnt
+    uint32_t rescued;  // per launch (FP8 plans): settled by the BF16 passes instead
     uint32_t crbase;   // first candidate row: the records of row i and column range c at
                        // crbase + c * (na padded to 128) + i (sl_cand_row)
 };
@@ -148,7 +149,7 @@ struct SlQueue {
 // Counters in the plan's control block (u32 words after work/error).
 enum : int { kCtlRescored = 2, kCtlQueueRows = 3, kCtlQueueCols = 4, kCtlMaxErr = 5, kCtlScanLen = 6,
              kCtlRescoreLen = 7, kCtlXItems = 8, kCtlXWork = 9, kCtlRoutedPairs = 10, kCtlRoutedRows = 11,
-             kCtlRoutedCols = 12, kCtlRouteMarks = 13 };
+             kCtlRoutedCols = 12, kCtlRouteMarks = 13, kCtlRescuedPairs = 14, kCtlRescuedRows = 15 };
 
 // Routed pairs: at most this many column chunks per 128-row tile; the exact
 // items of a launch number at most (routed row tiles) + (4 x SMs).
@@ -196,7 +197,19 @@ struct SlArgs {
     RowPart *xparts;             // one 128-row block per item
     unsigned long long *colbest; // by PairMeta::col_base
     uint32_t want_items;         // exact items wanted to fill the GPU (4 x SMs)
+    // FP8 plans: pairs the FP8 bound cannot settle (mid: too many wide rows) are
+    // rescued by a second, BF16 run of eps / pass 1 / mid / pass 2 / finalize
+    // over those pairs only (tier 1), instead of the exact kernel
+    uint32_t rescue;             // tier 0 of an FP8 plan: mid marks pairs rescued, not routed
+    uint32_t tier;               // 0: the plan's precision; 1: the BF16 rescue of an FP8 plan
 };
+
+// Whether a pair takes part in this tier's per-pair kernels (pass 2, finalize,
+// and, in tier 1, everything): tier 0 skips pairs routed to the exact kernel or
+// rescued by tier 1; tier 1 runs the rescued pairs only.
+__host__ __device__ inline bool sl_pair_on(const SlArgs &g, const SlPair &sp) {
+    return g.tier ? (sp.rescued && !sp.routed) : !(sp.routed || sp.rescued);
+}
 
 // Store-side builder: one CTA per entry {first store row of the view, rows,
 // tile within the view, view} of the tile table.
@@ -212,6 +225,10 @@ cudaError_t init_shortlist_kernels();
 int launch_shortlist_eps(const SlArgs &a, cudaStream_t s);
 int launch_shortlist_pass(const SlArgs &a, int pass, int sms, cudaStream_t s);
 int launch_shortlist_mid(const SlArgs &a, cudaStream_t s);
+int launch_shortlist_finalize(const SlArgs &a, cudaStream_t s);
+// Tier 1 before its pass 1: the rescued pairs' BF16 eps, column minima and counters.
+int launch_shortlist_rescue_prep(const SlArgs &a, cudaStream_t s);
+// After every tier's finalize: routing to the exact kernel, rescore, scans, compaction.
 int launch_shortlist_tail(const SlArgs &a, int sms, cudaStream_t s);
 // Dense results of a shortlist launch: pair p's row blocks in order, pairs
 // with counts[p] == 0 (none, or filtered out) skipped.

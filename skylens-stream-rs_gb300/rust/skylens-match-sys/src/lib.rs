@@ -43,6 +43,8 @@ pub struct slm_stats {
     pub kernel_launches: u64,
     pub pass_ms: [f32; 2],
     pub pairs_routed: u64,
+    pub pairs_rescued: u64,
+    pub rows_rescued: u64,
 }
 
 #[repr(C)]

@@ -27,7 +27,7 @@ class SlmStats(ctypes.Structure):
     _fields_ = [("pairs", c_u64), ("distances", c_u64), ("matches", c_u64), ("rows_recomputed", c_u64),
                 ("cols_recomputed", c_u64), ("rows_rescored", c_u64), ("kernel_ms", c_f32),
                 ("max_abs_err", c_f32), ("kernel_launches", c_u64), ("pass_ms", c_f32 * 2),
-                ("pairs_routed", c_u64)]
+                ("pairs_routed", c_u64), ("pairs_rescued", c_u64), ("rows_rescued", c_u64)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_}
