@@ -245,7 +245,9 @@ def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32"
     reqs = serve.zone_requests(z)
     out = {"metric": "serving: image pairs/s and p50/p99 request latency (view arrival -> match lists on host)",
            "config": {"workload": "serve_zone144", "views": len(z.counts), "pairs": int(len(z.pairs)),
-                      "n": "log-uniform [500, 4000]", "arrivals": "Poisson", "slots": 3}, "runs": []}
+                      "n": "log-uniform [500, 4000]", "arrivals": "Poisson", "slots": 3,
+                      "submission": "slm_server_submit_ptr: each view's rows read where they lie on admission"},
+           "runs": []}
     check = {}
     for prec in prec_list:
         for rate in [None if r == "burst" else float(r) for r in rates.split(",")]:

@@ -299,7 +299,9 @@ typedef struct {
     uint64_t max_descs;       /* store capacity (descriptors) */
     uint32_t max_views;       /* store capacity (views) */
     uint32_t slots;           /* concurrent batches (streams); 0: 3 */
-    uint32_t max_batch_pairs; /* image pairs per batch; 0: 4096 */
+    uint32_t max_batch_pairs; /* image pairs per batch; 0: 256 (batches of about 0.5 ms of BF16 work on
+                                 views of ~1700 descriptors: under a backlog, batches pipeline over the
+                                 slots instead of one large batch finishing last) */
     uint32_t tick_us;         /* batching tick; 0: 200 us */
     float ratio;              /* Lowe ratio (0.8 in the pipeline) */
     int mutual;
@@ -325,6 +327,15 @@ slm_status slm_server_destroy(slm_server *srv);
  * earlier submission. Returns the view's id and a ticket. */
 slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs, uint32_t np,
                              uint32_t *view_id, uint64_t *ticket);
+/* slm_server_submit without the copy (no reference counterpart: a client that
+ * already holds the view's descriptors, e.g. the feature cache of
+ * pipeline.rs:2614-2651, saves a host copy per request). desc is read where it
+ * lies when the request is admitted (by the device directly where it can read
+ * host memory and desc is 16-byte aligned, else by a copy); the caller keeps it
+ * valid and unchanged until slm_server_wait returns for the ticket (also after
+ * slm_server_cancel). */
+slm_status slm_server_submit_ptr(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs, uint32_t np,
+                                 uint32_t *view_id, uint64_t *ticket);
 /* Wait up to timeout_ms (0: poll) for a ticket. SLM_TIMEOUT if not done yet.
  * On completion copies pair k's matches to out[offsets[k] .. offsets[k+1])
  * (offsets has np+1 entries) and the request's latency (submit -> results on

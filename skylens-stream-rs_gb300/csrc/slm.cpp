@@ -9,6 +9,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -114,6 +115,35 @@ struct slm_ctx {
         cudaFree(p);
         used.fetch_sub(bytes);
     }
+    // Stream-ordered allocations from the context's pool, for buffers that one
+    // stream uses (a plan's): freeing one orders after that stream's earlier
+    // work instead of synchronising the device as cudaFree does, so a plan that
+    // grows does not stall the work of other streams (serving slots).
+    cudaMemPool_t pool = nullptr;
+    slm_status alloc_ordered(void **p, size_t bytes, cudaStream_t s) {
+        *p = nullptr;
+        if (bytes == 0) return SLM_OK;
+        uint64_t now = used.fetch_add(bytes) + bytes;
+        if (budget && now > budget) {
+            used.fetch_sub(bytes);
+            return fail(SLM_OOM, "HBM budget exceeded: need " + std::to_string(now) + " > budget " +
+                                     std::to_string(budget) + " bytes");
+        }
+        cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, s);
+        if (e != cudaSuccess) {
+            used.fetch_sub(bytes);
+            cudaGetLastError();
+            *p = nullptr;
+            return fail(SLM_OOM, std::string("cudaMallocFromPoolAsync(") + std::to_string(bytes) +
+                                     "): " + cudaGetErrorString(e));
+        }
+        return SLM_OK;
+    }
+    void release_ordered(void *p, size_t bytes, cudaStream_t s) {
+        if (!p) return;
+        cudaFreeAsync(p, s);
+        used.fetch_sub(bytes);
+    }
 };
 
 // A named range on the calling thread for profilers that read NVTX (nsys,
@@ -130,22 +160,39 @@ struct DevBuf {
     slm_ctx *ctx = nullptr;
     void *p = nullptr;
     size_t bytes = 0;
+    cudaStream_t ord = nullptr;  // set: allocated from the context's pool, ordered on this stream
+    bool pooled = false;         // p came from the pool
+    // Owners whose buffer one stream uses call this before ensure().
+    void order_on(cudaStream_t s) {
+        if (s == ord) return;
+        if (p && pooled) cudaStreamSynchronize(ord);  // the old stream's work is done before a later free
+        ord = s;
+    }
     slm_status ensure(slm_ctx *c, size_t need) {
         ctx = c;
         if (need <= bytes) return SLM_OK;
-        ctx->release(p, bytes);
-        p = nullptr;
-        bytes = 0;
+        free_();
         size_t want = need + need / 4;
-        SLM_TRY(ctx->alloc(&p, want));
+        if (ord && ctx->pool)
+            SLM_TRY(ctx->alloc_ordered(&p, want, ord));
+        else
+            SLM_TRY(ctx->alloc(&p, want));
+        pooled = ord && ctx->pool;
         bytes = want;
         return SLM_OK;
     }
-    void reset() {
-        if (ctx) ctx->release(p, bytes);
+    void free_() {
+        if (ctx && p) {
+            if (pooled)
+                ctx->release_ordered(p, bytes, ord);
+            else
+                ctx->release(p, bytes);
+        }
         p = nullptr;
         bytes = 0;
+        pooled = false;
     }
+    void reset() { free_(); }
     template <class T>
     T *as() const {
         return static_cast<T *>(p);
@@ -241,6 +288,21 @@ struct slm_plan {
             if (e) cudaEventDestroy(e);
     }
 };
+
+// Every device buffer of a plan: all are used on the plan's stream only, and
+// allocated ordered on it (DevBuf::order_on).
+std::array<DevBuf *, 29> plan_buffers(slm_plan *p) {
+    return {&p->d_meta, &p->d_items, &p->d_parts, &p->d_colbest, &p->d_slots, &p->d_counts, &p->d_ctl,
+            &p->d_offsets, &p->d_dense, &p->d_sitems, &p->d_spairs, &p->d_rowpart, &p->d_rownear,
+            &p->d_colmin, &p->d_rowthr, &p->d_colthr, &p->d_rowcnt, &p->d_rowrec, &p->d_rowrecj,
+            &p->d_colcnt, &p->d_rowdec, &p->d_queue, &p->d_rqueue, &p->d_dump, &p->d_xlist, &p->d_xitems,
+            &p->d_xparts, &p->d_blkcnt, &p->d_pairctl};
+}
+// Frees a plan's buffers while its stream still exists (their frees are
+// ordered on it): owners call it before destroying that stream.
+void plan_release(slm_plan *p) {
+    for (DevBuf *b : plan_buffers(p)) b->reset();
+}
 
 // Dense compaction of per-pair slots (device) into out + offsets.
 namespace slm {
@@ -858,6 +920,20 @@ extern "C" slm_status slm_ctx_create(const slm_opts *opts, slm_ctx **out) {
     }
     const char *no_direct = std::getenv("SLM_NO_HOST_DIRECT");
     c->host_direct = pageable == 1 && !(no_direct && no_direct[0] == '1');
+    {
+        // the pool keeps up to 1 GiB of freed plan buffers for reuse
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = dev;
+        uint64_t keep = 1ull << 30;
+        if (cudaMemPoolCreate(&c->pool, &pp) != cudaSuccess ||
+            cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+            cudaGetLastError();
+            if (c->pool) cudaMemPoolDestroy(c->pool);
+            c->pool = nullptr;  // plans then allocate with cudaMalloc
+        }
+    }
     *out = c;
     return SLM_OK;
 }
@@ -868,11 +944,13 @@ extern "C" slm_status slm_ctx_destroy(slm_ctx *c) {
     coalescer_destroy(c);
     cudaDeviceSynchronize();
     for (Workspace *w : c->all) {
+        plan_release(&w->plan);
         if (w->stream) cudaStreamDestroy(w->stream);
         if (w->single_host) cudaFreeHost(w->single_host);
         delete w;
     }
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (c->pool) cudaMemPoolDestroy(c->pool);
     delete c;
     return SLM_OK;
 }
@@ -915,6 +993,13 @@ extern "C" slm_status slm_store_create(slm_ctx *c, uint64_t max_descs, uint32_t 
         return s;
     }
     st->max_rows = rows;
+    // the packing kernels' tile table, at its largest size once (a buffer that
+    // grew later would be freed with a device-wide synchronisation)
+    s = st->tiletab.ensure(c, std::max<uint64_t>(rows / kTile, 1) * sizeof(uint4));
+    if (s != SLM_OK) {
+        delete st;
+        return s;
+    }
     *out = st;
     return SLM_OK;
 }
@@ -1078,6 +1163,7 @@ slm_status plan_init(slm_plan *p, slm_ctx *c, slm_store *st, const slm_pair *pai
                      int mutual, slm_precision prec, const slm_tune *tune, cudaStream_t stream) {
     p->ctx = c;
     p->stream = stream;
+    for (DevBuf *b : plan_buffers(p)) b->order_on(stream);
     p->st = st;
     p->np = np;
     p->ratio = ratio;
@@ -1680,7 +1766,10 @@ using Clock = std::chrono::steady_clock;
 struct ServeRequest {
     uint64_t ticket = 0;
     uint32_t view = 0;
-    std::vector<float> desc;         // host copy until uploaded
+    std::vector<float> desc;         // host copy (slm_server_submit), kept until the batch is done
+    const float *src = nullptr;      // the view's rows: desc.data(), or the caller's (slm_server_submit_ptr)
+    uint32_t n = 0;                  // rows of the view
+    bool dropped = false;            // cancelled while queued: uploaded (later requests may name it), no pairs
     std::vector<slm_pair> pairs;     // SLM_SELF resolved to `view`
     std::vector<slm_pair> matches;   // results, pair order
     std::vector<uint64_t> offsets;   // np + 1
@@ -1696,8 +1785,35 @@ struct ServeSlot {
     cudaEvent_t done = nullptr;
     slm_plan plan;
     std::vector<ServeRequest *> reqs;
+    uint32_t np = 0;                 // pairs of the running batch (0: uploads of dropped requests only)
     bool busy = false;
+    slm_pair *pin = nullptr;         // pinned staging of a finished batch's matches (grows)
+    uint64_t pin_cap = 0;
+    ~ServeSlot() {
+        if (pin) cudaFreeHost(pin);
+    }
 };
+
+// A finished batch's matches and per-pair offsets into the slot's pinned
+// staging: only the matches the batch found cross the link, in one copy.
+slm_status serve_read_results(ServeSlot *s, std::vector<uint64_t> &off) {
+    slm_plan *p = &s->plan;
+    SLM_CU(cudaStreamSynchronize(p->stream));
+    SLM_TRY(check_status_word(p));
+    off.resize(p->np + 1);
+    SLM_CU(cudaMemcpy(off.data(), p->d_offsets.p, sizeof(uint64_t) * (p->np + 1), cudaMemcpyDeviceToHost));
+    const uint64_t total = off[p->np];
+    if (total > s->pin_cap) {
+        if (s->pin) cudaFreeHost(s->pin);
+        s->pin = nullptr;
+        s->pin_cap = 0;
+        const uint64_t want = total + total / 2;
+        SLM_CU(cudaMallocHost(reinterpret_cast<void **>(&s->pin), sizeof(slm_pair) * want));
+        s->pin_cap = want;
+    }
+    if (total) SLM_CU(cudaMemcpy(s->pin, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost));
+    return SLM_OK;
+}
 
 }  // namespace
 
@@ -1715,6 +1831,7 @@ struct slm_server {
     uint64_t next_ticket = 1;
     uint32_t next_view = 0;
     uint64_t slot_budget = 0;
+    std::vector<uint32_t> view_n;       // rows of every submitted view, by view id (admission)
     bool stop = false;
     slm_server_stats stats{};
 };
@@ -1723,17 +1840,18 @@ namespace {
 
 // Scratch a batch needs (matches plan_build_shortlist's and plan_build's
 // allocations; used for admission).
-uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, slm_precision prec) {
+uint64_t batch_bytes(const slm_store *st, const std::vector<uint32_t> &vn, const std::vector<slm_pair> &pairs,
+                     slm_precision prec) {
     uint64_t rows = 0, cols = 0, na = 0, items = 0, supers = 0, cand_rows = 0;
     for (const slm_pair &p : pairs) {
-        const uint64_t a = p.i < st->n.size() ? st->n[p.i] : 0, b = p.j < st->n.size() ? st->n[p.j] : 0;
+        const uint64_t a = p.i < vn.size() ? vn[p.i] : 0, b = p.j < vn.size() ? vn[p.j] : 0;
         if (b) supers += (a + 2 * kTile - 1) / (2 * kTile);
     }
     // column ranges per pair as plan_build_shortlist splits them (default items per SM)
     const uint64_t want = (uint64_t)std::max(1, st->ctx->sms) * 3;
     const uint64_t split = supers && supers < want ? (want + supers - 1) / supers : 1;
     for (const slm_pair &p : pairs) {
-        const uint64_t a = p.i < st->n.size() ? st->n[p.i] : 0, b = p.j < st->n.size() ? st->n[p.j] : 0;
+        const uint64_t a = p.i < vn.size() ? vn[p.i] : 0, b = p.j < vn.size() ? vn[p.j] : 0;
         rows += pad_rows(a);
         cols += pad_rows(b);
         na += a;
@@ -1752,14 +1870,43 @@ uint64_t batch_bytes(const slm_store *st, const std::vector<slm_pair> &pairs, sl
     return bytes + bytes / 4;  // DevBuf growth slack
 }
 
-void serve_fail_request(ServeRequest *r, slm_status s) {
+void serve_fail_request(ServeRequest *r, slm_status s, const std::string &error) {
     r->status = s;
-    r->error = g_last_error;
+    r->error = error;
     r->done = true;
     r->t_done = Clock::now();
+    std::vector<slm_pair>().swap(r->matches);
+    std::vector<uint64_t>().swap(r->offsets);
 }
 
-// Worker: collect finished batches, then admit pending requests into free slots.
+// The views of a batch's requests, in submission order (their ids were given
+// at submit): one gather launch that reads every view where it lies when the
+// device can read host memory directly and the rows are 16-byte aligned, else
+// one copy per view. On the store's stream.
+slm_status serve_upload(slm_server *srv, const std::vector<ServeRequest *> &take) {
+    slm_store *st = srv->store;
+    bool direct = srv->ctx->host_direct;
+    for (const ServeRequest *r : take) direct &= (reinterpret_cast<uintptr_t>(r->src) & 15u) == 0;
+    std::vector<uint32_t> ids(take.size());
+    if (direct) {
+        std::vector<const float *> src(take.size());
+        std::vector<uint32_t> n(take.size());
+        for (size_t k = 0; k < take.size(); ++k) src[k] = take[k]->src, n[k] = take[k]->n;
+        SLM_TRY(store_append_direct(st, take.size(), src.data(), n.data(), ids.data(), srv->ctx->stream));
+    } else {
+        for (size_t k = 0; k < take.size(); ++k)
+            SLM_TRY(store_append(st, take[k]->src, take[k]->n, false, srv->ctx->stream, &ids[k]));
+    }
+    for (size_t k = 0; k < take.size(); ++k)
+        if (ids[k] != take[k]->view) return fail(SLM_INTERNAL, "serving: view ids out of order");
+    return SLM_OK;
+}
+
+// Worker: collect finished batches, then admit pending requests into free
+// slots. The lock is held only to move requests between the queue and the
+// slots and to publish results: uploads, planning, launches and result copies
+// run without it, so clients submit and wait meanwhile, and the requests that
+// arrive while the worker is busy make the next batch larger.
 void serve_loop(slm_server *srv) {
     cudaSetDevice(srv->ctx->device);
     std::unique_lock<std::mutex> lk(srv->mu);
@@ -1778,100 +1925,110 @@ void serve_loop(slm_server *srv) {
             for (ServeSlot *s : srv->slots) busy |= s->busy;
             if (!busy && srv->pending.empty()) break;
         }
-        // 1. completions
+        // 1. completions: results copied out without the lock, published with it
+        std::vector<ServeSlot *> fin;
         for (ServeSlot *s : srv->slots) {
-            if (!s->busy || cudaEventQuery(s->done) != cudaSuccess) continue;
-            cudaGetLastError();
-            const uint32_t np = s->plan.np;
-            std::vector<uint64_t> off(np + 1);
-            std::vector<slm_pair> out(std::max<uint64_t>(s->plan.n_slots, 1));
-            slm_stats st{};
-            const slm_status rs = slm_plan_results(&s->plan, out.data(), out.size(), off.data(), &st);
-            uint32_t k = 0;
-            for (ServeRequest *r : s->reqs) {
-                if (rs != SLM_OK || r->cancelled) {
-                    if (r->cancelled) g_last_error = "request cancelled";
-                    serve_fail_request(r, r->cancelled ? SLM_CANCELLED : rs);
-                    k += (uint32_t)r->pairs.size();
+            if (!s->busy) continue;
+            if (cudaEventQuery(s->done) == cudaSuccess) fin.push_back(s);
+            cudaGetLastError();  // cudaErrorNotReady
+        }
+        if (!fin.empty()) {
+            lk.unlock();
+            std::vector<slm_status> rs(fin.size(), SLM_OK);
+            std::vector<std::string> err(fin.size());
+            for (size_t f = 0; f < fin.size(); ++f) {
+                ServeSlot *s = fin[f];
+                if (!s->np) {  // requests without pairs (the first views of a zone)
+                    for (ServeRequest *r : s->reqs) r->offsets.assign(1, 0), r->matches.clear();
                     continue;
                 }
-                r->offsets.assign(1, 0);
-                for (size_t q = 0; q < r->pairs.size(); ++q, ++k) {
-                    r->matches.insert(r->matches.end(), out.begin() + off[k], out.begin() + off[k + 1]);
-                    r->offsets.push_back(r->matches.size());
+                std::vector<uint64_t> off;
+                rs[f] = serve_read_results(s, off);
+                if (rs[f] != SLM_OK) {
+                    err[f] = g_last_error;
+                    continue;
                 }
-                r->done = true;
-                r->t_done = Clock::now();
-                srv->stats.completed++;
-                srv->stats.matches += r->matches.size();
+                uint32_t k = 0;
+                for (ServeRequest *r : s->reqs) {
+                    if (r->dropped) continue;
+                    const uint64_t b0 = off[k];
+                    r->matches.assign(s->pin + b0, s->pin + off[k + r->pairs.size()]);
+                    r->offsets.resize(r->pairs.size() + 1);
+                    for (size_t q = 0; q <= r->pairs.size(); ++q) r->offsets[q] = off[k + q] - b0;
+                    k += (uint32_t)r->pairs.size();
+                }
             }
-            s->reqs.clear();
-            s->busy = false;
+            lk.lock();
+            for (size_t f = 0; f < fin.size(); ++f) {
+                ServeSlot *s = fin[f];
+                for (ServeRequest *r : s->reqs) {
+                    std::vector<float>().swap(r->desc);  // the upload has read it
+                    if (r->cancelled || r->dropped)
+                        serve_fail_request(r, SLM_CANCELLED, "request cancelled");
+                    else if (rs[f] != SLM_OK)
+                        serve_fail_request(r, rs[f], err[f]);
+                    else {
+                        r->done = true;
+                        r->t_done = Clock::now();
+                        srv->stats.completed++;
+                        srv->stats.matches += r->matches.size();
+                    }
+                }
+                s->reqs.clear();
+                s->busy = false;
+            }
+            srv->cv_done.notify_all();
         }
-        srv->cv_done.notify_all();
         // 2. admission: FIFO into each free slot while the batch fits
         for (ServeSlot *s : srv->slots) {
             if (s->busy || srv->pending.empty()) continue;
             std::vector<ServeRequest *> take;
             std::vector<slm_pair> pairs;
-            // upload views of requests about to be admitted (ordered on the store's stream)
             while (!srv->pending.empty()) {
                 ServeRequest *r = srv->pending.front();
-                if (!take.empty() && pairs.size() + r->pairs.size() > srv->opts.max_batch_pairs) break;
-                if (!r->uploaded) {
-                    uint32_t id = 0;
-                    const slm_status us = store_append(srv->store, r->desc.data(), (uint32_t)(r->desc.size() / kDesc),
-                                                       false, srv->ctx->stream, &id);
-                    if (us != SLM_OK) {
-                        srv->pending.pop_front();
-                        serve_fail_request(r, us);
-                        continue;
-                    }
-                    r->uploaded = true;
-                    std::vector<float>().swap(r->desc);
+                if (r->cancelled) {
+                    r->dropped = true;  // its view is still added to the store (later requests may name it)
+                } else {
+                    if (!pairs.empty() && pairs.size() + r->pairs.size() > srv->opts.max_batch_pairs) break;
+                    std::vector<slm_pair> trial = pairs;
+                    trial.insert(trial.end(), r->pairs.begin(), r->pairs.end());
+                    if (!pairs.empty() && batch_bytes(srv->store, srv->view_n, trial, srv->opts.prec) > srv->slot_budget)
+                        break;
+                    pairs.swap(trial);
                 }
-                if (r->cancelled) {  // its view stays in the store; its pairs are dropped
-                    srv->pending.pop_front();
-                    g_last_error = "request cancelled";
-                    serve_fail_request(r, SLM_CANCELLED);
-                    srv->cv_done.notify_all();
-                    continue;
-                }
-                std::vector<slm_pair> trial = pairs;
-                trial.insert(trial.end(), r->pairs.begin(), r->pairs.end());
-                if (!take.empty() && batch_bytes(srv->store, trial, srv->opts.prec) > srv->slot_budget) break;
-                pairs.swap(trial);
                 take.push_back(r);
                 srv->pending.pop_front();
             }
             if (take.empty()) continue;
-            // FP32 tiles and low-precision images of the new views, on the
-            // upload stream, so every slot that waits for the upload sees them.
-            {
-                slm_status ls = SLM_OK;
-                if (srv->opts.prec != SLM_PREC_BF16) ls = store_sync_fp32(srv->store, srv->ctx->stream);
-                if (ls == SLM_OK) ls = store_sync_plan_images(srv->store, srv->opts.prec, srv->ctx->stream);
-                if (ls != SLM_OK) {
-                    for (ServeRequest *r : take) serve_fail_request(r, ls);
-                    srv->cv_done.notify_all();
-                    continue;
-                }
+            lk.unlock();
+            // the new views, their FP32 tiles and low-precision images on the
+            // store's stream, so every slot that waits for the upload sees them
+            slm_status ps = serve_upload(srv, take);
+            if (ps == SLM_OK && srv->opts.prec != SLM_PREC_BF16) ps = store_sync_fp32(srv->store, srv->ctx->stream);
+            if (ps == SLM_OK) ps = store_sync_plan_images(srv->store, srv->opts.prec, srv->ctx->stream);
+            if (ps == SLM_OK && cudaEventRecord(srv->upload_done, srv->ctx->stream) != cudaSuccess)
+                ps = fail(SLM_CUDA_ERROR, "cudaEventRecord");
+            if (ps == SLM_OK && cudaStreamWaitEvent(s->stream, srv->upload_done, 0) != cudaSuccess)
+                ps = fail(SLM_CUDA_ERROR, "cudaStreamWaitEvent");
+            if (ps == SLM_OK && !pairs.empty()) {
+                slm_tune t{};
+                t.use_graph = 2;
+                ps = plan_init(&s->plan, srv->ctx, srv->store, pairs.data(), (uint32_t)pairs.size(), srv->opts.ratio,
+                               srv->opts.mutual, srv->opts.prec, &t, s->stream);
+                if (ps == SLM_OK) ps = plan_launch_on(&s->plan, s->stream, false);
             }
-            cudaEventRecord(srv->upload_done, srv->ctx->stream);
-            cudaStreamWaitEvent(s->stream, srv->upload_done, 0);
-            slm_tune t{};
-            t.use_graph = 2;
-            slm_status ps = plan_init(&s->plan, srv->ctx, srv->store, pairs.data(), (uint32_t)pairs.size(),
-                                      srv->opts.ratio, srv->opts.mutual, srv->opts.prec, &t, s->stream);
-            if (ps == SLM_OK) ps = plan_launch_on(&s->plan, s->stream, false);
             if (ps == SLM_OK && cudaEventRecord(s->done, s->stream) != cudaSuccess)
                 ps = fail(SLM_CUDA_ERROR, "cudaEventRecord");
+            const std::string err = ps == SLM_OK ? std::string() : g_last_error;
+            if (ps != SLM_OK) cudaStreamSynchronize(srv->ctx->stream);  // no upload still reads a request's rows
+            lk.lock();
             if (ps != SLM_OK) {
-                for (ServeRequest *r : take) serve_fail_request(r, ps);
+                for (ServeRequest *r : take) serve_fail_request(r, ps, err);
                 srv->cv_done.notify_all();
                 continue;
             }
             s->reqs = take;
+            s->np = (uint32_t)pairs.size();
             s->busy = true;
             srv->stats.batches++;
             srv->stats.pairs += pairs.size();
@@ -1894,7 +2051,7 @@ extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server 
     if (!srv) return fail(SLM_OOM, "host allocation failed");
     srv->opts = *opts;
     if (!srv->opts.slots) srv->opts.slots = 3;
-    if (!srv->opts.max_batch_pairs) srv->opts.max_batch_pairs = 4096;
+    if (!srv->opts.max_batch_pairs) srv->opts.max_batch_pairs = 256;
     if (!srv->opts.tick_us) srv->opts.tick_us = 200;
     slm_opts co{};
     co.device = opts->device;
@@ -1921,6 +2078,19 @@ extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server 
     const uint64_t used = srv->ctx->used.load();
     const uint64_t left = srv->ctx->budget > used ? srv->ctx->budget - used : 0;
     srv->slot_budget = left / srv->opts.slots;
+    // Map the slots' scratch into the context's pool now (up to the 1 GiB it
+    // keeps): the first batches then take their buffers from memory already
+    // mapped instead of growing the pool while other slots run.
+    if (srv->ctx->pool) {
+        void *warm = nullptr;
+        const uint64_t want = std::min<uint64_t>(left, 1ull << 30);
+        if (want && srv->ctx->alloc_ordered(&warm, want, srv->ctx->stream) == SLM_OK) {
+            srv->ctx->release_ordered(warm, want, srv->ctx->stream);
+            cudaStreamSynchronize(srv->ctx->stream);
+        }
+        g_last_error.clear();
+        cudaGetLastError();
+    }
     srv->worker = std::thread(serve_loop, srv);
     *out = srv;
     return SLM_OK;
@@ -1948,6 +2118,7 @@ extern "C" slm_status slm_server_destroy(slm_server *srv) {
             s->plan.ev1 = nullptr;
         }
         if (s->done) cudaEventDestroy(s->done);
+        plan_release(&s->plan);
         if (s->stream) cudaStreamDestroy(s->stream);
         delete s;
     }
@@ -1959,12 +2130,19 @@ extern "C" slm_status slm_server_destroy(slm_server *srv) {
     return SLM_OK;
 }
 
-extern "C" slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs,
-                                        uint32_t np, uint32_t *view_id, uint64_t *ticket) {
+namespace {
+slm_status server_submit(slm_server *srv, const float *desc, uint32_t n, bool copy, const slm_pair *pairs,
+                         uint32_t np, uint32_t *view_id, uint64_t *ticket) {
     if (!srv || (n && !desc) || (np && !pairs) || !ticket) return fail(SLM_INVALID_ARG, "NULL argument");
     auto *r = new (std::nothrow) ServeRequest();
     if (!r) return fail(SLM_OOM, "host allocation failed");
-    r->desc.assign(desc, desc + (size_t)n * kDesc);
+    if (copy) {
+        r->desc.assign(desc, desc + (size_t)n * kDesc);
+        r->src = r->desc.data();
+    } else {
+        r->src = desc;
+    }
+    r->n = n;
     r->t_submit = Clock::now();
     std::lock_guard<std::mutex> g(srv->mu);
     if (srv->next_view >= srv->opts.max_views) {
@@ -1982,6 +2160,7 @@ extern "C" slm_status slm_server_submit(slm_server *srv, const float *desc, uint
         }
         r->pairs.push_back(p);
     }
+    srv->view_n.push_back(n);
     srv->next_view++;
     r->ticket = srv->next_ticket++;
     srv->reqs[r->ticket] = r;
@@ -1991,6 +2170,17 @@ extern "C" slm_status slm_server_submit(slm_server *srv, const float *desc, uint
     *ticket = r->ticket;
     srv->cv_work.notify_all();
     return SLM_OK;
+}
+}  // namespace
+
+extern "C" slm_status slm_server_submit(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs,
+                                        uint32_t np, uint32_t *view_id, uint64_t *ticket) {
+    return server_submit(srv, desc, n, true, pairs, np, view_id, ticket);
+}
+
+extern "C" slm_status slm_server_submit_ptr(slm_server *srv, const float *desc, uint32_t n, const slm_pair *pairs,
+                                            uint32_t np, uint32_t *view_id, uint64_t *ticket) {
+    return server_submit(srv, desc, n, false, pairs, np, view_id, ticket);
 }
 
 extern "C" slm_status slm_server_wait(slm_server *srv, uint64_t ticket, uint32_t timeout_ms, slm_pair *out,
@@ -2287,6 +2477,7 @@ void coal_stop(slm_ctx *c) {
     for (CoalSlot &s : co->slots) {
         if (s.w.stream) cudaStreamSynchronize(s.w.stream);
         if (s.done) cudaEventDestroy(s.done);
+        plan_release(&s.w.plan);
         if (s.w.stream) cudaStreamDestroy(s.w.stream);
         s.w.stream = nullptr;
     }

@@ -115,6 +115,8 @@ SIGNATURES = {
     "slm_server_create": (c_int, [P(SlmServerOpts), P(ctypes.c_void_p)]),
     "slm_server_destroy": (c_int, [ctypes.c_void_p]),
     "slm_server_submit": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, P(SlmPair), c_u32, P(c_u32), P(c_u64)]),
+    "slm_server_submit_ptr": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, P(SlmPair), c_u32, P(c_u32),
+                                      P(c_u64)]),
     "slm_server_wait": (c_int, [ctypes.c_void_p, c_u64, c_u32, P(SlmPair), c_u64, P(c_u64),
                                 P(ctypes.c_double)]),
     "slm_server_stats_get": (c_int, [ctypes.c_void_p, P(SlmServerStats)]),

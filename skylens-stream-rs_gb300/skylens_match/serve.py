@@ -24,7 +24,7 @@ class Server:
     """libslm serving engine on one GPU."""
 
     def __init__(self, max_descs: int, max_views: int, precision="bf16", ratio: float = 0.8, mutual: bool = True,
-                 slots: int = 3, max_batch_pairs: int = 4096, tick_us: int = 200, device: int = 0,
+                 slots: int = 3, max_batch_pairs: int = 0, tick_us: int = 200, device: int = 0,
                  hbm_budget: int = 0):
         self._L = load()
         o = SlmServerOpts(device, hbm_budget, max_descs, max_views, slots, max_batch_pairs, tick_us,
@@ -33,33 +33,43 @@ class Server:
         check(self._L.slm_server_create(ctypes.byref(o), ctypes.byref(h)), "slm_server_create")
         self._h = h
         self._np = {}
+        self._keep = {}  # arrays of copy=False submissions, until their wait returns
 
-    def submit(self, desc, pairs) -> tuple[int, int]:
-        """Add one view and request the listed pairs (use SELF for this view)."""
+    def submit(self, desc, pairs, copy: bool = True) -> tuple[int, int]:
+        """Add one view and request the listed pairs (use SELF for this view).
+        copy=False (slm_server_submit_ptr): the rows are read where they lie
+        when the request is admitted; this object keeps the array alive until
+        the ticket's wait returns."""
         d = _desc(desc)
         pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.uint32).reshape(-1, 2))
         vid, t = ctypes.c_uint32(), ctypes.c_uint64()
-        check(self._L.slm_server_submit(self._h, ctypes.c_void_p(d.ctypes.data), len(d),
-                                        pr.ctypes.data_as(ctypes.POINTER(SlmPair)), len(pr), ctypes.byref(vid),
-                                        ctypes.byref(t)), "slm_server_submit")
+        fn = self._L.slm_server_submit if copy else self._L.slm_server_submit_ptr
+        check(fn(self._h, ctypes.c_void_p(d.ctypes.data), len(d), pr.ctypes.data_as(ctypes.POINTER(SlmPair)),
+                 len(pr), ctypes.byref(vid), ctypes.byref(t)), "slm_server_submit")
         self._np[t.value] = len(pr)
+        if not copy:
+            self._keep[t.value] = d
         return vid.value, t.value
 
     def wait(self, ticket: int, cap: int, timeout_s: float = 120.0):
         """(per-pair match arrays, latency ms); cap bounds the total matches."""
-        np_ = self._np.pop(ticket)
-        out = (SlmPair * max(cap, 1))()
+        np_ = self._np[ticket]
+        out = np.empty((max(cap, 1), 2), np.uint32)
         off = np.empty(np_ + 1, np.uint64)
         lat = ctypes.c_double()
         deadline = time.monotonic() + timeout_s
         while True:
-            st = self._L.slm_server_wait(self._h, ticket, 1000, out, max(cap, 1),
-                                         off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), ctypes.byref(lat))
+            st = self._L.slm_server_wait(self._h, ticket, 1000, out.ctypes.data_as(ctypes.POINTER(SlmPair)),
+                                         max(cap, 1), off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                         ctypes.byref(lat))
             if st != SLM_TIMEOUT or time.monotonic() > deadline:
                 break
+        if st != SLM_TIMEOUT:  # the ticket is released: its rows are no longer read
+            self._np.pop(ticket, None)
+            self._keep.pop(ticket, None)
         check(st, "slm_server_wait")
-        flat = np.frombuffer(out, dtype=np.uint32, count=2 * int(off[-1])).reshape(-1, 2)
-        return [flat[int(off[k]):int(off[k + 1])].copy() for k in range(np_)], lat.value
+        # per-pair views of one array (no copies)
+        return [out[int(off[k]):int(off[k + 1])] for k in range(np_)], lat.value
 
     def cancel(self, ticket: int) -> None:
         """slm_server_cancel: the request's pairs are dropped (or its results
@@ -92,10 +102,12 @@ def zone_requests(z: synth.Zone):
     return [(v, by_v.get(v, [])) for v in range(len(z.counts))]
 
 
-def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0):
+def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0, copy: bool = False):
     """Submit the zone's views with Poisson arrivals at `rate` views/s (None:
     all at once) and collect every result. Returns (results per view, latencies
-    ms, wall seconds from first submit to last result)."""
+    ms, wall seconds from first submit to last result). copy=False submits the
+    zone's rows where they lie (slm_server_submit_ptr), copy=True copies each
+    view at submission (slm_server_submit)."""
     reqs = zone_requests(z)
     rng = np.random.Generator(np.random.PCG64(seed))
     gaps = rng.exponential(1.0 / rate, size=len(reqs)) if rate else np.zeros(len(reqs))
@@ -110,11 +122,15 @@ def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0):
             dt = t - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            tickets[k] = srv.submit(z.view(v), pairs)[1]
+            tickets[k] = srv.submit(z.view(v), pairs, copy=copy)[1]
             ready.release()
 
-    th = threading.Thread(target=producer)
-    th.start()
+    if rate:
+        th = threading.Thread(target=producer)
+        th.start()
+    else:  # all at once: every submission before the first wait (no thread to share the interpreter with)
+        producer()
+        th = None
     results, lats = [], []
     for k, (v, pairs) in enumerate(reqs):
         ready.acquire()
@@ -122,7 +138,8 @@ def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0):
         results.append(res)
         lats.append(lat)
     wall = time.perf_counter() - t0
-    th.join()
+    if th is not None:
+        th.join()
     return results, np.asarray(lats), wall
 
 
