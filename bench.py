@@ -248,29 +248,34 @@ def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32"
                       "n": "log-uniform [500, 4000]", "arrivals": "Poisson", "slots": 3,
                       "submission": "slm_server_submit_ptr: each view's rows read where they lie on admission"},
            "runs": []}
-    check = {}
+    # every run back to back (the GPU stays busy between them), then the
+    # oracle's check of every 9th request of each run
+    npairs = sum(len(p) for _, p in reqs)
+    done = []
     for prec in prec_list:
         for rate in [None if r == "burst" else float(r) for r in rates.split(",")]:
             srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
             res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
             st = srv.stats()
             srv.close()
-            npairs = sum(len(p) for _, p in reqs)
-            mism = 0
-            for k in range(0, len(reqs), 9):
-                v, pairs = reqs[k]
-                for (u, _), got in zip(pairs, res[k]):
-                    key = (u, v)
-                    if key not in check:
-                        check[key] = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=threads)
-                    mism += not np.array_equal(got, check[key])
-            out["runs"].append({"precision": prec, "rate_views_per_s": rate if rate else "burst",
-                                "p50_ms": float(np.percentile(lats, 50)),
-                                "p99_ms": float(np.percentile(lats, 99)), "mean_ms": float(lats.mean()),
-                                "pairs_per_s": npairs / wall, "wall_s": wall, "batches": st["batches"],
-                                "max_batch_requests": st["max_batch_requests"], "max_inflight": st["max_inflight"],
-                                "bit_exact_sample_mismatches": int(mism)})
-            print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
+            done.append((prec, rate, res, lats, wall, st))
+    check = {}
+    for prec, rate, res, lats, wall, st in done:
+        mism = 0
+        for k in range(0, len(reqs), 9):
+            v, pairs = reqs[k]
+            for (u, _), got in zip(pairs, res[k]):
+                key = (u, v)
+                if key not in check:
+                    check[key] = O.ratio_match_np(z.view(u), z.view(v), 0.8, True, threads=threads)
+                mism += not np.array_equal(got, check[key])
+        out["runs"].append({"precision": prec, "rate_views_per_s": rate if rate else "burst",
+                            "p50_ms": float(np.percentile(lats, 50)),
+                            "p99_ms": float(np.percentile(lats, 99)), "mean_ms": float(lats.mean()),
+                            "pairs_per_s": npairs / wall, "wall_s": wall, "batches": st["batches"],
+                            "max_batch_requests": st["max_batch_requests"], "max_inflight": st["max_inflight"],
+                            "bit_exact_sample_mismatches": int(mism)})
+        print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
     return out
 
 

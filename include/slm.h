@@ -215,7 +215,8 @@ uint32_t slm_store_num_views(slm_store *st);
 /* Tuning knobs; zero fields take the autotuned or default values. */
 typedef struct {
     uint32_t items_per_sm;  /* FP32: target work items per SM when splitting columns */
-    uint32_t shortlist_k;   /* shortlist slots per row (BF16/FP8) */
+    uint32_t shortlist_k;   /* BF16/FP8: shortlist capacity, records of 4-column hit groups per
+                               row, column range and column half, 1..32 (0: 16) */
     uint32_t use_graph;     /* 1: replay a captured CUDA graph (default), 2: plain launches */
     uint32_t variant;       /* FP32: 0 packed f32x2 arithmetic (default), 1 all
                                scalar; both IEEE, bit-exact.
@@ -226,8 +227,9 @@ typedef struct {
                                (slm_autotune), tuning it first if none is cached */
 } slm_tune;
 
-/* Time a small grid of settings (row tiles per item, items per SM, FP32
- * arithmetic variant) on this batch with CUDA events and return the fastest in
+/* Time a grid of settings on this batch with CUDA events (FP32: items per SM
+ * {2, 4, 8} x arithmetic variant; BF16/FP8: items per SM {2, 4, 8} x row tiles
+ * per work item {1, 2} x shortlist_k {8, 12, 16}) and return the fastest in
  * *best (and its time in *best_ms). The result is cached in the context under
  * the batch's shape (precision, mean rows per pair, pair count), which plans
  * with slm_tune.autotune = 1 use. Launches the batch several times. */

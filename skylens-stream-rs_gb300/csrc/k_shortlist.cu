@@ -643,7 +643,8 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
             // pass 2: the records of this row and of the item's column range
             // (exactly one item writes them: plain stores, a running count)
             const uint32_t crow = PASS == 2 ? sl_cand_row(sp, pm.na, (mypart - sp.part_base) % sp.nchunk, i) : 0;
-            const uint32_t rec0 = crow * kSlRowRecs + h * kSlHalfRecs;
+            const uint32_t hr = g.half_recs;
+            const uint32_t rec0 = (2 * crow + h) * hr;
             uint32_t ncand = 0;
             bool ok = true;
             for (uint32_t t = item.ct0; t < item.ct1; ++t) {
@@ -752,7 +753,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                                         // past the capacity the store is predicated off (no access)
                                         st_rec_if(g.rowrec + (rec0 + ncand), g.rowrecj + (rec0 + ncand), d[4 * qq],
                                                   d[4 * qq + 1], d[4 * qq + 2], d[4 * qq + 3], j0 + 4 * qq,
-                                                  ncand < kSlHalfRecs);
+                                                  ncand < hr);
                                         ++ncand;
                                     }
                                 }
@@ -854,7 +855,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     g.rowcnt[2 * crow + h] = ncand;
                     // a wide shortlist (more than half the records): the pair's bound may be
                     // too loose for its distances (routing estimate of finalize)
-                    if (ncand > kSlHalfRecs / 2) atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
+                    if (ncand > hr / 2) atomicAdd(&g.pairctl[4 * (size_t)pid + kPcOver], 1u);
                 }
             }
         }
@@ -1153,11 +1154,11 @@ __global__ void __launch_bounds__(kThreads, 1) sl_finalize_kernel(SlArgs g) {
             for (uint32_t l = 0; l < 2 * sp.nchunk; ++l) {
                 const uint32_t cr = sl_cand_row(sp, pm.na, l >> 1, i);
                 const uint32_t nl = g.rowcnt[2 * cr + (l & 1)];
-                over |= nl > kSlHalfRecs;
-                const uint32_t b0 = cr * kSlRowRecs + (l & 1) * kSlHalfRecs;
+                over |= nl > g.half_recs;
+                const uint32_t b0 = (2 * cr + (l & 1)) * g.half_recs;
                 // two records per step, loaded before they are used
-                for (uint32_t r = 0; r < nl && r < kSlHalfRecs; r += 2) {
-                    const bool two = r + 1 < nl && r + 1 < kSlHalfRecs;
+                for (uint32_t r = 0; r < nl && r < g.half_recs; r += 2) {
+                    const bool two = r + 1 < nl && r + 1 < g.half_recs;
                     const float4 v0 = g.rowrec[b0 + r];
                     const uint32_t jb0 = g.rowrecj[b0 + r];
                     const float4 v1 = two ? g.rowrec[b0 + r + 1] : make_float4(kInf, kInf, kInf, kInf);
@@ -1272,7 +1273,7 @@ __global__ void __launch_bounds__(256) sl_rescore_kernel(SlArgs g) {
         for (uint32_t l = 0; l < 2 * sp.nchunk; ++l) {
             const uint32_t cr = sl_cand_row(sp, pm.na, l >> 1, qe.i);
             const uint32_t nl = g.rowcnt[2 * cr + (l & 1)];
-            const uint32_t b0 = cr * kSlRowRecs + (l & 1) * kSlHalfRecs;
+            const uint32_t b0 = (2 * cr + (l & 1)) * g.half_recs;
             for (uint32_t r = 0; r < nl; ++r) {
                 const float4 v4 = g.rowrec[b0 + r];
                 const uint32_t jb = g.rowrecj[b0 + r];

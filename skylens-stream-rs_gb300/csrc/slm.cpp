@@ -265,6 +265,7 @@ struct slm_plan {
     // shortlist path
     std::vector<SlItem> sitems;
     std::vector<SlPair> spairs;
+    uint32_t half_recs = kSlHalfRecs;  // records per candidate row and column half
     uint64_t rows_pad = 0, cand_rows_pad = 0, cols_pad = 0, sl_parts = 0, queue_cap = 0, xitem_cap = 0, row_blocks_total = 0;
     uint32_t row_blocks = 1;  // the most row blocks of any pair
     DevBuf d_sitems, d_spairs, d_rowpart, d_rownear, d_colmin, d_rowthr, d_colthr, d_rowcnt, d_rowrec, d_rowrecj, d_colcnt,
@@ -471,8 +472,9 @@ slm_status plan_build_shortlist(slm_plan *p, const slm_pair *pairs) {
     SLM_TRY(p->d_rowthr.ensure(c, sizeof(float) * p->rows_pad));
     SLM_TRY(p->d_colthr.ensure(c, sizeof(float) * p->cols_pad));
     SLM_TRY(p->d_rowcnt.ensure(c, 2 * sizeof(uint32_t) * p->cand_rows_pad));
-    SLM_TRY(p->d_rowrec.ensure(c, sizeof(float4) * kSlRowRecs * p->cand_rows_pad));
-    SLM_TRY(p->d_rowrecj.ensure(c, sizeof(uint32_t) * kSlRowRecs * p->cand_rows_pad));
+    p->half_recs = p->tune.shortlist_k ? p->tune.shortlist_k : kSlHalfRecs;
+    SLM_TRY(p->d_rowrec.ensure(c, sizeof(float4) * 2 * p->half_recs * p->cand_rows_pad));
+    SLM_TRY(p->d_rowrecj.ensure(c, sizeof(uint32_t) * 2 * p->half_recs * p->cand_rows_pad));
     SLM_TRY(p->d_colcnt.ensure(c, sizeof(uint32_t) * p->cols_pad));
     SLM_TRY(p->d_rowdec.ensure(c, sizeof(uint32_t) * p->rows_pad));
     SLM_TRY(p->d_queue.ensure(c, sizeof(SlQueue) * p->queue_cap));
@@ -570,6 +572,7 @@ slm_status plan_enqueue(slm_plan *p, cudaStream_t s) {
         a.colthr = p->d_colthr.as<float>();
         a.rowcnt = p->d_rowcnt.as<uint32_t>();
         a.rowrec = p->d_rowrec.as<float4>();
+        a.half_recs = p->half_recs;
         a.rowrecj = p->d_rowrecj.as<uint32_t>();
         a.colcnt = p->d_colcnt.as<float>();
         a.rowdec = p->d_rowdec.as<uint32_t>();
@@ -1253,19 +1256,26 @@ extern "C" slm_status slm_autotune(slm_ctx *c, slm_store *st, const slm_pair *pa
     SLM_TRY(validate_ratio(ratio));
     SLM_TRY(ctx_check_device(c));
     prec = resolve_prec(prec, prec == SLM_PREC_AUTO ? batch_distances(st, pairs, np) : 0);
+    // FP32: items per SM x arithmetic variant; BF16/FP8: items per SM x the
+    // M tile shape (128-row a tiles per CTA work item, M = 128 or 256) x the
+    // shortlist capacity (records of 4-column hit groups per row and column half)
     std::vector<slm_tune> grid;
     const uint32_t ips[3] = {2, 4, 8};
+    const uint32_t ks[3] = {8, 12, 16};
     for (uint32_t a = 0; a < 2; ++a)
-        for (uint32_t ipsm : ips) {
-            slm_tune t{};
-            t.use_graph = 2;
-            t.items_per_sm = ipsm;
-            if (prec == SLM_PREC_FP32)
-                t.variant = a;  // 0 packed f32x2 sub/add, 1 scalar
-            else
-                t.row_tiles = a + 1;
-            grid.push_back(t);
-        }
+        for (uint32_t ki = 0; ki < (prec == SLM_PREC_FP32 ? 1u : 3u); ++ki)
+            for (uint32_t ipsm : ips) {
+                slm_tune t{};
+                t.use_graph = 2;
+                t.items_per_sm = ipsm;
+                if (prec == SLM_PREC_FP32) {
+                    t.variant = a;  // 0 packed f32x2 sub/add, 1 scalar
+                } else {
+                    t.row_tiles = a + 1;
+                    t.shortlist_k = ks[ki];
+                }
+                grid.push_back(t);
+            }
     std::unique_ptr<slm_plan> p(new (std::nothrow) slm_plan());
     if (!p) return fail(SLM_OOM, "host allocation failed");
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1326,6 +1336,8 @@ extern "C" slm_status slm_plan_create(slm_ctx *c, slm_store *st, const slm_pair 
         if (tune && tune->use_graph) t.use_graph = tune->use_graph;
         t.autotune = 0;
     }
+    if (t.shortlist_k > kSlHalfRecsMax)
+        return fail(SLM_INVALID_ARG, "shortlist_k must be at most " + std::to_string(kSlHalfRecsMax));
     auto *p = new (std::nothrow) slm_plan();
     if (!p) return fail(SLM_OOM, "host allocation failed");
     slm_status s = plan_init(p, c, st, pairs, np, ratio, mutual, prec, &t, c->stream);
@@ -1863,7 +1875,7 @@ uint64_t batch_bytes(const slm_store *st, const std::vector<uint32_t> &vn, const
     if (prec == SLM_PREC_FP32)
         bytes += items * (sizeof(Item) + sizeof(RowPart) * kTile);
     else
-        bytes += rows * 3 * 4 + cand_rows * (2 * 4 + kSlRowRecs * 20) + cols * 12 + na * 2 * sizeof(SlQueue) +
+        bytes += rows * 3 * 4 + cand_rows * (2 * 4 + 2 * kSlHalfRecs * 20) + cols * 12 + na * 2 * sizeof(SlQueue) +
                  items * 256 * 12 +
                  pairs.size() * (4 + 16) + (rows / kSlRowBlock + pairs.size()) * 4 +
                  (rows / kTile + 4ull * (uint64_t)std::max(1, st->ctx->sms)) * (sizeof(Item) + sizeof(RowPart) * kTile);

@@ -38,7 +38,7 @@
 //     a minimum within 2 eps above the running row minimum; pass 2 skips
 //     routed pairs;
 //   - after pass 2 (finalize): more than 1/8 as many row halves as rows
-//     had a wide shortlist, more than kSlHalfRecs / 2 hit groups of one
+//     had a wide shortlist, more than half_recs / 2 hit groups of one
 //     column range (pass 2 counts them).
 // The routed pairs' exact work items are planned on the device (route_plan,
 // route_apply), run by exact_kernel, and route_finalize writes their rows'
@@ -50,17 +50,18 @@
 
 namespace slm {
 
-// Pass 2 keeps, per row, column range and column half, up to kSlHalfRecs
-// records of 4 consecutive columns (the group's first column and its 4 d~
-// values): one vector store per hit group. A half with more hit groups
-// overflows and the row is settled by an exact scan.
+// Pass 2 keeps, per row, column range and column half, up to half_recs
+// (SlArgs; the autotuner's shortlist_k, default kSlHalfRecs) records of 4
+// consecutive columns (the group's first column and its 4 d~ values): one
+// vector store per hit group. A half with more hit groups overflows and the
+// row is settled by an exact scan.
 constexpr int kSlHalfRecs = 16;
-constexpr int kSlRowRecs = 2 * kSlHalfRecs;
+constexpr int kSlHalfRecsMax = 32;
 // Routing estimate of a row's shortlist size (in columns).
 constexpr int kSlRowSlots = 32;
 // A pair's columns split into at most this many ranges (items that share its
 // rows); each range keeps its own records per row, so their memory is
-// (rows x ranges) x kSlRowRecs records.
+// (rows x ranges) x 2 half_recs records.
 constexpr uint32_t kSlMaxRanges = 4;
 constexpr int kSlStages = 4;       // b-tile ring depth (FP8; BF16 tiles are larger: 3)
 constexpr int kSlEpWarps = 16;     // epilogue warps
@@ -172,7 +173,7 @@ struct SlArgs {
     float *rowthr;               // mid -> pass 2
     float *colthr;               // mid -> pass 2
     uint32_t *rowcnt;            // pass 2: records per candidate row and column half
-    float4 *rowrec;              // pass 2: a record's 4 d~ values (BF16: d~ / 2), kSlRowRecs per candidate row
+    float4 *rowrec;              // pass 2: a record's 4 d~ values (BF16: d~ / 2), 2 half_recs per candidate row
     uint32_t *rowrecj;           // the record's first column
     float *colcnt;               // |C| per column (f32 counts: exact below 2^24)
     uint32_t *rowdec;            // finalize / rescore / scan
@@ -200,6 +201,7 @@ struct SlArgs {
     // FP8 plans: pairs the FP8 bound cannot settle (mid: too many wide rows) are
     // rescued by a second, BF16 run of eps / pass 1 / mid / pass 2 / finalize
     // over those pairs only (tier 1), instead of the exact kernel
+    uint32_t half_recs;          // records per candidate row and column half (1..kSlHalfRecsMax)
     uint32_t rescue;             // tier 0 of an FP8 plan: mid marks pairs rescued, not routed
     uint32_t tier;               // 0: the plan's precision; 1: the BF16 rescue of an FP8 plan
 };

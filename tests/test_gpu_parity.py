@@ -226,6 +226,35 @@ def test_zone_batch_one_row_tile_per_item(matcher, prec):
     st.close()
 
 
+@pytest.fixture(scope="module")
+def tune_zone():
+    z = synth.zone(positions=6, n_range=(200, 1500), seed=19)
+    want = [O.ratio_match_np(z.view(int(u)), z.view(int(v)), 0.8, True, threads=16) for u, v in z.pairs]
+    return z, want
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp8"])
+@pytest.mark.parametrize("row_tiles", [1, 2])
+@pytest.mark.parametrize("shortlist_k", [8, 12, 16, 2])
+def test_tuning_grid_points(matcher, tune_zone, prec, row_tiles, shortlist_k):
+    """Every setting the autotuner can pick gives the oracle's lists (shortlist
+    capacity 2 records per row half, below the grid, forces overflows: those
+    rows are scanned exactly)."""
+    z, want = tune_zone
+    st = matcher.store(int(z.counts.sum()), len(z.counts))
+    st.add_views_packed(z.desc, z.offsets, z.counts)
+    for ipsm in (2, 8):
+        plan = st.plan(z.pairs, 0.8, True, prec, items_per_sm=ipsm, row_tiles=row_tiles, shortlist_k=shortlist_k)
+        plan.launch()
+        per = plan.per_pair()
+        for k in range(len(z.pairs)):
+            assert np.array_equal(per[k], want[k]), (ipsm, k)
+        if shortlist_k == 2 and prec == "bf16":
+            assert plan.stats["rows_recomputed"] > 0  # overflowed rows went to the exact scan
+        plan.close()
+    st.close()
+
+
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
 def test_autotuned_plan(matcher, prec):
     z = synth.zone(positions=6, n_range=(200, 1000), seed=17)
@@ -233,6 +262,8 @@ def test_autotuned_plan(matcher, prec):
     st.add_views_packed(z.desc, z.offsets, z.counts)
     best, ms = st.autotune(z.pairs, 0.8, True, prec)
     assert ms > 0 and best["items_per_sm"] in (2, 4, 8)
+    if prec != "fp32":
+        assert best["shortlist_k"] in (8, 12, 16) and best["row_tiles"] in (1, 2)
     plan = st.plan(z.pairs, 0.8, True, prec, autotune=True)
     plan.launch()
     per = plan.per_pair()
