@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--rates", default="10,50,200,burst",
                     help="serving arrival rates, views/s ('burst': every view at once, the saturated server)")
     ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
+    ap.add_argument("--ransac", action="store_true", help="RANSAC hypothesis scoring (Sampson residuals)")
     ap.add_argument("--no-scheduled", action="store_true",
                     help="skip the scheduled_pairs(PairSchedule::default()) batch with the < 20 filter")
     ap.add_argument("--no-configs", action="store_true",
@@ -366,6 +367,52 @@ def pair_configs(m, steps: int, threads: int) -> list:
     return out
 
 
+def ransac_configs(m, threads: int, pairs: int = 100, hyps: int = 2000, reps: int = 3) -> dict:
+    """The RANSAC stage's hypothesis scoring (two_view.rs:804-823) for a block
+    of iterations of `pairs` kept pairs: matches per pair ~ U[200, 550] (the
+    240-view zone keeps 373 matches per pair on average), `hyps` hypotheses each
+    (500 iterations of up to 10 5-point solutions per pair in the reference).
+    GPU: slm_sampson_score from host arrays (copies in the timed call); CPU:
+    the oracle's restatement on all host threads. Counts must be equal."""
+    import oracle as O
+    from skylens_match import synth
+    rng = np.random.default_rng(5)
+    pts, off, th, hs, hp = [], [0], [], [], []
+    for p in range(pairs):
+        n = int(rng.integers(200, 551))
+        n1, n2, e = synth.two_view(rng, n, inlier_frac=rng.uniform(0.3, 0.9))
+        pts.append(np.concatenate([n1, n2], 1))
+        off.append(off[-1] + n)
+        th.append(1.5 / 800.0)
+        hs.append(synth.essential_hypotheses(rng, e, hyps))
+        hp += [p] * hyps
+    pts = np.concatenate(pts)
+    off = np.asarray(off, np.uint64)
+    th = np.asarray(th)
+    hs = np.concatenate(hs)
+    hp = np.asarray(hp, np.uint32)
+    residuals = int(sum(int(off[p + 1] - off[p]) for p in hp))
+    got, _ = m.sampson_score(pts, off, th, hs, hp)  # warm-up
+    gpu = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        got, _ = m.sampson_score(pts, off, th, hs, hp)
+        gpu.append(time.perf_counter() - t0)
+    cpu = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        want, _ = O.sampson_score(pts, off, th, hs, hp, threads=threads)
+        cpu.append(time.perf_counter() - t0)
+    g, c = float(np.median(gpu)), float(np.median(cpu))
+    return {"metric": "RANSAC hypothesis scoring: Sampson residuals/s (count_at_least / inliers_of)",
+            "config": {"pairs": pairs, "hypotheses": len(hs), "matches": int(off[-1]), "residuals": residuals,
+                       "dtype": "f64, the reference's operation order"},
+            "gpu": {"ms": g * 1e3, "residuals_per_s": residuals / g,
+                    "timed": "slm_sampson_score from host arrays (uploads and read-back included)"},
+            "cpu": {"ms": c * 1e3, "residuals_per_s": residuals / c, "threads": threads, "kind": "port"},
+            "equal_counts": bool(np.array_equal(got, want))}
+
+
 def settled_frac(s, na, prec):
     """Fractions of a single pair's rows settled by each tier: by the FP8 bound,
     by the BF16 bound (BF16 pairs, and FP8 pairs rescued by the BF16 passes),
@@ -397,6 +444,12 @@ def main():
         return run_serve(args)
     if args.pairs:
         return run_pairs(args)
+    if args.ransac:
+        import skylens_match as sm
+        m = sm.Matcher()
+        print(json.dumps(ransac_configs(m, os.cpu_count() or 1)), flush=True)
+        m.close()
+        return 0
     import torch
 
     import oracle as O
@@ -661,7 +714,8 @@ def main():
         # in every precision and the serving workload at one rate and in a burst
         t_c = time.perf_counter()
         line["configs"] = {"pairs": pair_configs(m, 3, os.cpu_count() or 1),
-                           "serve": serve_configs(args.seed, args.config_rates, os.cpu_count() or 1)}
+                           "serve": serve_configs(args.seed, args.config_rates, os.cpu_count() or 1),
+                           "ransac_scoring": ransac_configs(m, os.cpu_count() or 1)}
         line["configs"]["wall_s"] = time.perf_counter() - t_c
     if rank == 0:
         s = json.dumps(line)

@@ -277,6 +277,32 @@ slm_status slm_match_pairs(slm_ctx *ctx, slm_store *st, const uint64_t *views, u
                            uint32_t min_matches, slm_pair *pairs_out, uint64_t pairs_cap, uint64_t *n_pairs,
                            slm_pair *out, uint64_t cap, uint64_t *offsets, slm_stats *stats);
 
+/* ------------------------------------------ RANSAC hypothesis scoring */
+
+/* Sampson scoring of essential-matrix hypotheses, batched over image pairs:
+ * the per-hypothesis work of the RANSAC stage that runs on every pair
+ * match_pairs keeps (pipeline.rs:505 -> two_view.rs:774
+ * ransac_essential_candidates_stats). Replaces, for each hypothesis,
+ * count_at_least(e, need) and inliers_of(e) of ransac_essential_inner
+ * (two_view.rs:804-823), built on sampson_residual (two_view.rs:456-465);
+ * the caller keeps the sampling, the 5-point solver and the pool logic, and
+ * count_at_least(e, need) is counts[h] >= need ? counts[h] : none.
+ *   pts       the matches of all pairs, 4 doubles each: a.x, a.y, b.x, b.y
+ *             (the normalized coordinates n1[i], n2[i]); pair p's matches are
+ *             pts[pair_off[p] .. pair_off[p+1]), pair_off[0] = 0.
+ *   thresh    per pair, the normalized threshold (threshold_px / focal_px).
+ *   E         nh hypotheses, 9 doubles each, row-major (Matrix3::new order);
+ *             hyp_pair[h] is hypothesis h's pair.
+ *   counts    counts[h] = #{i : |residual| < thresh} (strict), in f64 with the
+ *             reference's operation order: the counts and masks are its own.
+ *   mask_off  optional (NULL: no masks): where mask_off[h] != UINT64_MAX, bit
+ *             i % 32 of masks[mask_off[h] + i / 32] is match i's inlier flag
+ *             (inliers_of); every other word of masks (mask_words words) is 0.
+ * Blocks until the results are in host memory. */
+slm_status slm_sampson_score(slm_ctx *ctx, const double *pts, const uint64_t *pair_off, uint32_t np,
+                             const double *thresh, const double *E, const uint32_t *hyp_pair, uint32_t nh,
+                             uint32_t *counts, const uint64_t *mask_off, uint32_t *masks, uint64_t mask_words);
+
 /* One-shot: plan, launch, read back, destroy. */
 slm_status slm_match_batch(slm_ctx *ctx, slm_store *st, const slm_pair *pairs, uint32_t np, float ratio,
                            int mutual, slm_precision prec, slm_pair *out, uint64_t cap, uint64_t *offsets,

@@ -15,6 +15,9 @@
  *   orc_pairs_hash                 crates/core/src/matching.rs:1866-1878 (`pairs_hash`, FNV-1a 64)
  *   orc_candidate_pairs            crates/core/src/matching.rs:14-40
  *   orc_scheduled_pairs            crates/core/src/matching.rs:103-142
+ *   orc_sampson_residual           crates/core/src/two_view.rs:456-465 (`sampson_residual`)
+ *   orc_sampson_score              crates/core/src/two_view.rs:804-823 (`inliers_of`,
+ *                                  `count_at_least` of ransac_essential_inner), batched
  * plus orc_sq_dist_f64, an FP64 distance used only to report the error of
  * low-precision distances (never for a match decision).
  *
@@ -468,4 +471,118 @@ int64_t orc_match_pairs(const float *desc, const int64_t *view_off, const int64_
     }
     free(tmp);
     return total;
+}
+
+/* ------------------------------------------------------ Sampson scoring */
+
+/* two_view.rs:456-465, in f64 and in the operation order of the reference's
+ * linear algebra (nalgebra 0.33.3, Cargo.lock), as its published source
+ * states it (the crate's source is not part of the reference, so this order
+ * is a restatement, not checked against the reference's own outputs):
+ *   - Matrix3 * Vector3 is a gemv that adds the columns in order: row i of
+ *     y = e p is ((e[i][0] * p0 + e[i][1] * p1) + e[i][2] * p2), every product
+ *     and sum rounded separately (Rust does not contract to FMA);
+ *   - e.transpose() * q the same with the columns of e^T (the rows of e);
+ *   - den = sqrt(((ep0^2 + ep1^2) + etq0^2) + etq1^2), left to right;
+ *   - q.dot(ep) = (q0 ep0 + q1 ep1) + q2 ep2;
+ *   - the residual is q.dot(ep) / den, or 0 when den is not > 0.
+ * e is row-major (e[3 r + c] = E[r][c], nalgebra's Matrix3::new order);
+ * p = (ax, ay, 1), q = (bx, by, 1). */
+double orc_sampson_residual(const double *e, double ax, double ay, double bx, double by) {
+    double ep[3], etq[3];
+    for (int i = 0; i < 3; ++i) {
+        double y = e[3 * i + 0] * ax;
+        y = e[3 * i + 1] * ay + y;
+        y = e[3 * i + 2] * 1.0 + y;
+        ep[i] = y;
+    }
+    for (int i = 0; i < 3; ++i) {
+        double y = e[0 * 3 + i] * bx;
+        y = e[1 * 3 + i] * by + y;
+        y = e[2 * 3 + i] * 1.0 + y;
+        etq[i] = y;
+    }
+    const double den = sqrt(((ep[0] * ep[0] + ep[1] * ep[1]) + etq[0] * etq[0]) + etq[1] * etq[1]);
+    if (den > 0.0) {
+        const double dot = (bx * ep[0] + by * ep[1]) + 1.0 * ep[2];
+        return dot / den;
+    }
+    return 0.0;
+}
+
+typedef struct {
+    const double *pts, *thresh, *E;
+    const uint64_t *pair_off, *mask_off;
+    const uint32_t *hyp_pair;
+    uint32_t *counts, *masks;
+    int64_t nh, next;
+    pthread_mutex_t mu;
+} ss_job;
+
+static void ss_one(ss_job *J, int64_t h) {
+    const uint32_t p = J->hyp_pair[h];
+    const uint64_t m0 = J->pair_off[p], m1 = J->pair_off[p + 1];
+    const double th = J->thresh[p];
+    const double *e = J->E + 9 * h;
+    uint32_t c = 0;
+    uint32_t *mk = (J->masks && J->mask_off && J->mask_off[h] != UINT64_MAX) ? J->masks + J->mask_off[h] : NULL;
+    for (uint64_t i = m0; i < m1; ++i) {
+        const double *q = J->pts + 4 * i;
+        /* inliers_of / count_at_least: |r| < th, strict (two_view.rs:806, :812) */
+        const int in = fabs(orc_sampson_residual(e, q[0], q[1], q[2], q[3])) < th;
+        c += (uint32_t)in;
+        if (mk) {
+            const uint64_t k = i - m0;
+            if ((k & 31) == 0) mk[k >> 5] = 0;
+            if (in) mk[k >> 5] |= 1u << (k & 31);
+        }
+    }
+    J->counts[h] = c;
+}
+
+static void *ss_worker(void *arg) {
+    ss_job *J = (ss_job *)arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        const int64_t h0 = J->next;
+        J->next += 64;
+        pthread_mutex_unlock(&J->mu);
+        if (h0 >= J->nh) break;
+        const int64_t h1 = h0 + 64 < J->nh ? h0 + 64 : J->nh;
+        for (int64_t h = h0; h < h1; ++h) ss_one(J, h);
+    }
+    return NULL;
+}
+
+/* Every hypothesis h (E + 9 h, of pair hyp_pair[h]) scored over its pair's
+ * matches pts[pair_off[p] .. pair_off[p+1]) (4 doubles each: a.x, a.y, b.x,
+ * b.y): counts[h] = #{i : |r_h(i)| < thresh[p]} (the count count_at_least
+ * returns when it reaches `need`, the length of inliers_of's true set), and,
+ * where mask_off[h] != UINT64_MAX, the inlier bits of inliers_of at
+ * masks[mask_off[h] ..] (bit i % 32 of word i / 32). Hypotheses are spread
+ * over `threads` threads. */
+void orc_sampson_score(const double *pts, const uint64_t *pair_off, const double *thresh, const double *E,
+                       const uint32_t *hyp_pair, int64_t nh, uint32_t *counts, const uint64_t *mask_off,
+                       uint32_t *masks, int threads) {
+    ss_job J;
+    J.pts = pts;
+    J.thresh = thresh;
+    J.E = E;
+    J.pair_off = pair_off;
+    J.mask_off = mask_off;
+    J.hyp_pair = hyp_pair;
+    J.counts = counts;
+    J.masks = masks;
+    J.nh = nh;
+    J.next = 0;
+    pthread_mutex_init(&J.mu, NULL);
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int t = 1; t < threads; ++t)
+        if (pthread_create(&th[started], NULL, ss_worker, &J) == 0) ++started;
+    ss_worker(&J);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&J.mu);
 }

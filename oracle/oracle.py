@@ -79,6 +79,10 @@ def lib():
                                               ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
                                               ctypes.c_uint64, u32p, i64]
             L.orc_scheduled_pairs.restype = i64
+            f64p = P(ctypes.c_double)
+            L.orc_sampson_residual.argtypes = [f64p] + [ctypes.c_double] * 4
+            L.orc_sampson_residual.restype = ctypes.c_double
+            L.orc_sampson_score.argtypes = [f64p, u64p, f64p, f64p, u32p, i64, u32p, u64p, u32p, ctypes.c_int]
             L.orc_match_pairs.argtypes = [f32p, P(ctypes.c_int64), P(ctypes.c_int64), u32p, i64, ctypes.c_float,
                                           ctypes.c_int, ctypes.c_int, P(ctypes.c_int64)]
             L.orc_match_pairs.restype = i64
@@ -242,3 +246,38 @@ def match_pairs(desc, view_off, view_n, pairs, ratio: float, mutual: bool, threa
                                 _p(pr, ctypes.c_uint32), len(pr), ctypes.c_float(ratio), int(bool(mutual)),
                                 int(threads), _p(counts, ctypes.c_int64))
     return tot, counts
+
+
+def sampson_residual(e, a, b) -> float:
+    """two_view.rs:456-465: signed Sampson residual of one correspondence
+    (a, b: normalized coordinates) under the row-major 3x3 matrix e."""
+    e = np.ascontiguousarray(e, dtype=np.float64).reshape(9)
+    return lib().orc_sampson_residual(_p(e, ctypes.c_double), float(a[0]), float(a[1]), float(b[0]), float(b[1]))
+
+
+def sampson_score(pts, pair_off, thresh, E, hyp_pair, mask_off=None, threads: int = 1):
+    """two_view.rs:804-823 (inliers_of, count_at_least), batched: counts (and
+    inlier bit masks where mask_off[h] != 2**64 - 1) of every hypothesis over
+    its pair's matches. pts: (M, 4) f64 (a.x, a.y, b.x, b.y); pair_off: (P+1,)
+    uint64; thresh: (P,) f64; E: (H, 3, 3) f64; hyp_pair: (H,) uint32."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 4)
+    po = np.ascontiguousarray(pair_off, dtype=np.uint64)
+    th = np.ascontiguousarray(thresh, dtype=np.float64)
+    E = np.ascontiguousarray(E, dtype=np.float64).reshape(-1, 9)
+    hp = np.ascontiguousarray(hyp_pair, dtype=np.uint32)
+    counts = np.empty(len(E), np.uint32)
+    masks = None
+    mo = None
+    if mask_off is not None:
+        mo = np.ascontiguousarray(mask_off, dtype=np.uint64)
+        nwords = 0
+        for h in range(len(E)):
+            if mo[h] != np.uint64(2**64 - 1):
+                n = int(po[hp[h] + 1] - po[hp[h]])
+                nwords = max(nwords, int(mo[h]) + (n + 31) // 32)
+        masks = np.zeros(max(nwords, 1), np.uint32)
+    lib().orc_sampson_score(_p(pts, ctypes.c_double), _p(po, ctypes.c_uint64), _p(th, ctypes.c_double),
+                            _p(E, ctypes.c_double), _p(hp, ctypes.c_uint32), len(E), _p(counts, ctypes.c_uint32),
+                            None if mo is None else _p(mo, ctypes.c_uint64),
+                            None if masks is None else _p(masks, ctypes.c_uint32), int(threads))
+    return counts, masks

@@ -693,6 +693,7 @@ struct Workspace {
     slm_store store;
     slm_plan plan;
     DevBuf single;                   // FP32 single-pair calls: inputs and scratch
+    DevBuf score;                    // slm_sampson_score: inputs and outputs
     unsigned char *single_host = nullptr;  // their result block: pinned host memory the kernels write
     size_t single_host_bytes = 0;
 };
@@ -2243,6 +2244,77 @@ extern "C" slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st
     *st = srv->stats;
     st->bytes_in_use = srv->ctx->used.load();
     return SLM_OK;
+}
+
+// --------------------------------------------------------- Sampson scoring
+
+extern "C" slm_status slm_sampson_score(slm_ctx *c, const double *pts, const uint64_t *pair_off, uint32_t np,
+                                        const double *thresh, const double *E, const uint32_t *hyp_pair, uint32_t nh,
+                                        uint32_t *counts, const uint64_t *mask_off, uint32_t *masks,
+                                        uint64_t mask_words) {
+    NvtxRange range_("slm_sampson_score");
+    if (!c || (np && !thresh) || !pair_off || (nh && (!E || !hyp_pair || !counts)) ||
+        (mask_off && mask_words && !masks))
+        return fail(SLM_INVALID_ARG, "NULL argument");
+    for (uint32_t q = 0; q < np; ++q)
+        if (pair_off[q + 1] < pair_off[q]) return fail(SLM_INVALID_ARG, "pair_off must not decrease");
+    const uint64_t m = pair_off[np];
+    if (pair_off[0] != 0) return fail(SLM_INVALID_ARG, "pair_off[0] must be 0");
+    if (m && !pts) return fail(SLM_INVALID_ARG, "NULL pts");
+    for (uint32_t h = 0; h < nh; ++h) {
+        if (hyp_pair[h] >= np) return fail(SLM_INVALID_ARG, "hyp_pair names no pair");
+        if (mask_off && mask_off[h] != ~0ull) {
+            const uint64_t n = pair_off[hyp_pair[h] + 1] - pair_off[hyp_pair[h]];
+            if (mask_off[h] > mask_words || (n + 31) / 32 > mask_words - mask_off[h])
+                return fail(SLM_INVALID_ARG, "a mask does not fit in mask_words");
+        }
+    }
+    if (!nh) return SLM_OK;
+    SLM_TRY(ctx_check_device(c));
+    Workspace *w = nullptr;
+    SLM_TRY(ws_acquire(c, &w));
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_pts = 0, o_off = al(o_pts + 32 * m), o_th = al(o_off + 8 * (uint64_t)(np + 1)),
+                 o_e = al(o_th + 8 * (uint64_t)np), o_hp = al(o_e + 72 * (uint64_t)nh),
+                 o_cnt = al(o_hp + 4 * (uint64_t)nh), o_moff = al(o_cnt + 4 * (uint64_t)nh),
+                 o_mask = al(o_moff + (mask_off ? 8 * (uint64_t)nh : 0)),
+                 bytes = al(o_mask + (mask_off ? 4 * mask_words : 0));
+    slm_status st = w->score.ensure(c, bytes);
+    if (st == SLM_OK) {
+        unsigned char *d = w->score.as<unsigned char>();
+        cudaStream_t s = w->stream;
+        auto up = [&](size_t off, const void *src, size_t n) {
+            return n ? cudaMemcpyAsync(d + off, src, n, cudaMemcpyHostToDevice, s) : cudaSuccess;
+        };
+        cudaError_t e = up(o_pts, pts, 32 * m);
+        if (e == cudaSuccess) e = up(o_off, pair_off, 8 * (uint64_t)(np + 1));
+        if (e == cudaSuccess) e = up(o_th, thresh, 8 * (uint64_t)np);
+        if (e == cudaSuccess) e = up(o_e, E, 72 * (uint64_t)nh);
+        if (e == cudaSuccess) e = up(o_hp, hyp_pair, 4 * (uint64_t)nh);
+        if (e == cudaSuccess && mask_off) e = up(o_moff, mask_off, 8 * (uint64_t)nh);
+        if (e == cudaSuccess && mask_off && mask_words) e = cudaMemsetAsync(d + o_mask, 0, 4 * mask_words, s);
+        if (e == cudaSuccess) {
+            SampsonArgs a{};
+            a.pts = reinterpret_cast<const double4 *>(d + o_pts);
+            a.pair_off = reinterpret_cast<const uint64_t *>(d + o_off);
+            a.thresh = reinterpret_cast<const double *>(d + o_th);
+            a.E = reinterpret_cast<const double *>(d + o_e);
+            a.hyp_pair = reinterpret_cast<const uint32_t *>(d + o_hp);
+            a.nh = nh;
+            a.counts = reinterpret_cast<uint32_t *>(d + o_cnt);
+            a.mask_off = mask_off ? reinterpret_cast<const uint64_t *>(d + o_moff) : nullptr;
+            a.masks = mask_off ? reinterpret_cast<uint32_t *>(d + o_mask) : nullptr;
+            launch_sampson(a, s);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(counts, d + o_cnt, 4 * (uint64_t)nh, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && mask_off && mask_words)
+            e = cudaMemcpyAsync(masks, d + o_mask, 4 * mask_words, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = fail(SLM_CUDA_ERROR, std::string("slm_sampson_score: ") + cudaGetErrorString(e));
+    }
+    ws_release(c, w);
+    return st;
 }
 
 // ------------------------------------------------------------- coalescing

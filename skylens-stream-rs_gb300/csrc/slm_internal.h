@@ -139,4 +139,22 @@ cudaError_t single_exact_enqueue(unsigned char *scratch, const SingleLayout &L, 
                                  const float *d_b, uint32_t nb, float ratio, int mutual, slm_pair *d_out,
                                  uint32_t cap, uint32_t *d_count, int sms, cudaStream_t s);
 
+// Sampson scoring of essential-matrix hypotheses (k_sampson.cu), all device
+// pointers: pair p's matches are pts[pair_off[p] .. pair_off[p+1]) (a.x, a.y,
+// b.x, b.y), hypothesis h is E[9 h .. 9 h + 9) (row-major) of pair
+// hyp_pair[h]; counts[h] = #{i : |r| < thresh[p]}; with mask_off[h] !=
+// ~0, the inlier bits at masks[mask_off[h] ..].
+struct SampsonArgs {
+    const double4 *pts;
+    const uint64_t *pair_off;
+    const double *thresh;
+    const double *E;
+    const uint32_t *hyp_pair;
+    uint64_t nh;
+    uint32_t *counts;
+    const uint64_t *mask_off;  // may be null (no masks)
+    uint32_t *masks;
+};
+void launch_sampson(const SampsonArgs &a, cudaStream_t s);
+
 }  // namespace slm

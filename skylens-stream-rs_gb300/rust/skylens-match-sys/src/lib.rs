@@ -145,4 +145,7 @@ extern "C" {
                            sch: *const slm_pair_schedule, ratio: f32, mutual: c_int, prec: SlmPrecision,
                            min_matches: u32, pairs_out: *mut slm_pair, pairs_cap: u64, n_pairs: *mut u64,
                            out: *mut slm_pair, cap: u64, offsets: *mut u64, stats: *mut slm_stats) -> SlmStatus;
+    pub fn slm_sampson_score(ctx: *mut slm_ctx, pts: *const f64, pair_off: *const u64, np: u32, thresh: *const f64,
+                             e: *const f64, hyp_pair: *const u32, nh: u32, counts: *mut u32, mask_off: *const u64,
+                             masks: *mut u32, mask_words: u64) -> SlmStatus;
 }

@@ -5,6 +5,9 @@
 //! * `candidate_pairs(views, temporal, cross, pow2_max)` (matching.rs:18)
 //! * `match_pairs(descs, pairs, ratio, mutual)`: the matching half of
 //!   pipeline.rs:485-493 as one GPU batch.
+//! * `sampson_counts(pts, th, hyps)`: inlier counts of essential-matrix
+//!   hypotheses over one pair's matches (two_view.rs:804-823, count_at_least),
+//!   for a block of RANSAC iterations at once.
 //!
 //! The one deviation from the reference: it cannot fail on the CPU, this can
 //! fail on the GPU; a non-OK status panics with libslm's message (there is no
@@ -230,4 +233,26 @@ pub fn match_scheduled_pairs<D: Descriptor>(imgs: &[&[D]], views: &[(usize, usiz
             (pairs_out[k].i as usize, pairs_out[k].j as usize, m)
         })
         .collect()
+}
+
+/// Inlier counts of `hyps` (row-major 3x3 matrices, `Matrix3::new` order) over
+/// one pair's matches `pts` (`[n1.x, n1.y, n2.x, n2.y]` in normalized
+/// coordinates): `#{i : |sampson_residual(e, n1[i], n2[i])| < th}` for each, in
+/// the reference's f64 order (two_view.rs:456-465, 804-823).
+pub fn sampson_counts(pts: &[[f64; 4]], th: f64, hyps: &[[f64; 9]]) -> Vec<u32> {
+    if hyps.is_empty() {
+        return Vec::new();
+    }
+    let off = [0u64, pts.len() as u64];
+    let hp = vec![0u32; hyps.len()];
+    let mut counts = vec![0u32; hyps.len()];
+    check(
+        unsafe {
+            sys::slm_sampson_score(ctx(), pts.as_ptr() as *const f64, off.as_ptr(), 1, &th,
+                                   hyps.as_ptr() as *const f64, hp.as_ptr(), hyps.len() as u32,
+                                   counts.as_mut_ptr(), std::ptr::null(), std::ptr::null_mut(), 0)
+        },
+        "slm_sampson_score",
+    );
+    counts
 }

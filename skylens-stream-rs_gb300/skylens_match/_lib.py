@@ -129,6 +129,8 @@ SIGNATURES = {
     "slm_match_pairs": (c_int, [ctypes.c_void_p, ctypes.c_void_p, P(c_u64), c_u32, P(SlmPairSchedule), c_f32, c_int,
                                 c_int, c_u32, P(SlmPair), c_u64, P(c_u64), P(SlmPair), c_u64, P(c_u64),
                                 P(SlmStats)]),
+    "slm_sampson_score": (c_int, [ctypes.c_void_p, P(ctypes.c_double), P(c_u64), c_u32, P(ctypes.c_double),
+                                  P(ctypes.c_double), P(c_u32), c_u32, P(c_u32), P(c_u64), P(c_u32), c_u64]),
 }
 
 _lock = threading.Lock()

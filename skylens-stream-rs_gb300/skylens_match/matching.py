@@ -151,6 +151,46 @@ class Matcher:
                                              ctypes.c_void_p(d_out), cap, ctypes.c_void_p(d_count)),
               "slm_ratio_match_device")
 
+    # ------------------------------------------------------ RANSAC scoring
+    def sampson_score(self, pts, pair_off, thresh, E, hyp_pair, masks_for=None):
+        """slm_sampson_score: inlier counts of every essential-matrix hypothesis
+        over its pair's matches (two_view.rs:804-823, count_at_least /
+        inliers_of). pts (M, 4) f64 (a.x, a.y, b.x, b.y); pair_off (P + 1,)
+        uint64 from 0; thresh (P,) f64 (threshold_px / focal_px); E (H, 3, 3)
+        f64; hyp_pair (H,) uint32. masks_for: hypotheses whose inlier masks to
+        return. Returns (counts (H,) uint32, {h: bool mask of its pair's matches})."""
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 4)
+        po = np.ascontiguousarray(pair_off, dtype=np.uint64)
+        th = np.ascontiguousarray(thresh, dtype=np.float64)
+        Ev = np.ascontiguousarray(E, dtype=np.float64).reshape(-1, 9)
+        hp = np.ascontiguousarray(hyp_pair, dtype=np.uint32)
+        nh = len(Ev)
+        counts = np.empty(max(nh, 1), np.uint32)
+        mo = masks = None
+        words = 0
+        if masks_for is not None and len(masks_for):
+            mo = np.full(max(nh, 1), np.uint64(2**64 - 1), np.uint64)
+            for h in masks_for:
+                mo[h] = words
+                words += (int(po[hp[h] + 1] - po[hp[h]]) + 31) // 32
+            masks = np.zeros(max(words, 1), np.uint32)
+        P = ctypes.POINTER
+        check(self._L.slm_sampson_score(self._h, pts.ctypes.data_as(P(ctypes.c_double)),
+                                        po.ctypes.data_as(P(ctypes.c_uint64)), len(po) - 1,
+                                        th.ctypes.data_as(P(ctypes.c_double)), Ev.ctypes.data_as(P(ctypes.c_double)),
+                                        hp.ctypes.data_as(P(ctypes.c_uint32)), nh,
+                                        counts.ctypes.data_as(P(ctypes.c_uint32)),
+                                        None if mo is None else mo.ctypes.data_as(P(ctypes.c_uint64)),
+                                        None if masks is None else masks.ctypes.data_as(P(ctypes.c_uint32)),
+                                        words), "slm_sampson_score")
+        out = {}
+        if mo is not None:
+            for h in masks_for:
+                n = int(po[hp[h] + 1] - po[hp[h]])
+                bits = np.unpackbits(masks[int(mo[h]):int(mo[h]) + (n + 31) // 32].view(np.uint8), bitorder="little")
+                out[h] = bits[:n].astype(bool)
+        return counts[:nh], out
+
     # ------------------------------------------------------------ batches
     def store(self, max_descs: int, max_views: int) -> "DescriptorStore":
         return DescriptorStore(self, max_descs, max_views)

@@ -164,3 +164,48 @@ def zone(positions: int = 80, cameras: int = 3, n_range=(300, 2000), sigma: floa
     offsets = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
     pairs = candidate_pairs_np(views)
     return Zone(views, desc, offsets, counts.astype(np.uint32), pairs, np.concatenate(lmk))
+
+
+def two_view(rng: np.random.Generator, n: int, inlier_frac: float = 0.6, noise_px: float = 0.5,
+             focal: float = 800.0):
+    """Calibrated two-view correspondences of a random scene, the input of the
+    RANSAC stage (normalized coordinates, as pipeline.rs:497-498 forms them): a
+    random pose (rotation of 3-20 degrees about a random axis, unit
+    translation), points 4-10 units in front of both cameras, Gaussian pixel
+    noise (noise_px / focal in normalized units), and (1 - inlier_frac) of the
+    matches replaced by random points. Returns (n1 (n, 2), n2 (n, 2), E (3, 3)
+    = [t]x R, row-major)."""
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    ang = rng.uniform(0.05, 0.35)
+    k = np.array([[0.0, -ax[2], ax[1]], [ax[2], 0.0, -ax[0]], [-ax[1], ax[0], 0.0]])
+    r = np.eye(3) + np.sin(ang) * k + (1.0 - np.cos(ang)) * (k @ k)
+    t = rng.normal(size=3)
+    t /= np.linalg.norm(t)
+    x = np.stack([rng.uniform(-3, 3, n), rng.uniform(-3, 3, n), rng.uniform(4, 10, n)], 1)
+    x2 = x @ r.T + 0.5 * t
+    n1 = x[:, :2] / x[:, 2:3]
+    n2 = x2[:, :2] / x2[:, 2:3]
+    n1 = n1 + rng.normal(0.0, noise_px / focal, n1.shape)
+    n2 = n2 + rng.normal(0.0, noise_px / focal, n2.shape)
+    bad = rng.permutation(n)[: int(round(n * (1.0 - inlier_frac)))]
+    if len(bad):
+        lo, hi = n2.min(0), n2.max(0)
+        n2[bad] = rng.uniform(lo, hi, (len(bad), 2))
+    tx = np.array([[0.0, -t[2], t[1]], [t[2], 0.0, -t[0]], [-t[1], t[0], 0.0]])
+    return n1, n2, tx @ r
+
+
+def essential_hypotheses(rng: np.random.Generator, e_true: np.ndarray, count: int) -> np.ndarray:
+    """Hypotheses like a RANSAC pool's: the true matrix, perturbations of it at
+    scales 1e-6 .. 1e-1, random essential matrices, scaled copies and the zero
+    matrix (whose residuals are all 0). (count, 3, 3) f64."""
+    out = [e_true, np.zeros((3, 3)), 1e-3 * e_true, 1e3 * e_true]
+    while len(out) < count:
+        kind = len(out) % 3
+        if kind == 0:
+            out.append(e_true + rng.normal(0.0, 10.0 ** rng.uniform(-6, -1), (3, 3)))
+        else:
+            _, _, e = two_view(rng, 1)
+            out.append(e * 10.0 ** rng.uniform(-2, 2))
+    return np.asarray(out[:count], dtype=np.float64)
