@@ -294,18 +294,22 @@ __global__ void __launch_bounds__(128) pack_lowp_kernel(const uint4 *__restrict_
     }
     if constexpr (!FP8) {
         // norm extension (slm_shortlist.h): |a|^2 / 2 = hi + lo (the difference
-        // of a float and its bf16 rounding is exact in f32); padding rows stay 0
+        // of a float and its bf16 rounding is exact in f32). Padding rows get
+        // hi = NaN: every product with a padding row or column is NaN, which
+        // min.f32 and redux.min ignore and no threshold admits, so the pass
+        // kernels need no masks for ragged tiles
         const float half = valid ? 0.5f * nrm : 0.f;
         const __nv_bfloat16 hi = __float2bfloat16_rn(half);
         const __nv_bfloat16 lo = __float2bfloat16_rn(half - __bfloat162float(hi));
-        const uint32_t hl = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
-        const uint32_t ones = valid ? 0x3f803f80u : 0u;  // two bf16 1.0
+        const uint32_t hl = valid ? ((uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16))
+                                  : 0x00007fc0u;  // padding rows: hi = NaN, lo = 0
+        const uint32_t ones = 0x3f803f80u;  // two bf16 1.0
         uint8_t *ext = dst + kBf16TileBytes + (r >> 3) * 384 + (r & 7) * 16;
         *reinterpret_cast<uint4 *>(ext) = make_uint4(hl, ones, 0u, 0u);        // kc0: hi lo 1 1
         *reinterpret_cast<uint4 *>(ext + 128) = make_uint4(ones, hl, 0u, 0u);  // kc1: 1 1 hi lo
         *reinterpret_cast<uint4 *>(ext + 256) = make_uint4(0u, 0u, 0u, 0u);    // kc2
     }
-    norms[row0 + row] = valid ? nrm : 0.f;
+    norms[row0 + row] = valid ? nrm : __int_as_float(0x7fc00000);  // FP8: NaN distances to padding rows too
     if constexpr (FP8) qscale[row0 + row] = inv;
     // statistics (non-negative floats compare as their bit patterns)
     float s_n = valid ? sqrtf(nrm) : 0.f, s_r = valid ? sqrtf(res) : 0.f, s_q = valid ? sqrtf(nq) : 0.f;
@@ -659,7 +663,6 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                 }
                 tc_fence_after();
                 if (qvalid) {
-                    const bool any_invalid_row = __any_sync(0xffffffffu, !rvalid);
                     const uint32_t tcol = tmem + lane_addr + (tb * 2 + at) * 128 + h * 64;
                     // chunks of 16 columns, two per iteration: loads double-buffered,
                     // the body kept at two copies (instruction-cache footprint)
@@ -683,17 +686,6 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
 #pragma unroll
                             for (int k = 0; k < 16; ++k) d[k] = __uint_as_float(vc[k]);  // d~ / 2
                         }
-                        if (j0 + 16 > pm.nb) {
-                            // ragged last tile: padding columns never win. Pass 1
-                            // gives them +inf (the row state stays ordered); pass 2
-                            // gives them NaN, which no threshold admits, not even
-                            // the +inf of a row with a single finite chunk
-                            // (min.f32 ignores NaN)
-                            const float pad_d = PASS == 1 ? kInf : __int_as_float(0x7fffffff);
-#pragma unroll
-                            for (int k = 0; k < 16; ++k)
-                                if (j0 + k >= pm.nb) d[k] = pad_d;
-                        }
                         if constexpr (PASS == 1) {
                             if (DUMP && pid == 0 && rvalid) {
 #pragma unroll
@@ -706,10 +698,7 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                             if constexpr (FP8) near += (cm >= m1 && cm <= m1 + w2) ? 1u : 0u;
                             m2 = fminf(m2, fmaxf(m1, cm));
                             m1 = fminf(m1, cm);
-                            if (any_invalid_row) {
-#pragma unroll
-                                for (int k = 0; k < 16; ++k) d[k] = rvalid ? d[k] : kInf;
-                            }
+
                             float4 *cp = reinterpret_cast<float4 *>(&S.colpart[tb][combo][cb]);
 #pragma unroll
                             for (int k4 = 0; k4 < 4; ++k4) {
@@ -774,9 +763,12 @@ __global__ void __maxnreg__(kSlMaxRegs) sl_pass_kernel(SlArgs g) {
                     // of the sub-partition cover the load's latency
                     const ulonglong2 *bt2 = reinterpret_cast<const ulonglong2 *>(
                         two && at == 1 ? &S.bthr2[st][h * 64] : &S.bthr[st][h * 64]);
+                    // chunks of this tile's column half holding columns of the pair
+                    // (warp-uniform; the rest are padding): a loop bound, not a test per chunk
+                    const uint32_t jt = t * kTile + h * 64;
+                    const int nc = jt >= pm.nb ? 0 : (int)min(4u, (pm.nb - jt + 15) / 16);
 #pragma unroll 1
-                    for (int c = 0; c < 4; ++c) {
-                        if (t * kTile + h * 64 + c * 16 >= pm.nb) break;  // padding only (warp-uniform)
+                    for (int c = 0; c < nc; ++c) {
                         ulonglong2 tt[4];  // pass 2: the chunk's column thresholds, read before the wait
                         if constexpr (PASS == 2) {
 #pragma unroll
