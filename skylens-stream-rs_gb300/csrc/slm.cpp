@@ -1802,8 +1802,27 @@ struct ServeSlot {
     bool busy = false;
     slm_pair *pin = nullptr;         // pinned staging of a finished batch's matches (grows)
     uint64_t pin_cap = 0;
+    uint64_t *pin_off = nullptr;     // pinned staging of its per-pair offsets (grows)
+    uint64_t pin_off_cap = 0;
+    // Outgrown staging blocks, freed with the slot: cudaFreeHost waits for
+    // the whole device, which would stall the worker behind the other slots.
+    std::vector<void *> retired;
     ~ServeSlot() {
         if (pin) cudaFreeHost(pin);
+        if (pin_off) cudaFreeHost(pin_off);
+        for (void *q : retired) cudaFreeHost(q);
+    }
+    // Grows a pinned block to hold `need` elements (half as much again).
+    template <class T>
+    slm_status grow(T *&buf, uint64_t &cap, uint64_t need) {
+        if (need <= cap) return SLM_OK;
+        if (buf) retired.push_back(buf);
+        buf = nullptr;
+        cap = 0;
+        const uint64_t want = need + need / 2;
+        SLM_CU(cudaMallocHost(reinterpret_cast<void **>(&buf), sizeof(T) * want));
+        cap = want;
+        return SLM_OK;
     }
 };
 
@@ -1813,18 +1832,17 @@ slm_status serve_read_results(ServeSlot *s, std::vector<uint64_t> &off) {
     slm_plan *p = &s->plan;
     SLM_CU(cudaStreamSynchronize(p->stream));
     SLM_TRY(check_status_word(p));
-    off.resize(p->np + 1);
-    SLM_CU(cudaMemcpy(off.data(), p->d_offsets.p, sizeof(uint64_t) * (p->np + 1), cudaMemcpyDeviceToHost));
+    SLM_TRY(s->grow(s->pin_off, s->pin_off_cap, p->np + 1));
+    SLM_CU(cudaMemcpyAsync(s->pin_off, p->d_offsets.p, sizeof(uint64_t) * (p->np + 1), cudaMemcpyDeviceToHost,
+                           p->stream));
+    SLM_CU(cudaStreamSynchronize(p->stream));
+    off.assign(s->pin_off, s->pin_off + p->np + 1);
     const uint64_t total = off[p->np];
-    if (total > s->pin_cap) {
-        if (s->pin) cudaFreeHost(s->pin);
-        s->pin = nullptr;
-        s->pin_cap = 0;
-        const uint64_t want = total + total / 2;
-        SLM_CU(cudaMallocHost(reinterpret_cast<void **>(&s->pin), sizeof(slm_pair) * want));
-        s->pin_cap = want;
+    SLM_TRY(s->grow(s->pin, s->pin_cap, total));
+    if (total) {
+        SLM_CU(cudaMemcpyAsync(s->pin, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost, p->stream));
+        SLM_CU(cudaStreamSynchronize(p->stream));
     }
-    if (total) SLM_CU(cudaMemcpy(s->pin, p->d_dense.p, sizeof(slm_pair) * total, cudaMemcpyDeviceToHost));
     return SLM_OK;
 }
 
@@ -2081,6 +2099,10 @@ extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server 
             cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess)
             s = fail(SLM_CUDA_ERROR, "stream/event creation failed");
         sl->plan.ctx = srv->ctx;
+        // staging for a full batch of typical pairs (up to 2048 matches each),
+        // so a burst does not grow pinned memory while other slots run
+        if (s == SLM_OK) s = sl->grow(sl->pin, sl->pin_cap, uint64_t(srv->opts.max_batch_pairs) * 1366);
+        if (s == SLM_OK) s = sl->grow(sl->pin_off, sl->pin_off_cap, uint64_t(srv->opts.max_batch_pairs) + 1);
     }
     if (s != SLM_OK) {
         std::string keep = g_last_error;
