@@ -380,6 +380,57 @@ slm_status slm_server_stats_get(slm_server *srv, slm_server_stats *st);
  * releases it; other requests are unaffected. */
 slm_status slm_server_cancel(slm_server *srv, uint64_t ticket);
 
+/* ------------------------------------------------ descriptor producer */
+
+/* Keypoint (features.rs:296-304): input-image pixels, scale sigma, DoG
+ * response, dominant orientation in radians [0, 2 pi). */
+typedef struct {
+    float x, y, sigma, response, angle;
+} slm_keypoint;
+
+/* DetectorConfig (features.rs:253-293). */
+typedef struct {
+    uint32_t octaves;       /* at most 16 */
+    uint32_t scales;        /* intervals per octave s (DoG layers s + 2), 1..32 */
+    float sigma0;
+    float contrast;         /* minimum |DoG| (brightness in [0, 1]) */
+    float edge_ratio;       /* principal curvature ratio bound r */
+    uint32_t max_features;
+    uint32_t upscale_below; /* 0: never detect on the 2x upsampled image */
+    int32_t upscale_fill;
+} slm_detector_config;
+
+/* DetectorConfig::default() (features.rs:278-293). */
+void slm_detector_config_default(slm_detector_config *cfg);
+
+/* detect_and_describe (features.rs:594) for n gray images of w x h pixels
+ * (row-major f32, GrayImage::data; host or device memory), run together on
+ * the GPU: Gaussian pyramid, DoG extrema refined to sub-pixel and sub-scale,
+ * contrast and edge tests, dominant orientations, 128-d descriptors, the
+ * |response| order and max_features cut, and for images below upscale_below
+ * that found too few features, the de-duplicated features of the 2x
+ * upsampled image. Image k's features are kps[off[k] .. off[k+1]) and rows
+ * off[k] .. off[k+1]) of desc (n_features x 128 floats; host or device
+ * memory); off has n + 1 entries and is always written. SLM_CAPACITY when
+ * off[n] > cap (nothing else is written). kps or desc may be NULL.
+ * Arithmetic follows the reference's f32 operation order; its per-pixel and
+ * per-keypoint exp, atan2, powf, cos and sin are evaluated correctly rounded,
+ * where the reference calls the platform's float functions (equal wherever
+ * those are correctly rounded). Images up to 32767 pixels a side. */
+slm_status slm_detect_and_describe(slm_ctx *ctx, const float *imgs, uint32_t n, uint32_t w, uint32_t h,
+                                   const slm_detector_config *cfg, slm_keypoint *kps, float *desc, uint64_t cap,
+                                   uint64_t *off);
+/* The same from interleaved 8-bit RGB images (n x h x w x 3 bytes), converted
+ * on the device as GrayImage::from_rgb (features.rs:165-189) does. */
+slm_status slm_detect_and_describe_rgb8(slm_ctx *ctx, const uint8_t *rgb, uint32_t n, uint32_t w, uint32_t h,
+                                        const slm_detector_config *cfg, slm_keypoint *kps, float *desc,
+                                        uint64_t cap, uint64_t *off);
+/* describe(img, x, y, sigma, angle) (features.rs:509) for n keypoints of one
+ * gray image (response ignored; 0 < sigma <= 64, |x|, |y| <= 1e6): desc is
+ * n x 128 floats (host or device memory). */
+slm_status slm_describe(slm_ctx *ctx, const float *img, uint32_t w, uint32_t h, const slm_keypoint *kps, uint32_t n,
+                        float *desc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SRC = os.path.join(HERE, "oracle.c")
+SRCS = [SRC, os.path.join(HERE, "features.c")]
 
 _lock = threading.Lock()
 _lib = None
@@ -28,11 +29,11 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile oracle.c with gcc (-O3, no FMA contraction) into _build/liboracle.so."""
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(f) for f in SRCS):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = ["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-o", tmp, SRC, "-lm", "-lpthread"]
+           "-o", tmp, *SRCS, "-lm", "-lpthread"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB
@@ -86,6 +87,20 @@ def lib():
             L.orc_match_pairs.argtypes = [f32p, P(ctypes.c_int64), P(ctypes.c_int64), u32p, i64, ctypes.c_float,
                                           ctypes.c_int, ctypes.c_int, P(ctypes.c_int64)]
             L.orc_match_pairs.restype = i64
+            i32 = ctypes.c_int
+            f32 = ctypes.c_float
+            L.orc_blur_taps.argtypes = [f32, f32p]
+            L.orc_blur_taps.restype = i64
+            L.orc_gaussian_blur.argtypes = [f32p, i64, i64, f32, f32p]
+            L.orc_upsample2.argtypes = [f32p, i64, i64, f32p]
+            L.orc_gray_from_rgb8.argtypes = [P(ctypes.c_uint8), i64, f32p]
+            L.orc_orientations.argtypes = [f32p, f32p, i64, i64, f32, f32, f32, i32, f32p]
+            L.orc_orientations.restype = i64
+            L.orc_describe.argtypes = [f32p, i64, i64, f32, f32, f32, f32, i32, f32p]
+            L.orc_dominant_orientations.argtypes = [f32p, i64, i64, f32, f32, f32, i32, f32p]
+            L.orc_dominant_orientations.restype = i64
+            L.orc_detect_and_describe.argtypes = [f32p, i64, i64, ctypes.c_void_p, i32, f32p, f32p, i64]
+            L.orc_detect_and_describe.restype = i64
             _lib = L
     return _lib
 
@@ -281,3 +296,92 @@ def sampson_score(pts, pair_off, thresh, E, hyp_pair, mask_off=None, threads: in
                             None if mo is None else _p(mo, ctypes.c_uint64),
                             None if masks is None else _p(masks, ctypes.c_uint32), int(threads))
     return counts, masks
+
+
+# ---- descriptor producer (features.c; crates/core/src/features.rs) -------
+
+class DetectorConfig(ctypes.Structure):
+    """DetectorConfig (features.rs:253-293), defaults of `Default` (:278-293)."""
+    _fields_ = [("octaves", ctypes.c_int64), ("scales", ctypes.c_int64), ("sigma0", ctypes.c_float),
+                ("contrast", ctypes.c_float), ("edge_ratio", ctypes.c_float), ("max_features", ctypes.c_int64),
+                ("upscale_below", ctypes.c_int64), ("upscale_fill", ctypes.c_int)]
+
+    def __init__(self, octaves=4, scales=3, sigma0=1.6, contrast=0.01, edge_ratio=10.0, max_features=8192,
+                 upscale_below=800, upscale_fill=False):
+        super().__init__(octaves, scales, sigma0, contrast, edge_ratio, max_features, upscale_below,
+                         int(bool(upscale_fill)))
+
+
+def _img(img) -> np.ndarray:
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    assert img.ndim == 2
+    return img
+
+
+def gray_from_rgb8(rgb) -> np.ndarray:
+    """GrayImage::from_rgb (features.rs:165-189): (0.299 r + 0.587 g + 0.114 b) / 255 in f32."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w, _ = rgb.shape
+    out = np.empty((h, w), np.float32)
+    lib().orc_gray_from_rgb8(_p(rgb, ctypes.c_uint8), h * w, _p(out, ctypes.c_float))
+    return out
+
+
+def blur_taps(sigma: float) -> np.ndarray:
+    """gaussian_blur's normalised taps (features.rs:215-220)."""
+    k = np.empty(4096, np.float32)
+    r = lib().orc_blur_taps(ctypes.c_float(sigma), _p(k, ctypes.c_float))
+    return k[:2 * r + 1].copy()
+
+
+def gaussian_blur(img, sigma: float) -> np.ndarray:
+    """gaussian_blur (features.rs:214-250)."""
+    img = _img(img)
+    out = np.empty_like(img)
+    lib().orc_gaussian_blur(_p(img, ctypes.c_float), img.shape[1], img.shape[0], ctypes.c_float(sigma),
+                            _p(out, ctypes.c_float))
+    return out
+
+
+def upsample2(img) -> np.ndarray:
+    """GrayImage::upsample2 (features.rs:62-85)."""
+    img = _img(img)
+    out = np.empty((img.shape[0] * 2, img.shape[1] * 2), np.float32)
+    lib().orc_upsample2(_p(img, ctypes.c_float), img.shape[1], img.shape[0], _p(out, ctypes.c_float))
+    return out
+
+
+def dominant_orientations(img, x: float, y: float, sigma: float, cr: bool = False) -> np.ndarray:
+    """dominant_orientations (features.rs:314-323); cr: transcendental
+    functions correctly rounded through double (as the GPU), else the
+    platform's float functions (as the reference)."""
+    img = _img(img)
+    out = np.empty(36, np.float32)
+    n = lib().orc_dominant_orientations(_p(img, ctypes.c_float), img.shape[1], img.shape[0], ctypes.c_float(x),
+                                        ctypes.c_float(y), ctypes.c_float(sigma), int(cr), _p(out, ctypes.c_float))
+    return out[:n].copy()
+
+
+def describe(img, x: float, y: float, sigma: float, angle: float, cr: bool = False) -> np.ndarray:
+    """describe (features.rs:509-592)."""
+    img = _img(img)
+    out = np.empty(128, np.float32)
+    lib().orc_describe(_p(img, ctypes.c_float), img.shape[1], img.shape[0], ctypes.c_float(x), ctypes.c_float(y),
+                       ctypes.c_float(sigma), ctypes.c_float(angle), int(cr), _p(out, ctypes.c_float))
+    return out
+
+
+def detect_and_describe(img, cfg: DetectorConfig | None = None, cr: bool = False):
+    """detect_and_describe (features.rs:594-648) -> (keypoints (n, 5): x, y,
+    sigma, response, angle; descriptors (n, 128))."""
+    img = _img(img)
+    cfg = cfg or DetectorConfig()
+    L = lib()
+    h, w = img.shape
+    cap = max(int(cfg.max_features), 1)  # the original features plus the added ones never exceed it
+    kps = np.empty((cap, 5), np.float32)
+    desc = np.empty((cap, 128), np.float32)
+    n = L.orc_detect_and_describe(_p(img, ctypes.c_float), w, h, ctypes.byref(cfg), int(cr),
+                                  _p(kps, ctypes.c_float), _p(desc, ctypes.c_float), cap)
+    assert n <= cap
+    return kps[:n].copy(), desc[:n].copy()

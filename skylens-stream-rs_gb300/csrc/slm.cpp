@@ -694,6 +694,10 @@ struct Workspace {
     slm_plan plan;
     DevBuf single;                   // FP32 single-pair calls: inputs and scratch
     DevBuf score;                    // slm_sampson_score: inputs and outputs
+    DevBuf feat_in;                  // descriptor producer: the batch's images
+    DevBuf feat_up;                  // the images it upsamples 2x, and their upsampling
+    DevBuf feat_pyr;                 // its pyramid, gradient tables and candidates
+    DevBuf feat_desc[2];             // its descriptors (input-size and upsampled detections) and jobs
     unsigned char *single_host = nullptr;  // their result block: pinned host memory the kernels write
     size_t single_host_bytes = 0;
 };
@@ -2666,4 +2670,515 @@ extern "C" slm_status slm_ctx_coalescing_stats(slm_ctx *c, uint64_t *batches, ui
     *calls = co->pairs;
     *max_batch = co->max_batch;
     return SLM_OK;
+}
+
+// ----------------------------------------------------- descriptor producer
+//
+// detect_and_describe (features.rs:594-648) over a batch of images of one
+// size. The pyramid, gradient tables, extrema, orientations and descriptors
+// run on the device (k_features.cu); the host makes the per-layer blur taps
+// with the platform's expf and the scale step with its powf (the reference
+// computes these scalars with the same library calls), orders the candidates
+// as the reference emits them, applies its stable sort by |response| and the
+// max_features cut, and runs the upsampled detection's de-duplication.
+
+namespace {
+
+// gaussian_blur's taps (features.rs:215-220)
+slm_status make_blur_taps(float sigma, BlurTaps &t) {
+    float rf = std::ceil(3.0f * sigma);
+    if (!(rf >= 1.0f)) rf = 1.0f;  // f32::max(1.0), NaN included
+    if (!(rf <= (float)kMaxBlurR)) return fail(SLM_INVALID_ARG, "blur radius ceil(3 sigma) above 127");
+    const int r = (int)rf;
+    for (int i = -r; i <= r; ++i) t.k[i + r] = expf((float)(-(i * i)) / (2.0f * sigma * sigma));
+    float sum = -0.0f;
+    for (int i = 0; i < 2 * r + 1; ++i) sum += t.k[i];
+    for (int i = 0; i < 2 * r + 1; ++i) t.k[i] /= sum;
+    t.r = r;
+    return SLM_OK;
+}
+
+// f32::powi with a run-time exponent (compiler-rt __powisf2: square and
+// multiply over the exponent's bits)
+float powi_f32(float a, int b) {
+    const bool recip = b < 0;
+    float r = 1.0f;
+    for (;;) {
+        if (b & 1) r *= a;
+        b /= 2;
+        if (b == 0) break;
+        a *= a;
+    }
+    return recip ? 1.0f / r : r;
+}
+
+uint64_t feat_align(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+// One detect_core over a batch (its device state stays in `pyr` until the
+// next run): the kept features of every image, in the reference's order.
+struct FeatCore {
+    std::vector<OctaveGeom> geom;
+    std::vector<FeatCand> cands;
+    std::vector<float> angles;  // kMaxAngles per candidate
+    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> kept;  // per image: (candidate, angle slot)
+    // device addresses inside pyr
+    float2 *d_grads = nullptr;
+    FeatCand *d_cands = nullptr;
+    OctaveGeom *d_geom = nullptr;
+    int s = 0;
+};
+
+slm_status feat_core(slm_ctx *c, cudaStream_t st, DevBuf &pyr, const float *d_img, uint32_t n, int w, int h,
+                     const slm_detector_config &cfg, float in_sigma, FeatCore &out) {
+    out = FeatCore();
+    out.kept.assign(n, {});
+    const int s = (int)cfg.scales, ng = s + 3;
+    out.s = s;
+    {
+        int wo = w, ho = h;
+        uint64_t goff = 0;
+        for (uint32_t o = 0; o < cfg.octaves; ++o) {
+            if (wo < 16 || ho < 16) break;
+            OctaveGeom g{};
+            g.w = wo;
+            g.h = ho;
+            g.layer_stride = (uint64_t)wo * ho;
+            g.grad_off = goff;
+            goff += (uint64_t)n * s * g.layer_stride;
+            out.geom.push_back(g);
+            wo /= 2;
+            ho /= 2;
+        }
+    }
+    if (out.geom.empty() || n == 0) return SLM_OK;
+    const uint64_t wh0 = out.geom[0].layer_stride;
+    const uint64_t wh1 = out.geom.size() > 1 ? out.geom[1].layer_stride : 0;
+    uint64_t ngrad = 0;
+    for (const OctaveGeom &g : out.geom) ngrad += (uint64_t)n * s * g.layer_stride;
+    uint32_t cap = std::max<uint32_t>(4096, std::min<uint64_t>(uint64_t(n) * 16384, 1u << 26));
+    const float kstep = powf(2.0f, 1.0f / (float)s);
+    float sb = cfg.sigma0 * cfg.sigma0 - in_sigma * in_sigma;
+    if (!(sb >= 0.01f)) sb = 0.01f;  // f32::max(0.01)
+    const float sigma_base = std::sqrt(sb);
+    const float er1 = cfg.edge_ratio + 1.0f;
+    const float edge_thr = er1 * er1 / cfg.edge_ratio;
+    std::vector<BlurTaps> taps(ng);
+    SLM_TRY(make_blur_taps(sigma_base, taps[0]));
+    for (int i = 1; i < ng; ++i) {
+        const float prev = cfg.sigma0 * powi_f32(kstep, i - 1);
+        const float cur = prev * kstep;
+        SLM_TRY(make_blur_taps(std::sqrt(cur * cur - prev * prev), taps[i]));
+    }
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const uint64_t o_geom = 0, o_gauss = feat_align(o_geom + sizeof(OctaveGeom) * out.geom.size()),
+                       o_dog = feat_align(o_gauss + 4 * (uint64_t)n * ng * wh0),
+                       o_tmp = feat_align(o_dog + 4 * (uint64_t)n * (ng - 1) * wh0),
+                       o_base = feat_align(o_tmp + 4 * (uint64_t)n * wh0),
+                       o_grad = feat_align(o_base + 4 * (uint64_t)n * wh1),
+                       o_cand = feat_align(o_grad + 8 * ngrad), o_cnt = feat_align(o_cand + sizeof(FeatCand) * cap),
+                       o_ang = feat_align(o_cnt + 16), o_nang = feat_align(o_ang + 4ull * kMaxAngles * cap),
+                       bytes = feat_align(o_nang + cap);
+        SLM_TRY(pyr.ensure(c, bytes));
+        unsigned char *d = pyr.as<unsigned char>();
+        float *gauss = reinterpret_cast<float *>(d + o_gauss), *dog = reinterpret_cast<float *>(d + o_dog),
+              *tmp = reinterpret_cast<float *>(d + o_tmp), *base = reinterpret_cast<float *>(d + o_base);
+        out.d_geom = reinterpret_cast<OctaveGeom *>(d + o_geom);
+        out.d_grads = reinterpret_cast<float2 *>(d + o_grad);
+        out.d_cands = reinterpret_cast<FeatCand *>(d + o_cand);
+        uint32_t *d_count = reinterpret_cast<uint32_t *>(d + o_cnt);
+        float *d_ang = reinterpret_cast<float *>(d + o_ang);
+        uint8_t *d_nang = reinterpret_cast<uint8_t *>(d + o_nang);
+        SLM_CU(cudaMemcpyAsync(out.d_geom, out.geom.data(), sizeof(OctaveGeom) * out.geom.size(),
+                               cudaMemcpyHostToDevice, st));
+        SLM_CU(cudaMemsetAsync(d_count, 0, 4, st));
+        for (size_t o = 0; o < out.geom.size(); ++o) {
+            const OctaveGeom &G = out.geom[o];
+            const uint64_t wh = G.layer_stride;
+            if (o == 0) {
+                launch_blur(d_img, tmp, gauss, nullptr, nullptr, G.w, G.h, (int)n, wh, ng * wh, 0, taps[0], st);
+            } else {
+                const OctaveGeom &P = out.geom[o - 1];
+                launch_downsample(gauss + s * P.layer_stride, base, P.w, P.h, (int)n, ng * P.layer_stride, wh, st);
+                SLM_CU(cudaMemcpy2DAsync(gauss, 4 * ng * wh, base, 4 * wh, 4 * wh, n, cudaMemcpyDeviceToDevice, st));
+            }
+            for (int i = 1; i < ng; ++i)
+                launch_blur(gauss + (i - 1) * wh, tmp, gauss + i * wh, gauss + (i - 1) * wh, dog + (i - 1) * wh, G.w,
+                            G.h, (int)n, ng * wh, ng * wh, (ng - 1) * wh, taps[i], st);
+            launch_grad(gauss, out.d_grads + G.grad_off, G.w, G.h, s, ng * wh, 1, (int)n, st);
+            ExtremaArgs ea{};
+            ea.dog = dog;
+            ea.layer_stride = wh;
+            ea.w = G.w;
+            ea.h = G.h;
+            ea.s = s;
+            ea.ng = ng;
+            ea.octave = (int)o;
+            ea.contrast = cfg.contrast;
+            ea.edge_thr = edge_thr;
+            ea.sigma0 = cfg.sigma0;
+            ea.kstep = kstep;
+            ea.cands = out.d_cands;
+            ea.count = d_count;
+            ea.cap = cap;
+            launch_extrema(ea, (int)n, st);
+        }
+        SLM_CU(cudaGetLastError());
+        uint32_t count = 0;
+        SLM_CU(cudaMemcpyAsync(&count, d_count, 4, cudaMemcpyDeviceToHost, st));
+        SLM_CU(cudaStreamSynchronize(st));
+        if (count > cap) {  // the list overflowed: run again with room for every candidate
+            if (attempt) return fail(SLM_INTERNAL, "feature candidates overflowed twice");
+            cap = count;
+            continue;
+        }
+        OrientArgs oa{};
+        oa.cands = out.d_cands;
+        oa.count = d_count;
+        oa.cap = cap;
+        oa.grads = out.d_grads;
+        oa.geom = out.d_geom;
+        oa.s = s;
+        oa.angles = d_ang;
+        oa.nang = d_nang;
+        launch_orient(oa, count, st);
+        SLM_CU(cudaGetLastError());
+        out.cands.resize(count);
+        out.angles.resize((size_t)count * kMaxAngles);
+        std::vector<uint8_t> nang(count);
+        if (count) {
+            SLM_CU(cudaMemcpyAsync(out.cands.data(), out.d_cands, sizeof(FeatCand) * count, cudaMemcpyDeviceToHost,
+                                   st));
+            SLM_CU(cudaMemcpyAsync(out.angles.data(), d_ang, 4ull * kMaxAngles * count, cudaMemcpyDeviceToHost, st));
+            SLM_CU(cudaMemcpyAsync(nang.data(), d_nang, count, cudaMemcpyDeviceToHost, st));
+        }
+        SLM_CU(cudaStreamSynchronize(st));
+        // the reference's emission order (octave, layer, row, column of the
+        // scanned extremum; angles in bin order), then its stable sort by
+        // |response| descending (f32::total_cmp of abs(): the bits of |v|) and
+        // the max_features cut (features.rs:776-778)
+        std::vector<std::vector<uint32_t>> by_img(n);
+        for (uint32_t i = 0; i < count; ++i) by_img[out.cands[i].img].push_back(i);
+        for (uint32_t k = 0; k < n; ++k) {
+            std::vector<uint32_t> &ci = by_img[k];
+            std::sort(ci.begin(), ci.end(), [&](uint32_t a, uint32_t b) { return out.cands[a].key < out.cands[b].key; });
+            std::vector<std::pair<uint32_t, uint32_t>> f;
+            for (uint32_t i : ci)
+                for (uint32_t a = 0; a < nang[i]; ++a) f.emplace_back(i, a);
+            auto mag = [&](uint32_t i) {
+                uint32_t u;
+                std::memcpy(&u, &out.cands[i].value, 4);
+                return u & 0x7fffffffu;
+            };
+            std::stable_sort(f.begin(), f.end(), [&](const std::pair<uint32_t, uint32_t> &a,
+                                                     const std::pair<uint32_t, uint32_t> &b) {
+                return mag(a.first) > mag(b.first);
+            });
+            if (f.size() > cfg.max_features) f.resize(cfg.max_features);
+            out.kept[k] = std::move(f);
+        }
+        return SLM_OK;
+    }
+    return fail(SLM_INTERNAL, "feature candidates overflowed");
+}
+
+// Keypoint of a kept feature in input-image pixels (features.rs:755-763).
+slm_keypoint feat_keypoint(const FeatCore &fc, uint32_t cand, uint32_t a) {
+    const FeatCand &c = fc.cands[cand];
+    const float scale = (float)(1ull << c.octave);
+    slm_keypoint k;
+    k.x = c.x * scale;
+    k.y = c.y * scale;
+    k.sigma = c.sig * scale;
+    k.response = c.value;
+    k.angle = fc.angles[(size_t)cand * kMaxAngles + a];
+    return k;
+}
+
+// Descriptors of the listed features of one run, into rows 0.. of `buf`
+// (after its job table).
+slm_status feat_describe(slm_ctx *c, cudaStream_t st, DevBuf &buf, const FeatCore &fc,
+                         const std::vector<std::pair<uint32_t, uint32_t>> &list, float **d_desc) {
+    *d_desc = nullptr;
+    if (list.empty()) return SLM_OK;
+    const uint64_t o_jobs = 0, o_desc = feat_align(sizeof(DescJob) * list.size()),
+                   bytes = o_desc + 4ull * kDesc * list.size();
+    SLM_TRY(buf.ensure(c, bytes));
+    std::vector<DescJob> jobs(list.size());
+    for (size_t i = 0; i < list.size(); ++i) {
+        jobs[i].cand = list[i].first;
+        jobs[i].angle = fc.angles[(size_t)list[i].first * kMaxAngles + list[i].second];
+        jobs[i].out_row = (uint32_t)i;
+        jobs[i].pad = 0;
+    }
+    unsigned char *d = buf.as<unsigned char>();
+    SLM_CU(cudaMemcpyAsync(d + o_jobs, jobs.data(), sizeof(DescJob) * jobs.size(), cudaMemcpyHostToDevice, st));
+    DescribeArgs da{};
+    da.jobs = reinterpret_cast<const DescJob *>(d + o_jobs);
+    da.cands = fc.d_cands;
+    da.grads = fc.d_grads;
+    da.geom = fc.d_geom;
+    da.s = fc.s;
+    da.desc = reinterpret_cast<float *>(d + o_desc);
+    launch_describe(da, (uint32_t)jobs.size(), st);
+    SLM_CU(cudaGetLastError());
+    // the job table is read by the kernel before the host vector goes away
+    SLM_CU(cudaStreamSynchronize(st));
+    *d_desc = da.desc;
+    return SLM_OK;
+}
+
+slm_status check_detector_config(const slm_detector_config *cfg) {
+    if (!cfg) return fail(SLM_INVALID_ARG, "NULL detector config");
+    if (cfg->scales < 1 || cfg->scales > 32) return fail(SLM_INVALID_ARG, "scales must be in 1..32");
+    if (cfg->octaves > 16) return fail(SLM_INVALID_ARG, "octaves must be at most 16");
+    if (!(cfg->sigma0 > 0.0f) || !std::isfinite(cfg->sigma0)) return fail(SLM_INVALID_ARG, "sigma0 must be > 0");
+    if (!std::isfinite(cfg->contrast) || !std::isfinite(cfg->edge_ratio) || !(cfg->edge_ratio > 0.0f))
+        return fail(SLM_INVALID_ARG, "contrast and edge_ratio must be finite, edge_ratio > 0");
+    return SLM_OK;
+}
+
+// Shared body of the gray and RGB8 entry points; d_gray holds the n images.
+slm_status detect_describe_dev(slm_ctx *c, Workspace *ws, const float *d_gray, uint32_t n, uint32_t w, uint32_t h,
+                               const slm_detector_config &cfg, slm_keypoint *kps, float *desc, uint64_t cap,
+                               uint64_t *off) {
+    cudaStream_t st = ws->stream;
+    FeatCore run;
+    SLM_TRY(feat_core(c, st, ws->feat_pyr, d_gray, n, (int)w, (int)h, cfg, 0.5f, run));
+    std::vector<std::pair<uint32_t, uint32_t>> all1;
+    std::vector<uint64_t> first1(n + 1, 0);
+    for (uint32_t k = 0; k < n; ++k) {
+        first1[k] = all1.size();
+        all1.insert(all1.end(), run.kept[k].begin(), run.kept[k].end());
+    }
+    first1[n] = all1.size();
+    float *d_desc1 = nullptr;
+    SLM_TRY(feat_describe(c, st, ws->feat_desc[0], run, all1, &d_desc1));
+    std::vector<std::vector<slm_keypoint>> kp(n);
+    for (uint32_t k = 0; k < n; ++k)
+        for (const auto &f : run.kept[k]) kp[k].push_back(feat_keypoint(run, f.first, f.second));
+    // the 2x upsampled detection of small images short of features
+    // (features.rs:595-647)
+    std::vector<uint32_t> up;
+    const uint32_t big = std::max(w, h);
+    if (!(cfg.upscale_below == 0 || big >= cfg.upscale_below))
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint64_t nk = kp[k].size();
+            if (nk >= cfg.max_features || (!cfg.upscale_fill && nk * 2 >= cfg.max_features)) continue;
+            up.push_back(k);
+        }
+    std::vector<std::vector<slm_keypoint>> kp2(n);
+    std::vector<uint64_t> first2(n + 1, 0);
+    std::vector<std::pair<uint32_t, uint32_t>> all2;
+    float *d_desc2 = nullptr;
+    if (!up.empty()) {
+        const uint64_t wh = (uint64_t)w * h, nu = up.size();
+        // the images to upsample, gathered, then their upsampling
+        const uint64_t o_up = feat_align(4 * nu * wh) / 4;
+        SLM_TRY(ws->feat_up.ensure(c, 4 * (o_up + 4 * nu * wh)));
+        float *fu = ws->feat_up.as<float>();
+        for (uint64_t q = 0; q < nu; ++q)
+            SLM_CU(cudaMemcpyAsync(fu + q * wh, d_gray + up[q] * wh, 4 * wh, cudaMemcpyDeviceToDevice, st));
+        launch_upsample2(fu, fu + o_up, (int)w, (int)h, (int)nu, st);
+        SLM_CU(cudaGetLastError());
+        FeatCore run2;
+        SLM_TRY(feat_core(c, st, ws->feat_pyr, fu + o_up, (uint32_t)nu, 2 * (int)w, 2 * (int)h, cfg, 1.0f, run2));
+        const float cell = 4.0f;
+        const int64_t gw = (int64_t)((float)w / cell) + 2, gh = (int64_t)((float)h / cell) + 2;
+        auto key = [&](float x, float y) {
+            return std::make_pair(std::clamp<int64_t>((int64_t)std::floor(x / cell), -1, gw - 1),
+                                  std::clamp<int64_t>((int64_t)std::floor(y / cell), -1, gh - 1));
+        };
+        for (uint64_t q = 0; q < nu; ++q) {
+            const uint32_t k = up[q];
+            const uint64_t need = cfg.max_features - kp[k].size();
+            std::map<std::pair<int64_t, int64_t>, std::vector<const slm_keypoint *>> grid;
+            for (const slm_keypoint &o : kp[k]) grid[key(o.x, o.y)].push_back(&o);
+            first2[k] = all2.size();
+            for (const auto &f : run2.kept[q]) {
+                if (kp2[k].size() >= need) break;
+                slm_keypoint e = feat_keypoint(run2, f.first, f.second);
+                e.x = e.x / 2.0f - 0.25f;
+                e.y = e.y / 2.0f - 0.25f;
+                e.sigma /= 2.0f;
+                const auto kk = key(e.x, e.y);
+                bool dup = false;
+                for (int64_t i = kk.first - 1; i <= kk.first + 1 && !dup; ++i)
+                    for (int64_t j = kk.second - 1; j <= kk.second + 1 && !dup; ++j) {
+                        auto it = grid.find({i, j});
+                        if (it == grid.end()) continue;
+                        for (const slm_keypoint *o : it->second) {
+                            const float r = std::fmax(o->sigma / e.sigma, e.sigma / o->sigma);
+                            if (hypotf(o->x - e.x, o->y - e.y) <= 1.0f && r <= 1.5f) {
+                                dup = true;
+                                break;
+                            }
+                        }
+                    }
+                if (!dup) {
+                    kp2[k].push_back(e);
+                    all2.push_back(f);
+                }
+            }
+        }
+        // first2 as offsets into all2 by image (images without upsampling add nothing)
+        uint64_t acc = 0;
+        for (uint32_t k = 0; k < n; ++k) {
+            first2[k] = acc;
+            acc += kp2[k].size();
+        }
+        first2[n] = acc;
+        SLM_TRY(feat_describe(c, st, ws->feat_desc[1], run2, all2, &d_desc2));
+    }
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        off[k] = total;
+        total += kp[k].size() + kp2[k].size();
+    }
+    off[n] = total;
+    if (total > cap) return fail(SLM_CAPACITY, "feature output holds " + std::to_string(cap) + " of " +
+                                                   std::to_string(total) + " features");
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint64_t n1 = kp[k].size(), n2 = kp2[k].size();
+        if (kps) {
+            std::memcpy(kps + off[k], kp[k].data(), sizeof(slm_keypoint) * n1);
+            if (n2) std::memcpy(kps + off[k] + n1, kp2[k].data(), sizeof(slm_keypoint) * n2);
+        }
+        if (desc) {
+            if (n1)
+                SLM_CU(cudaMemcpyAsync(desc + off[k] * kDesc, d_desc1 + first1[k] * kDesc, 4ull * kDesc * n1,
+                                       cudaMemcpyDefault, st));
+            if (n2)
+                SLM_CU(cudaMemcpyAsync(desc + (off[k] + n1) * kDesc, d_desc2 + first2[k] * kDesc, 4ull * kDesc * n2,
+                                       cudaMemcpyDefault, st));
+        }
+    }
+    SLM_CU(cudaStreamSynchronize(st));
+    return SLM_OK;
+}
+
+slm_status feat_entry_checks(slm_ctx *c, const void *imgs, uint32_t n, uint32_t w, uint32_t h,
+                             const slm_detector_config *cfg, uint64_t *off) {
+    if (!c || !off) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (n && !imgs) return fail(SLM_INVALID_ARG, "NULL images");
+    if (n > 65535) return fail(SLM_INVALID_ARG, "at most 65535 images per call");
+    if (w > 32767 || h > 32767) return fail(SLM_INVALID_ARG, "images up to 32767 pixels a side");
+    return check_detector_config(cfg);
+}
+
+}  // namespace
+
+extern "C" void slm_detector_config_default(slm_detector_config *cfg) {
+    if (!cfg) return;
+    cfg->octaves = 4;
+    cfg->scales = 3;
+    cfg->sigma0 = 1.6f;
+    cfg->contrast = 0.01f;
+    cfg->edge_ratio = 10.0f;
+    cfg->max_features = 8192;
+    cfg->upscale_below = 800;
+    cfg->upscale_fill = 0;
+}
+
+extern "C" slm_status slm_detect_and_describe(slm_ctx *c, const float *imgs, uint32_t n, uint32_t w, uint32_t h,
+                                              const slm_detector_config *cfg, slm_keypoint *kps, float *desc,
+                                              uint64_t cap, uint64_t *off) {
+    NvtxRange range_("slm_detect_and_describe");
+    SLM_TRY(feat_entry_checks(c, imgs, n, w, h, cfg, off));
+    for (uint32_t k = 0; k <= n; ++k) off[k] = 0;
+    const uint64_t wh = (uint64_t)w * h;
+    if (!n || !wh) return SLM_OK;
+    SLM_TRY(ctx_check_device(c));
+    Workspace *ws = nullptr;
+    SLM_TRY(ws_acquire(c, &ws));
+    slm_status st = ws->feat_in.ensure(c, 4 * n * wh);
+    if (st == SLM_OK && cudaMemcpyAsync(ws->feat_in.p, imgs, 4 * n * wh, cudaMemcpyDefault, ws->stream) != cudaSuccess)
+        st = fail(SLM_CUDA_ERROR, std::string("slm_detect_and_describe: ") + cudaGetErrorString(cudaGetLastError()));
+    if (st == SLM_OK) st = detect_describe_dev(c, ws, ws->feat_in.as<float>(), n, w, h, *cfg, kps, desc, cap, off);
+    if (st != SLM_OK) cudaStreamSynchronize(ws->stream);
+    ws_release(c, ws);
+    return st;
+}
+
+extern "C" slm_status slm_detect_and_describe_rgb8(slm_ctx *c, const uint8_t *rgb, uint32_t n, uint32_t w,
+                                                   uint32_t h, const slm_detector_config *cfg, slm_keypoint *kps,
+                                                   float *desc, uint64_t cap, uint64_t *off) {
+    NvtxRange range_("slm_detect_and_describe_rgb8");
+    SLM_TRY(feat_entry_checks(c, rgb, n, w, h, cfg, off));
+    for (uint32_t k = 0; k <= n; ++k) off[k] = 0;
+    const uint64_t wh = (uint64_t)w * h;
+    if (!n || !wh) return SLM_OK;
+    SLM_TRY(ctx_check_device(c));
+    Workspace *ws = nullptr;
+    SLM_TRY(ws_acquire(c, &ws));
+    // the gray images first in feat_in, the RGB bytes staged after them
+    const uint64_t o_rgb = feat_align(4 * n * wh);
+    slm_status st = ws->feat_in.ensure(c, o_rgb + 3 * n * wh);
+    unsigned char *d = ws->feat_in.as<unsigned char>();
+    if (st == SLM_OK && cudaMemcpyAsync(d + o_rgb, rgb, 3 * n * wh, cudaMemcpyDefault, ws->stream) != cudaSuccess)
+        st = fail(SLM_CUDA_ERROR, std::string("slm_detect_and_describe_rgb8: ") +
+                                      cudaGetErrorString(cudaGetLastError()));
+    if (st == SLM_OK) {
+        launch_gray_from_rgb8(d + o_rgb, reinterpret_cast<float *>(d), n * wh, ws->stream);
+        if (cudaGetLastError() != cudaSuccess) st = fail(SLM_CUDA_ERROR, "gray conversion launch failed");
+    }
+    if (st == SLM_OK) st = detect_describe_dev(c, ws, ws->feat_in.as<float>(), n, w, h, *cfg, kps, desc, cap, off);
+    if (st != SLM_OK) cudaStreamSynchronize(ws->stream);
+    ws_release(c, ws);
+    return st;
+}
+
+extern "C" slm_status slm_describe(slm_ctx *c, const float *img, uint32_t w, uint32_t h, const slm_keypoint *kps,
+                                   uint32_t n, float *desc) {
+    NvtxRange range_("slm_describe");
+    if (!c || (n && (!img || !kps || !desc))) return fail(SLM_INVALID_ARG, "NULL argument");
+    if (w > 32767 || h > 32767) return fail(SLM_INVALID_ARG, "images up to 32767 pixels a side");
+    const uint64_t wh = (uint64_t)w * h;
+    if (!n) return SLM_OK;
+    for (uint32_t i = 0; i < n; ++i)
+        if (!std::isfinite(kps[i].x) || !std::isfinite(kps[i].y) || !std::isfinite(kps[i].angle) ||
+            !(kps[i].sigma > 0.0f) || kps[i].sigma > 64.0f || std::fabs(kps[i].x) > 1e6f ||
+            std::fabs(kps[i].y) > 1e6f)
+            return fail(SLM_INVALID_ARG, "keypoints need |x|, |y| <= 1e6, a finite angle and 0 < sigma <= 64");
+    SLM_TRY(ctx_check_device(c));
+    Workspace *ws = nullptr;
+    SLM_TRY(ws_acquire(c, &ws));
+    cudaStream_t st_ = ws->stream;
+    // image, its gradient table, the geometry, keypoints, jobs, descriptors
+    const uint64_t o_img = 0, o_grad = feat_align(4 * wh), o_geom = feat_align(o_grad + 8 * wh),
+                   o_kps = feat_align(o_geom + sizeof(OctaveGeom)), o_jobs = feat_align(o_kps + sizeof(slm_keypoint) * n),
+                   o_desc = feat_align(o_jobs + sizeof(DescJob) * n), bytes = o_desc + 4ull * kDesc * n;
+    slm_status st = ws->feat_pyr.ensure(c, bytes);
+    if (st == SLM_OK) {
+        unsigned char *d = ws->feat_pyr.as<unsigned char>();
+        OctaveGeom g{};
+        g.w = (int)w;
+        g.h = (int)h;
+        g.layer_stride = wh;
+        std::vector<DescJob> jobs(n);
+        for (uint32_t i = 0; i < n; ++i) jobs[i] = DescJob{i, kps[i].angle, i, 0};
+        cudaError_t e = wh ? cudaMemcpyAsync(d + o_img, img, 4 * wh, cudaMemcpyDefault, st_) : cudaSuccess;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + o_geom, &g, sizeof g, cudaMemcpyHostToDevice, st_);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + o_kps, kps, sizeof(slm_keypoint) * n, cudaMemcpyDefault, st_);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + o_jobs, jobs.data(), sizeof(DescJob) * n, cudaMemcpyHostToDevice, st_);
+        if (e == cudaSuccess && wh) {
+            launch_grad(reinterpret_cast<const float *>(d + o_img), reinterpret_cast<float2 *>(d + o_grad), (int)w,
+                        (int)h, 1, wh, 0, 1, st_);
+            DescribeArgs da{};
+            da.jobs = reinterpret_cast<const DescJob *>(d + o_jobs);
+            da.kps = reinterpret_cast<const slm_keypoint *>(d + o_kps);
+            da.grads = reinterpret_cast<const float2 *>(d + o_grad);
+            da.geom = reinterpret_cast<const OctaveGeom *>(d + o_geom);
+            da.s = 1;
+            da.desc = reinterpret_cast<float *>(d + o_desc);
+            launch_describe(da, n, st_);
+            e = cudaGetLastError();
+        } else if (e == cudaSuccess) {
+            e = cudaMemsetAsync(d + o_desc, 0, 4ull * kDesc * n, st_);  // no pixels: every histogram is empty
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(desc, d + o_desc, 4ull * kDesc * n, cudaMemcpyDefault, st_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) st = fail(SLM_CUDA_ERROR, std::string("slm_describe: ") + cudaGetErrorString(e));
+    }
+    ws_release(c, ws);
+    return st;
 }

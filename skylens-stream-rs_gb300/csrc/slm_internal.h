@@ -157,4 +157,89 @@ struct SampsonArgs {
 };
 void launch_sampson(const SampsonArgs &a, cudaStream_t s);
 
+// ---------------------------------------------------- descriptor producer
+// (k_features.cu; crates/core/src/features.rs)
+
+constexpr int kMaxBlurR = 127;  // blur radius ceil(3 sigma) the kernels take
+constexpr int kMaxAngles = 18;  // local maxima of a 36-bin circular histogram
+
+// Normalised taps of one gaussian_blur (features.rs:215-220), made on the host.
+struct BlurTaps {
+    float k[2 * kMaxBlurR + 1];
+    int r;
+};
+
+// A refined DoG extremum that passed the contrast and edge tests.
+struct __align__(16) FeatCand {
+    float x, y;        // refined position in octave pixels
+    float sig;         // sig_oct = sigma0 * kstep^s
+    float value;       // refined DoG response
+    uint16_t img;      // image of the batch
+    uint8_t octave;
+    uint8_t layer;     // refined layer (its gradient table)
+    uint32_t pad;
+    uint64_t key;      // emission order: octave << 48 | start layer << 32 | start y << 16 | start x
+};
+
+// One octave of a batch: its size and where its gradient tables start.
+struct OctaveGeom {
+    int w, h;
+    uint64_t layer_stride;  // w * h
+    uint64_t grad_off;      // float2 offset of (image 0, layer 1)
+};
+
+struct ExtremaArgs {
+    const float *dog;       // [img][ng - 1][h][w]
+    uint64_t layer_stride;
+    int w, h, s, ng, octave;
+    float contrast, edge_thr, sigma0, kstep;
+    FeatCand *cands;
+    uint32_t *count;
+    uint32_t cap;
+};
+
+struct OrientArgs {
+    const FeatCand *cands;
+    const uint32_t *count;
+    uint32_t cap;
+    const float2 *grads;    // every octave's tables: [img][layer 1..s][h][w] at geom.grad_off
+    const OctaveGeom *geom;
+    int s;
+    float *angles;          // kMaxAngles per candidate
+    uint8_t *nang;
+};
+
+struct DescJob {
+    uint32_t cand;          // candidate (or keypoint) index
+    float angle;
+    uint32_t out_row;       // descriptor row written
+    uint32_t pad;
+};
+
+struct DescribeArgs {
+    const DescJob *jobs;
+    const FeatCand *cands;  // null: keypoints kps (image pixels) on one table, grads, geom[0]
+    const slm_keypoint *kps;
+    const float2 *grads;
+    const OctaveGeom *geom;
+    int s;
+    float *desc;
+};
+
+// Both passes of a blur of nimg images (src -> tmp -> dst); with dog, also
+// dog = dst - prev (prev strided as dst). Strides are per image, in floats.
+void launch_blur(const float *src, float *tmp, float *dst, const float *prev, float *dog, int w, int h, int nimg,
+                 uint64_t stride_src, uint64_t stride_dst, uint64_t stride_dog, const BlurTaps &t, cudaStream_t s);
+void launch_downsample(const float *src, float *dst, int w, int h, int nimg, uint64_t stride_src,
+                       uint64_t stride_dst, cudaStream_t s);
+void launch_upsample2(const float *src, float *dst, int w, int h, int nimg, cudaStream_t s);
+void launch_gray_from_rgb8(const uint8_t *rgb, float *out, uint64_t n, cudaStream_t s);
+// gradient tables of layers l0 .. l0 + s_ - 1 of each image (image k's layer l
+// at gauss + k * img_stride + l * w * h); grad: [img][s_][h][w]
+void launch_grad(const float *gauss, float2 *grad, int w, int h, int s_, uint64_t img_stride, int l0, int nimg,
+                 cudaStream_t s);
+void launch_extrema(const ExtremaArgs &a, int nimg, cudaStream_t s);
+void launch_orient(const OrientArgs &a, uint32_t n, cudaStream_t s);
+void launch_describe(const DescribeArgs &a, uint32_t njobs, cudaStream_t s);
+
 }  // namespace slm

@@ -67,6 +67,16 @@ class SlmServerStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class SlmKeypoint(ctypes.Structure):
+    _fields_ = [("x", c_f32), ("y", c_f32), ("sigma", c_f32), ("response", c_f32), ("angle", c_f32)]
+
+
+class SlmDetectorConfig(ctypes.Structure):
+    _fields_ = [("octaves", c_u32), ("scales", c_u32), ("sigma0", c_f32), ("contrast", c_f32),
+                ("edge_ratio", c_f32), ("max_features", c_u32), ("upscale_below", c_u32),
+                ("upscale_fill", ctypes.c_int32)]
+
+
 class SlmError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str):
         self.status = status
@@ -131,6 +141,14 @@ SIGNATURES = {
                                 P(SlmStats)]),
     "slm_sampson_score": (c_int, [ctypes.c_void_p, P(ctypes.c_double), P(c_u64), c_u32, P(ctypes.c_double),
                                   P(ctypes.c_double), P(c_u32), c_u32, P(c_u32), P(c_u64), P(c_u32), c_u64]),
+    "slm_detector_config_default": (None, [P(SlmDetectorConfig)]),
+    "slm_detect_and_describe": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, c_u32, c_u32,
+                                        P(SlmDetectorConfig), ctypes.c_void_p, ctypes.c_void_p, c_u64, P(c_u64)]),
+    "slm_detect_and_describe_rgb8": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, c_u32, c_u32,
+                                             P(SlmDetectorConfig), ctypes.c_void_p, ctypes.c_void_p, c_u64,
+                                             P(c_u64)]),
+    "slm_describe": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p, c_u32,
+                             ctypes.c_void_p]),
 }
 
 _lock = threading.Lock()

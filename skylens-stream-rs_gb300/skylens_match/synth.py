@@ -209,3 +209,40 @@ def essential_hypotheses(rng: np.random.Generator, e_true: np.ndarray, count: in
             _, _, e = two_view(rng, 1)
             out.append(e * 10.0 ** rng.uniform(-2, 2))
     return np.asarray(out[:count], dtype=np.float64)
+
+
+def scene_canvas(width: int, height: int, seed: int = 11, density: float = 0.004) -> np.ndarray:
+    """A seeded textured scene for the descriptor producer: gaussian spots of
+    radius 1.5-8 px and signed contrast over a slow brightness ramp, float32
+    in [0, 1]. `density` spots per pixel."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    yy, xx = np.mgrid[0:height, 0:width].astype(np.float32)
+    img = 0.45 + 0.1 * np.sin(xx / 97.0) * np.cos(yy / 61.0)
+    n = int(density * width * height)
+    cx = rng.uniform(0, width, n).astype(np.float32)
+    cy = rng.uniform(0, height, n).astype(np.float32)
+    rad = rng.uniform(1.5, 8.0, n).astype(np.float32)
+    amp = rng.uniform(-0.35, 0.35, n).astype(np.float32)
+    for k in range(n):
+        r = int(np.ceil(3.5 * rad[k]))
+        x0, x1 = max(0, int(cx[k]) - r), min(width, int(cx[k]) + r + 1)
+        y0, y1 = max(0, int(cy[k]) - r), min(height, int(cy[k]) + r + 1)
+        if x0 >= x1 or y0 >= y1:
+            continue
+        d2 = (xx[y0:y1, x0:x1] - cx[k]) ** 2 + (yy[y0:y1, x0:x1] - cy[k]) ** 2
+        img[y0:y1, x0:x1] += amp[k] * np.exp(-d2 / (2.0 * rad[k] * rad[k]))
+    return np.clip(img, 0.0, 1.0).astype(np.float32)
+
+
+def scene_views(n: int, width: int = 960, height: int = 540, step: int = 24, seed: int = 11) -> np.ndarray:
+    """n RGB8 views (n, height, width, 3) of one scene, each shifted `step`
+    pixels along x from the last (a camera moving along a facade), so
+    neighbouring views share most of their content; 8-bit quantised like
+    decoded photos, a faint colour tint per channel."""
+    canvas = scene_canvas(width + step * max(n - 1, 0), height, seed)
+    out = np.empty((n, height, width, 3), np.uint8)
+    tint = np.array([1.0, 0.97, 0.93], np.float32)
+    for k in range(n):
+        v = canvas[:, k * step:k * step + width, None] * tint
+        out[k] = np.clip(np.rint(v * 255.0), 0, 255).astype(np.uint8)
+    return out
