@@ -65,6 +65,7 @@ def parse():
                     help="serving arrival rates, views/s ('burst': every view at once, the saturated server)")
     ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
     ap.add_argument("--ransac", action="store_true", help="RANSAC hypothesis scoring (Sampson residuals)")
+    ap.add_argument("--features", action="store_true", help="descriptor producer (detect_and_describe, 960 x 540)")
     ap.add_argument("--no-scheduled", action="store_true",
                     help="skip the scheduled_pairs(PairSchedule::default()) batch with the < 20 filter")
     ap.add_argument("--no-configs", action="store_true",
@@ -413,6 +414,91 @@ def ransac_configs(m, threads: int, pairs: int = 100, hyps: int = 2000, reps: in
             "equal_counts": bool(np.array_equal(got, want))}
 
 
+def features_configs(m, threads: int, n: int = 24, reps: int = 5, cpu_images: int = 32) -> dict:
+    """The descriptor producer (features.rs:594 detect_and_describe, default
+    DetectorConfig) on `n` RGB8 views of 960 x 540, the size of the
+    pipeline's synthetic frames, of one seeded textured scene (a camera
+    moving along a facade; the reference's rendered scenes stand in). GPU:
+    slm_detect_and_describe_rgb8 on images already in HBM with descriptors
+    left in HBM (`value`), and from pinned host images to host keypoints and
+    descriptors (`e2e`). CPU: the oracle's restatement (the platform's float
+    functions, as the reference) over `cpu_images` images on all host threads,
+    one image per thread as the pipeline's par_iter does. Checks: two images
+    bit-exact against the oracle with correctly rounded functions (the GPU's
+    arithmetic), and the largest descriptor difference against the platform's."""
+    import ctypes
+    from concurrent.futures import ThreadPoolExecutor
+
+    import torch
+
+    import oracle as O
+    from skylens_match import synth
+    from skylens_match import features as F
+    w, h = 960, 540
+    views = synth.scene_views(n, w, h, seed=11)
+    cfg = F.detector_config()
+    cap = n * int(cfg.max_features)
+    L = m._L
+    off = np.zeros(n + 1, np.uint64)
+
+    def call(img_ptr, kps_ptr, desc_ptr):
+        st = L.slm_detect_and_describe_rgb8(m.handle, ctypes.c_void_p(img_ptr), n, w, h, ctypes.byref(cfg),
+                                            ctypes.c_void_p(kps_ptr), ctypes.c_void_p(desc_ptr), cap,
+                                            off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        if st:
+            raise RuntimeError(f"slm_detect_and_describe_rgb8: status {st}")
+
+    d_img = torch.from_numpy(views).cuda()
+    d_desc = torch.empty((cap, 128), dtype=torch.float32, device="cuda")
+    p_img = torch.from_numpy(views).pin_memory()
+    p_kps = torch.empty((cap, 5), dtype=torch.float32).pin_memory()
+    p_desc = torch.empty((cap, 128), dtype=torch.float32).pin_memory()
+    call(d_img.data_ptr(), p_kps.data_ptr(), d_desc.data_ptr())  # warm-up
+    dev, e2e = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        call(d_img.data_ptr(), p_kps.data_ptr(), d_desc.data_ptr())
+        dev.append(time.perf_counter() - t0)
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        call(p_img.data_ptr(), p_kps.data_ptr(), p_desc.data_ptr())
+        e2e.append(time.perf_counter() - t0)
+    nfeat = int(off[-1])
+    kps = p_kps.numpy()[:nfeat].copy()
+    desc = p_desc.numpy()[:nfeat].copy()
+    exact, maxdiff = True, 0.0
+    for k in range(2):
+        g = O.gray_from_rgb8(views[k])
+        a, b = int(off[k]), int(off[k + 1])
+        k1, d1 = O.detect_and_describe(g, cr=True)
+        exact &= bool(np.array_equal(k1, kps[a:b]) and np.array_equal(d1, desc[a:b]))
+        k0, d0 = O.detect_and_describe(g, cr=False)
+        if len(k0) == b - a:
+            maxdiff = max(maxdiff, float(np.abs(d0 - desc[a:b]).max()))
+        else:
+            maxdiff = float("nan")
+    cpu_views = synth.scene_views(cpu_images, w, h, seed=11)
+    grays = [O.gray_from_rgb8(v) for v in cpu_views]
+    cpu = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda g: O.detect_and_describe(g, cr=False), grays))
+        cpu.append(time.perf_counter() - t0)
+    gd, ge, c = float(np.median(dev)), float(np.median(e2e)), float(np.median(cpu))
+    return {"metric": "descriptor producer: images/s (detect_and_describe, 960 x 540 RGB8, default DetectorConfig)",
+            "config": {"workload": "scene960", "images": n, "width": w, "height": h, "features": nfeat,
+                       "features_per_image": nfeat / n},
+            "value": n / gd, "unit": "images/s", "ms": gd * 1e3, "features_per_s": nfeat / gd,
+            "timed": "slm_detect_and_describe_rgb8, images in HBM, descriptors left in HBM, keypoints to pinned host",
+            "e2e": {"value": n / ge, "unit": "images/s", "ms": ge * 1e3, "h2d_bytes": int(views.nbytes),
+                    "d2h_bytes": nfeat * (128 + 5) * 4},
+            "bit_exact_vs_oracle_cr": exact, "max_desc_diff_vs_platform_functions": maxdiff,
+            "cpu_baseline": {"value": cpu_images / c, "unit": "images/s", "threads": threads, "kind": "port",
+                             "sample": f"{cpu_images} images of the same scene, one per thread, median of 2"}}
+
+
 def settled_frac(s, na, prec):
     """Fractions of a single pair's rows settled by each tier: by the FP8 bound,
     by the BF16 bound (BF16 pairs, and FP8 pairs rescued by the BF16 passes),
@@ -448,6 +534,12 @@ def main():
         import skylens_match as sm
         m = sm.Matcher()
         print(json.dumps(ransac_configs(m, os.cpu_count() or 1)), flush=True)
+        m.close()
+        return 0
+    if args.features:
+        import skylens_match as sm
+        m = sm.Matcher()
+        print(json.dumps(features_configs(m, os.cpu_count() or 1)), flush=True)
         m.close()
         return 0
     import torch
@@ -715,7 +807,8 @@ def main():
         t_c = time.perf_counter()
         line["configs"] = {"pairs": pair_configs(m, 3, os.cpu_count() or 1),
                            "serve": serve_configs(args.seed, args.config_rates, os.cpu_count() or 1),
-                           "ransac_scoring": ransac_configs(m, os.cpu_count() or 1)}
+                           "ransac_scoring": ransac_configs(m, os.cpu_count() or 1),
+                           "descriptor_producer": features_configs(m, os.cpu_count() or 1)}
         line["configs"]["wall_s"] = time.perf_counter() - t_c
     if rank == 0:
         s = json.dumps(line)

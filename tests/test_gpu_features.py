@@ -160,3 +160,46 @@ def test_argument_checks(matcher):
         F.describe(matcher, img, np.array([[5, 5, 0.0, 0.0, 0.0]], np.float32))  # sigma 0
     with pytest.raises(SlmError):
         F.describe(matcher, img, np.array([[5, 5, 1.0, 0.0, np.inf]], np.float32))
+
+
+def test_images_to_store_to_matches_on_the_device(matcher):
+    """The pipeline's load -> match_pairs chain without descriptors crossing to
+    the host: detect_and_describe writes descriptors to device memory, the
+    store takes them from there, and a BF16 batch matches the views; the lists
+    equal ratio_match on the same features (oracle)."""
+    import ctypes
+
+    import torch
+
+    import skylens_match as sm
+    views = synth.scene_views(4, 480, 270, seed=17)
+    cfg = F.detector_config()
+    n, cap = len(views), len(views) * int(cfg.max_features)
+    d_img = torch.from_numpy(views).cuda()
+    d_desc = torch.empty((cap, 128), dtype=torch.float32, device="cuda")
+    kps = np.empty((cap, 5), np.float32)
+    off = np.zeros(n + 1, np.uint64)
+    st = matcher._L.slm_detect_and_describe_rgb8(matcher.handle, ctypes.c_void_p(d_img.data_ptr()), n, 480, 270,
+                                                 ctypes.byref(cfg), ctypes.c_void_p(kps.ctypes.data),
+                                                 ctypes.c_void_p(d_desc.data_ptr()), cap,
+                                                 off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    assert st == 0
+    counts = np.diff(off).astype(np.uint32)
+    assert counts.min() > 20
+    store = sm.DescriptorStore(matcher, int(off[-1]) + 1024, n)
+    ids = store.add_views_ptr(d_desc.data_ptr(), off[:-1], counts)
+    pairs = [(0, 1), (1, 2), (0, 2), (2, 3), (0, 3)]
+    plan = store.plan(pairs, 0.8, True, "bf16")
+    plan.launch()
+    res, roff = plan.results()
+    got = [res[int(roff[k]):int(roff[k + 1])] for k in range(len(pairs))]
+    host = d_desc.cpu().numpy()
+    for k, (u, v) in enumerate(pairs):
+        a = host[int(off[ids[u]]):int(off[ids[u] + 1])]
+        b = host[int(off[ids[v]]):int(off[ids[v] + 1])]
+        want = O.ratio_match_np(a, b, 0.8, True, threads=8)
+        assert np.array_equal(got[k], want), (u, v)
+    # neighbouring views share the scene: many matches
+    assert len(got[0]) > 50
+    plan.close()
+    store.close()
