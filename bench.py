@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--pairs", action="store_true", help="single-pair configurations (800, 8192, 32768 FP8)")
     ap.add_argument("--ransac", action="store_true", help="RANSAC hypothesis scoring (Sampson residuals)")
     ap.add_argument("--features", action="store_true", help="descriptor producer (detect_and_describe, 960 x 540)")
+    ap.add_argument("--features-reps", type=int, default=5, help="timed calls per arm of --features")
     ap.add_argument("--no-scheduled", action="store_true",
                     help="skip the scheduled_pairs(PairSchedule::default()) batch with the < 20 filter")
     ap.add_argument("--no-configs", action="store_true",
@@ -478,14 +479,15 @@ def features_configs(m, threads: int, n: int = 24, reps: int = 5, cpu_images: in
             maxdiff = max(maxdiff, float(np.abs(d0 - desc[a:b]).max()))
         else:
             maxdiff = float("nan")
-    cpu_views = synth.scene_views(cpu_images, w, h, seed=11)
+    cpu_views = synth.scene_views(cpu_images, w, h, seed=11) if cpu_images else []
     grays = [O.gray_from_rgb8(v) for v in cpu_views]
     cpu = []
-    for _ in range(2):
+    for _ in range(2 if cpu_images else 0):
         t0 = time.perf_counter()
         with ThreadPoolExecutor(max_workers=threads) as ex:
             list(ex.map(lambda g: O.detect_and_describe(g, cr=False), grays))
         cpu.append(time.perf_counter() - t0)
+    cpu = cpu or [float("nan")]
     gd, ge, c = float(np.median(dev)), float(np.median(e2e)), float(np.median(cpu))
     return {"metric": "descriptor producer: images/s (detect_and_describe, 960 x 540 RGB8, default DetectorConfig)",
             "config": {"workload": "scene960", "images": n, "width": w, "height": h, "features": nfeat,
@@ -495,7 +497,7 @@ def features_configs(m, threads: int, n: int = 24, reps: int = 5, cpu_images: in
             "e2e": {"value": n / ge, "unit": "images/s", "ms": ge * 1e3, "h2d_bytes": int(views.nbytes),
                     "d2h_bytes": nfeat * (128 + 5) * 4},
             "bit_exact_vs_oracle_cr": exact, "max_desc_diff_vs_platform_functions": maxdiff,
-            "cpu_baseline": {"value": cpu_images / c, "unit": "images/s", "threads": threads, "kind": "port",
+            "cpu_baseline": {"value": cpu_images / c if cpu_images else None, "unit": "images/s", "threads": threads, "kind": "port",
                              "sample": f"{cpu_images} images of the same scene, one per thread, median of 2"}}
 
 
@@ -539,7 +541,8 @@ def main():
     if args.features:
         import skylens_match as sm
         m = sm.Matcher()
-        print(json.dumps(features_configs(m, os.cpu_count() or 1)), flush=True)
+        print(json.dumps(features_configs(m, os.cpu_count() or 1, reps=args.features_reps,
+                                          cpu_images=0 if args.no_cpu_baseline else 32)), flush=True)
         m.close()
         return 0
     import torch

@@ -87,6 +87,29 @@ pub struct slm_ctx {
 pub struct slm_store {
     _private: [u8; 0],
 }
+/// Keypoint (features.rs:296-304).
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default, PartialEq)]
+pub struct slm_keypoint {
+    pub x: f32,
+    pub y: f32,
+    pub sigma: f32,
+    pub response: f32,
+    pub angle: f32,
+}
+/// DetectorConfig (features.rs:253-293).
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct slm_detector_config {
+    pub octaves: u32,
+    pub scales: u32,
+    pub sigma0: f32,
+    pub contrast: f32,
+    pub edge_ratio: f32,
+    pub max_features: u32,
+    pub upscale_below: u32,
+    pub upscale_fill: i32,
+}
 #[repr(C)]
 pub struct slm_plan {
     _private: [u8; 0],
@@ -148,4 +171,13 @@ extern "C" {
     pub fn slm_sampson_score(ctx: *mut slm_ctx, pts: *const f64, pair_off: *const u64, np: u32, thresh: *const f64,
                              e: *const f64, hyp_pair: *const u32, nh: u32, counts: *mut u32, mask_off: *const u64,
                              masks: *mut u32, mask_words: u64) -> SlmStatus;
+    pub fn slm_detector_config_default(cfg: *mut slm_detector_config);
+    pub fn slm_detect_and_describe(ctx: *mut slm_ctx, imgs: *const f32, n: u32, w: u32, h: u32,
+                                   cfg: *const slm_detector_config, kps: *mut slm_keypoint, desc: *mut f32,
+                                   cap: u64, off: *mut u64) -> SlmStatus;
+    pub fn slm_detect_and_describe_rgb8(ctx: *mut slm_ctx, rgb: *const u8, n: u32, w: u32, h: u32,
+                                        cfg: *const slm_detector_config, kps: *mut slm_keypoint, desc: *mut f32,
+                                        cap: u64, off: *mut u64) -> SlmStatus;
+    pub fn slm_describe(ctx: *mut slm_ctx, img: *const f32, w: u32, h: u32, kps: *const slm_keypoint, n: u32,
+                        desc: *mut f32) -> SlmStatus;
 }

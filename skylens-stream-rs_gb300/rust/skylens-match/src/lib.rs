@@ -5,6 +5,8 @@
 //! * `candidate_pairs(views, temporal, cross, pow2_max)` (matching.rs:18)
 //! * `match_pairs(descs, pairs, ratio, mutual)`: the matching half of
 //!   pipeline.rs:485-493 as one GPU batch.
+//! * `detect_and_describe_rgb8(images, w, h, cfg)`: features of images of one
+//!   size (features.rs:594 detect_and_describe after GrayImage::from_rgb).
 //! * `sampson_counts(pts, th, hyps)`: inlier counts of essential-matrix
 //!   hypotheses over one pair's matches (two_view.rs:804-823, count_at_least),
 //!   for a block of RANSAC iterations at once.
@@ -255,4 +257,43 @@ pub fn sampson_counts(pts: &[[f64; 4]], th: f64, hyps: &[[f64; 9]]) -> Vec<u32> 
         "slm_sampson_score",
     );
     counts
+}
+
+/// `DetectorConfig::default()` (features.rs:278-293) as libslm takes it.
+pub fn detector_config_default() -> sys::slm_detector_config {
+    let mut c = sys::slm_detector_config::default();
+    unsafe { sys::slm_detector_config_default(&mut c) };
+    c
+}
+
+/// `detect_and_describe(&GrayImage::from_rgb(w, h, rgb), cfg)` for several
+/// images of one size in one GPU call (pipeline.rs:452-463 `load` does one
+/// per image): per image, its keypoints and 128-float descriptors in the
+/// reference's order.
+pub fn detect_and_describe_rgb8(images: &[&[u8]], w: u32, h: u32, cfg: &sys::slm_detector_config)
+                                -> Vec<(Vec<sys::slm_keypoint>, Vec<[f32; 128]>)> {
+    let n = images.len();
+    let px = w as usize * h as usize * 3;
+    let mut rgb = Vec::with_capacity(n * px);
+    for im in images {
+        assert_eq!(im.len(), px, "image buffer is not w x h x 3 bytes");
+        rgb.extend_from_slice(im);
+    }
+    let cap = n * cfg.max_features as usize;
+    let mut kps = vec![sys::slm_keypoint::default(); cap.max(1)];
+    let mut desc = vec![[0f32; 128]; cap.max(1)];
+    let mut off = vec![0u64; n + 1];
+    check(
+        unsafe {
+            sys::slm_detect_and_describe_rgb8(ctx(), rgb.as_ptr(), n as u32, w, h, cfg, kps.as_mut_ptr(),
+                                              desc.as_mut_ptr() as *mut f32, cap as u64, off.as_mut_ptr())
+        },
+        "slm_detect_and_describe_rgb8",
+    );
+    (0..n)
+        .map(|k| {
+            let (a, b) = (off[k] as usize, off[k + 1] as usize);
+            (kps[a..b].to_vec(), desc[a..b].to_vec())
+        })
+        .collect()
 }
