@@ -9,15 +9,20 @@
 // is compiled without FMA contraction and with IEEE division and square root,
 // so each f32 value is the reference's. The reference's per-pixel and
 // per-keypoint transcendental functions (atan2, exp, powf, cos, sin; the
-// platform's float functions) are evaluated here in double and rounded once
-// to float: the correctly rounded value (double rounding aside, probability
-// about 2^-29 a call), which equals the platform's float result wherever that
-// one is correctly rounded. Sums that the reference accumulates in one order
-// (histogram bins, the descriptor's norm) are accumulated in that order.
+// platform's float functions) are evaluated correctly rounded: atan2 and exp,
+// called per pixel and per window sample, by the float-float evaluations of
+// fmath_cr.h (FP32 and FMA, with a rounding test that falls back to double in
+// a few calls in 10^5), powf, cos and sin, once per keypoint, in double
+// rounded to float. Both equal the double function rounded to float (double
+// rounding aside, probability about 2^-29 a call), which equals the
+// platform's float result wherever that one is correctly rounded. Sums that
+// the reference accumulates in one order (histogram bins, the descriptor's
+// norm) are accumulated in that order.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
+#include "fmath_cr.h"
 #include "slm_internal.h"
 
 namespace slm {
@@ -28,13 +33,23 @@ constexpr float kTwoPi = 6.28318530717958647692f;  // std::f32::consts::TAU
 constexpr float kSqrt2 = 1.41421356237309504880f;  // std::f32::consts::SQRT_2
 constexpr int kOriBins = 36;                        // features.rs:307
 
-__device__ __forceinline__ float exp_cr(float x) { return (float)exp((double)x); }
-__device__ __forceinline__ float atan2_cr(float y, float x) { return (float)atan2((double)y, (double)x); }
+__device__ __forceinline__ float exp_cr(float x) { return slm_expf_cr(x); }
+__device__ __forceinline__ float atan2_cr(float y, float x) { return slm_atan2f_cr(y, x); }
 
-// f32::rem_euclid: a % b, plus |b| when negative
+// f32::rem_euclid(a, b) for b > 0: a % b (fmodf), plus b when negative. For
+// |a| < 2b the remainder is a, or a - b with a's sign (exact: b <= |a| < 2b),
+// and a zero remainder keeps a's sign as fmodf's does; fmodf otherwise.
 __device__ __forceinline__ float rem_euclid(float a, float b) {
-    const float r = fmodf(a, b);
-    return r < 0.0f ? r + fabsf(b) : r;
+    float r;
+    const float aa = fabsf(a);
+    if (aa < b) {
+        r = a;
+    } else if (aa < 2.0f * b) {
+        r = copysignf(aa - b, a);
+    } else {
+        r = fmodf(a, b);
+    }
+    return r < 0.0f ? r + b : r;
 }
 
 // `v as isize` (truncation; the values here are small and finite)
@@ -304,40 +319,68 @@ __global__ void __launch_bounds__(256) orient_kernel(OrientArgs a) {
             if (bj == lane + 32) h1 += vj;
         }
     }
-    hs[warp][lane] = h0;
-    if (lane < kOriBins - 32) hs[warp][lane + 32] = h1;
-    __syncwarp();
-    if (lane != 0) return;
+    // six [1,1,1]/3 smoothings, lane b computing bins b and b + 32 (each bin
+    // from the previous pass's three, ((l + c) + r) / 3 as the reference)
     float *hist = hs[warp];
+    const int b1 = lane + 32;
+    const bool has1 = b1 < kOriBins;
     for (int it = 0; it < 6; ++it) {
-        float prev[kOriBins];
-        for (int i = 0; i < kOriBins; ++i) prev[i] = hist[i];
-        for (int i = 0; i < kOriBins; ++i)
-            hist[i] = (prev[(i + kOriBins - 1) % kOriBins] + prev[i] + prev[(i + 1) % kOriBins]) / 3.0f;
+        hist[lane] = h0;
+        if (has1) hist[b1] = h1;
+        __syncwarp();
+        const float n0 = (hist[(lane + kOriBins - 1) % kOriBins] + h0 + hist[(lane + 1) % kOriBins]) / 3.0f;
+        const float n1 = has1 ? (hist[(b1 + kOriBins - 1) % kOriBins] + h1 + hist[(b1 + 1) % kOriBins]) / 3.0f : 0.0f;
+        __syncwarp();
+        h0 = n0;
+        h1 = n1;
     }
-    float mx = 0.0f;
-    for (int i = 0; i < kOriBins; ++i) mx = fmaxf(mx, hist[i]);
-    int na = 0;
+    hist[lane] = h0;
+    if (has1) hist[b1] = h1;
+    __syncwarp();
+    // fold(0.0, f32::max): fmaxf is order-free (NaN ignored either way)
+    float mx = fmaxf(h0, has1 ? h1 : 0.0f);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mx = fmaxf(0.0f, mx);
+    // peaks in bin order: bins 0..31 by lane, then 32..35
     float *out = a.angles + (uint64_t)ci * kMaxAngles;
+    int na = 0;
     if (mx > 0.0f) {
-        for (int i = 0; i < kOriBins; ++i) {
-            const float l = hist[(i + kOriBins - 1) % kOriBins], cc = hist[i], rr = hist[(i + 1) % kOriBins];
-            if (cc >= 0.8f * mx && cc > l && cc > rr) {
-                const float off = 0.5f * (l - rr) / (l - 2.0f * cc + rr);
-                out[na++] = rem_euclid(((float)i + off) / (float)kOriBins * kTwoPi, kTwoPi);
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int i = half ? b1 : lane;
+            bool peak = false;
+            float ang = 0.0f;
+            if (i < kOriBins) {
+                const float l = hist[(i + kOriBins - 1) % kOriBins], cc = hist[i], rr = hist[(i + 1) % kOriBins];
+                if (cc >= 0.8f * mx && cc > l && cc > rr) {
+                    const float off = 0.5f * (l - rr) / (l - 2.0f * cc + rr);
+                    ang = rem_euclid(((float)i + off) / (float)kOriBins * kTwoPi, kTwoPi);
+                    peak = true;
+                }
             }
+            const unsigned m = __ballot_sync(0xffffffffu, peak);
+            if (peak) out[na + __popc(m & ((1u << lane) - 1u))] = ang;
+            na += __popc(m);
         }
     }
-    a.nang[ci] = (uint8_t)na;
+    if (lane == 0) a.nang[ci] = (uint8_t)na;
 }
 
 // ----------------------------------------------------------------- describe
 
 constexpr int kDescThreads = 128;
 
+// One window sample's contributions: the products m * (1 - dv) and m * dv
+// for its two spatial rows iv0 and iv0 + 1 (the first factor of the
+// reference's ((m * wv) * wu) * wo), the column and orientation weights, and
+// the lanes (iu * 8 + io) it adds to in a row: `hit`, of which `second_u`
+// take du instead of 1 - du and `second_o` take dob instead of 1 - dob.
 struct DescSample {
-    float m, du, dv, dob;
-    int iu0, iv0, io0, pad;
+    float pv0, pv1, wu0, wu1;
+    float wo0, wo1;
+    int iv0;
+    uint32_t hit, second_u, second_o, pad0, pad1;
 };
 
 // One CTA per feature (describe_with, features.rs:521-592). The (2r+1)^2
@@ -383,7 +426,7 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
     const int side = 2 * r + 1;
     const int total = side * side;
     float acc = 0.0f;  // bin (warp, lane)
-    const int my_iu = lane >> 3, my_io = lane & 7;
+    const uint32_t my_bit = 1u << lane;
     for (int base = 0; base < total; base += kDescThreads) {
         const int t = base + tid;
         bool valid = false;
@@ -400,14 +443,28 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
                     const float ori = rem_euclid(gm.y - angle, kTwoPi);
                     const float bo = ori / kTwoPi * (float)NO;
                     const float wgt = exp_cr(-(u * u + v * v) / (2.0f * 4.0f));
-                    q.m = gm.x * wgt;
+                    const float m = gm.x * wgt;
                     const float u0 = floorf(bu), v0 = floorf(bv), o0 = floorf(bo);
-                    q.du = bu - u0;
-                    q.dv = bv - v0;
-                    q.dob = bo - o0;
-                    q.iu0 = f2i(u0);
+                    const float du = bu - u0, dv = bv - v0, dob = bo - o0;
+                    q.pv0 = m * (1.0f - dv);
+                    q.pv1 = m * dv;
+                    q.wu0 = 1.0f - du;
+                    q.wu1 = du;
+                    q.wo0 = 1.0f - dob;
+                    q.wo1 = dob;
                     q.iv0 = f2i(v0);
-                    q.io0 = o0 < 0.0f ? 0 : f2i(o0);
+                    const int iu0 = f2i(u0);
+                    const int io0 = o0 < 0.0f ? 0 : f2i(o0);
+                    const int olo = io0 % NO, ohi = (io0 + 1) % NO;
+#pragma unroll
+                    for (int da = 0; da < 2; ++da) {
+                        const int iu = iu0 + da;
+                        if (iu < 0 || iu >= NC) continue;
+                        const uint32_t blo = 1u << (iu * NO + olo), bhi = 1u << (iu * NO + ohi);
+                        q.hit |= blo | bhi;
+                        q.second_o |= bhi;
+                        if (da) q.second_u |= blo | bhi;
+                    }
                     valid = true;
                 }
             }
@@ -425,14 +482,13 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
             while (m) {
                 const int j = g * 32 + __ffs(m) - 1;
                 m &= m - 1;
-                const DescSample s = smp[j];
-                const float wv = s.iv0 == warp ? 1.0f - s.dv : s.dv;
-                const bool iu_hit = my_iu == s.iu0 || my_iu == s.iu0 + 1;
-                const int o_lo = s.io0 % NO, o_hi = (s.io0 + 1) % NO;
-                if (iu_hit && (my_io == o_lo || my_io == o_hi)) {
-                    const float wu = my_iu == s.iu0 ? 1.0f - s.du : s.du;
-                    const float wo = my_io == o_lo ? 1.0f - s.dob : s.dob;
-                    acc += s.m * wv * wu * wo;
+                const DescSample &s = smp[j];
+                const uint32_t hit = s.hit;
+                if (hit & my_bit) {
+                    const float pv = s.iv0 == warp ? s.pv0 : s.pv1;
+                    const float wu = (s.second_u & my_bit) ? s.wu1 : s.wu0;
+                    const float wo = (s.second_o & my_bit) ? s.wo1 : s.wo0;
+                    acc += pv * wu * wo;
                 }
             }
         }

@@ -2718,8 +2718,9 @@ uint64_t feat_align(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 // next run): the kept features of every image, in the reference's order.
 struct FeatCore {
     std::vector<OctaveGeom> geom;
-    std::vector<FeatCand> cands;
-    std::vector<float> angles;  // kMaxAngles per candidate
+    // read back into the workspace's pinned block (valid until its next use)
+    const FeatCand *cands = nullptr;
+    const float *angles = nullptr;  // kMaxAngles per candidate
     std::vector<std::vector<std::pair<uint32_t, uint32_t>>> kept;  // per image: (candidate, angle slot)
     // device addresses inside pyr
     float2 *d_grads = nullptr;
@@ -2728,8 +2729,10 @@ struct FeatCore {
     int s = 0;
 };
 
-slm_status feat_core(slm_ctx *c, cudaStream_t st, DevBuf &pyr, const float *d_img, uint32_t n, int w, int h,
+slm_status feat_core(slm_ctx *c, Workspace *ws, const float *d_img, uint32_t n, int w, int h,
                      const slm_detector_config &cfg, float in_sigma, FeatCore &out) {
+    cudaStream_t st = ws->stream;
+    DevBuf &pyr = ws->feat_pyr;
     out = FeatCore();
     out.kept.assign(n, {});
     const int s = (int)cfg.scales, ng = s + 3;
@@ -2842,38 +2845,54 @@ slm_status feat_core(slm_ctx *c, cudaStream_t st, DevBuf &pyr, const float *d_im
         oa.nang = d_nang;
         launch_orient(oa, count, st);
         SLM_CU(cudaGetLastError());
-        out.cands.resize(count);
-        out.angles.resize((size_t)count * kMaxAngles);
-        std::vector<uint8_t> nang(count);
+        // candidates, angle counts and angles into pinned host memory
+        const uint64_t h_ang = feat_align(sizeof(FeatCand) * (uint64_t)count),
+                       h_nang = feat_align(h_ang + 4ull * kMaxAngles * count), h_bytes = h_nang + count + 16;
+        SLM_TRY(ws_host_block(ws, h_bytes));
+        unsigned char *hb = ws->single_host;
+        out.cands = reinterpret_cast<const FeatCand *>(hb);
+        out.angles = reinterpret_cast<const float *>(hb + h_ang);
+        const uint8_t *nang = hb + h_nang;
         if (count) {
-            SLM_CU(cudaMemcpyAsync(out.cands.data(), out.d_cands, sizeof(FeatCand) * count, cudaMemcpyDeviceToHost,
-                                   st));
-            SLM_CU(cudaMemcpyAsync(out.angles.data(), d_ang, 4ull * kMaxAngles * count, cudaMemcpyDeviceToHost, st));
-            SLM_CU(cudaMemcpyAsync(nang.data(), d_nang, count, cudaMemcpyDeviceToHost, st));
+            SLM_CU(cudaMemcpyAsync(hb, out.d_cands, sizeof(FeatCand) * count, cudaMemcpyDeviceToHost, st));
+            SLM_CU(cudaMemcpyAsync(hb + h_ang, d_ang, 4ull * kMaxAngles * count, cudaMemcpyDeviceToHost, st));
+            SLM_CU(cudaMemcpyAsync(hb + h_nang, d_nang, count, cudaMemcpyDeviceToHost, st));
         }
         SLM_CU(cudaStreamSynchronize(st));
         // the reference's emission order (octave, layer, row, column of the
         // scanned extremum; angles in bin order), then its stable sort by
         // |response| descending (f32::total_cmp of abs(): the bits of |v|) and
         // the max_features cut (features.rs:776-778)
-        std::vector<std::vector<uint32_t>> by_img(n);
-        for (uint32_t i = 0; i < count; ++i) by_img[out.cands[i].img].push_back(i);
-        for (uint32_t k = 0; k < n; ++k) {
-            std::vector<uint32_t> &ci = by_img[k];
-            std::sort(ci.begin(), ci.end(), [&](uint32_t a, uint32_t b) { return out.cands[a].key < out.cands[b].key; });
-            std::vector<std::pair<uint32_t, uint32_t>> f;
-            for (uint32_t i : ci)
-                for (uint32_t a = 0; a < nang[i]; ++a) f.emplace_back(i, a);
-            auto mag = [&](uint32_t i) {
+        // One sort per image of compact candidate records by (|response|
+        // descending, emission key); a candidate's features follow in angle
+        // order: the same list as the stable sort of the emitted features,
+        // since every feature of a candidate shares its |response| and key.
+        struct Ord {
+            uint32_t nmag;  // ~bits(|value|): ascending = |value| descending
+            uint32_t idx;
+            uint64_t key;
+        };
+        std::vector<uint32_t> per(n + 1, 0);
+        for (uint32_t i = 0; i < count; ++i) per[out.cands[i].img + 1]++;
+        for (uint32_t k = 0; k < n; ++k) per[k + 1] += per[k];
+        std::vector<Ord> ord(count);
+        {
+            std::vector<uint32_t> fill(per.begin(), per.end() - 1);
+            for (uint32_t i = 0; i < count; ++i) {
+                const FeatCand &fc = out.cands[i];
                 uint32_t u;
-                std::memcpy(&u, &out.cands[i].value, 4);
-                return u & 0x7fffffffu;
-            };
-            std::stable_sort(f.begin(), f.end(), [&](const std::pair<uint32_t, uint32_t> &a,
-                                                     const std::pair<uint32_t, uint32_t> &b) {
-                return mag(a.first) > mag(b.first);
+                std::memcpy(&u, &fc.value, 4);
+                ord[fill[fc.img]++] = Ord{~(u & 0x7fffffffu), i, fc.key};
+            }
+        }
+        for (uint32_t k = 0; k < n; ++k) {
+            std::sort(ord.begin() + per[k], ord.begin() + per[k + 1], [](const Ord &a, const Ord &b) {
+                return a.nmag != b.nmag ? a.nmag < b.nmag : a.key < b.key;
             });
-            if (f.size() > cfg.max_features) f.resize(cfg.max_features);
+            std::vector<std::pair<uint32_t, uint32_t>> f;
+            for (uint32_t q = per[k]; q < per[k + 1] && f.size() < cfg.max_features; ++q)
+                for (uint32_t a = 0; a < nang[ord[q].idx] && f.size() < cfg.max_features; ++a)
+                    f.emplace_back(ord[q].idx, a);
             out.kept[k] = std::move(f);
         }
         return SLM_OK;
@@ -2921,8 +2940,7 @@ slm_status feat_describe(slm_ctx *c, cudaStream_t st, DevBuf &buf, const FeatCor
     da.desc = reinterpret_cast<float *>(d + o_desc);
     launch_describe(da, (uint32_t)jobs.size(), st);
     SLM_CU(cudaGetLastError());
-    // the job table is read by the kernel before the host vector goes away
-    SLM_CU(cudaStreamSynchronize(st));
+    // (the pageable job table was staged by the copy call: the vector may go)
     *d_desc = da.desc;
     return SLM_OK;
 }
@@ -2943,7 +2961,7 @@ slm_status detect_describe_dev(slm_ctx *c, Workspace *ws, const float *d_gray, u
                                uint64_t *off) {
     cudaStream_t st = ws->stream;
     FeatCore run;
-    SLM_TRY(feat_core(c, st, ws->feat_pyr, d_gray, n, (int)w, (int)h, cfg, 0.5f, run));
+    SLM_TRY(feat_core(c, ws, d_gray, n, (int)w, (int)h, cfg, 0.5f, run));
     std::vector<std::pair<uint32_t, uint32_t>> all1;
     std::vector<uint64_t> first1(n + 1, 0);
     for (uint32_t k = 0; k < n; ++k) {
@@ -2981,7 +2999,7 @@ slm_status detect_describe_dev(slm_ctx *c, Workspace *ws, const float *d_gray, u
         launch_upsample2(fu, fu + o_up, (int)w, (int)h, (int)nu, st);
         SLM_CU(cudaGetLastError());
         FeatCore run2;
-        SLM_TRY(feat_core(c, st, ws->feat_pyr, fu + o_up, (uint32_t)nu, 2 * (int)w, 2 * (int)h, cfg, 1.0f, run2));
+        SLM_TRY(feat_core(c, ws, fu + o_up, (uint32_t)nu, 2 * (int)w, 2 * (int)h, cfg, 1.0f, run2));
         const float cell = 4.0f;
         const int64_t gw = (int64_t)((float)w / cell) + 2, gh = (int64_t)((float)h / cell) + 2;
         auto key = [&](float x, float y) {

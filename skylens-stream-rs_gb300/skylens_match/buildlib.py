@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libslm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_exact.cu", "k_compact.cu", "k_shortlist.cu", "k_noalloc.cu", "k_sampson.cu", "k_features.cu"]
 CPP_SOURCES = ["slm.cpp"]
-HEADERS = ["pack.cuh", "ptx.cuh", "slm_internal.h", "slm_shortlist.h"]
+HEADERS = ["pack.cuh", "ptx.cuh", "slm_internal.h", "slm_shortlist.h", "fmath_cr.h", "fmath_tables.h"]
 
 
 def _nvcc() -> str:
