@@ -98,6 +98,49 @@ __global__ void __launch_bounds__(kBlurX) blur_cols_kernel(const float *__restri
     if (dog) dog[b * img_stride_dog + p] = acc - prev[b * img_stride_out + p];
 }
 
+// Both passes in one kernel for radii up to kFusedR: a 64 x 32 output tile
+// with its halo of clamped input pixels in shared memory, the horizontal sums
+// of the tile's rows (halo rows included) in shared memory, then the vertical
+// sums; with `dog`, also dog = out - src at each pixel (src is the previous
+// layer). Each sum runs over j in order from 0.0, exactly as the two-kernel
+// form and the reference do.
+constexpr int kFusedR = 16;
+constexpr int kFX = 64, kFY = 32;
+__global__ void __launch_bounds__(256) blur_fused_kernel(const float *__restrict__ src, float *__restrict__ dst,
+                                                         float *__restrict__ dog, int w, int h,
+                                                         uint64_t img_stride_src, uint64_t img_stride_dst,
+                                                         uint64_t img_stride_dog, BlurTaps t) {
+    __shared__ float in[kFY + 2 * kFusedR][kFX + 2 * kFusedR];
+    __shared__ float hs[kFY + 2 * kFusedR][kFX];
+    const int r = t.r, b = blockIdx.z;
+    const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY;
+    const float *S = src + b * img_stride_src;
+    const int rows = kFY + 2 * r, cols = kFX + 2 * r;
+    for (int e = threadIdx.x; e < rows * cols; e += 256) {
+        const int ry = e / cols, rx = e % cols;
+        const int yy = clampi(y0 + ry - r, 0, h - 1), xx = clampi(x0 + rx - r, 0, w - 1);
+        in[ry][rx] = S[(uint64_t)yy * w + xx];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * kFX; e += 256) {
+        const int ry = e / kFX, cx = e % kFX;
+        float acc = 0.0f;
+        for (int j = 0; j <= 2 * r; ++j) acc += t.k[j] * in[ry][cx + j];
+        hs[ry][cx] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kFY * kFX; e += 256) {
+        const int ty = e / kFX, cx = e % kFX;
+        const int x = x0 + cx, y = y0 + ty;
+        if (x >= w || y >= h) continue;
+        float acc = 0.0f;
+        for (int j = 0; j <= 2 * r; ++j) acc += t.k[j] * hs[ty + j][cx];
+        const uint64_t p = (uint64_t)y * w + x;
+        dst[b * img_stride_dst + p] = acc;
+        if (dog) dog[b * img_stride_dog + p] = acc - in[ty + r][cx + r];
+    }
+}
+
 // base of the next octave: the even pixels of gauss[s] (GrayImage::downsample)
 __global__ void downsample_kernel(const float *__restrict__ src, float *__restrict__ dst, int w, int h, int nw, int nh,
                                   uint64_t img_stride_src, uint64_t img_stride_dst) {
@@ -518,6 +561,11 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
 
 void launch_blur(const float *src, float *tmp, float *dst, const float *prev, float *dog, int w, int h, int nimg,
                  uint64_t stride_src, uint64_t stride_dst, uint64_t stride_dog, const BlurTaps &t, cudaStream_t s) {
+    if (t.r <= kFusedR && (!dog || (prev == src && stride_src == stride_dst))) {
+        const dim3 g((w + kFX - 1) / kFX, (h + kFY - 1) / kFY, nimg);
+        blur_fused_kernel<<<g, 256, 0, s>>>(src, dst, dog, w, h, stride_src, stride_dst, stride_dog, t);
+        return;
+    }
     const dim3 grid((w + kBlurX - 1) / kBlurX, h, nimg);
     blur_rows_kernel<<<grid, kBlurX, 0, s>>>(src, tmp, w, h, stride_src, (uint64_t)w * h, t);
     blur_cols_kernel<<<grid, kBlurX, 0, s>>>(tmp, dst, prev, dog, w, h, (uint64_t)w * h, stride_dst, stride_dog, t);

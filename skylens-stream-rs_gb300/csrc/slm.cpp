@@ -2919,6 +2919,7 @@ slm_status feat_describe(slm_ctx *c, cudaStream_t st, DevBuf &buf, const FeatCor
                          const std::vector<std::pair<uint32_t, uint32_t>> &list, float **d_desc) {
     *d_desc = nullptr;
     if (list.empty()) return SLM_OK;
+    if (list.size() >= (1ull << 31)) return fail(SLM_INVALID_ARG, "too many features in one call");
     const uint64_t o_jobs = 0, o_desc = feat_align(sizeof(DescJob) * list.size()),
                    bytes = o_desc + 4ull * kDesc * list.size();
     SLM_TRY(buf.ensure(c, bytes));
@@ -3080,7 +3081,10 @@ slm_status feat_entry_checks(slm_ctx *c, const void *imgs, uint32_t n, uint32_t 
     if (n && !imgs) return fail(SLM_INVALID_ARG, "NULL images");
     if (n > 65535) return fail(SLM_INVALID_ARG, "at most 65535 images per call");
     if (w > 32767 || h > 32767) return fail(SLM_INVALID_ARG, "images up to 32767 pixels a side");
-    return check_detector_config(cfg);
+    SLM_TRY(check_detector_config(cfg));
+    // launch grids put (image, layer) in one 16-bit grid dimension
+    if ((uint64_t)n * cfg->scales > 65535) return fail(SLM_INVALID_ARG, "n * scales must be at most 65535");
+    return SLM_OK;
 }
 
 }  // namespace
