@@ -257,10 +257,19 @@ def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32"
     done = []
     for prec in prec_list:
         for rate in [None if r == "burst" else float(r) for r in rates.split(",")]:
-            srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
-            res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
-            st = srv.stats()
-            srv.close()
+            # a burst lasts milliseconds: three of them, each on a fresh server,
+            # and the median is reported (with all three)
+            runs = []
+            for _ in range(1 if rate else 3):
+                srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
+                res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
+                st = srv.stats()
+                srv.close()
+                runs.append((wall, res, lats, st))
+            walls = [x[0] for x in runs]
+            wall, res, lats, st = runs[int(np.argsort(walls)[len(walls) // 2])]
+            st = dict(st)
+            st["pairs_per_s_each"] = [npairs / x for x in walls]
             done.append((prec, rate, res, lats, wall, st))
     check = {}
     for prec, rate, res, lats, wall, st in done:
@@ -278,6 +287,9 @@ def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32"
                             "pairs_per_s": npairs / wall, "wall_s": wall, "batches": st["batches"],
                             "max_batch_requests": st["max_batch_requests"], "max_inflight": st["max_inflight"],
                             "bit_exact_sample_mismatches": int(mism)})
+        if "pairs_per_s_each" in st and rate is None:
+            out["runs"][-1]["pairs_per_s_each_run"] = st["pairs_per_s_each"]
+            out["runs"][-1]["runs"] = "median of 3 bursts, each on a fresh server"
         print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
     return out
 
@@ -808,8 +820,13 @@ def main():
         # the other configurations, bounded (about half a minute): single pairs
         # in every precision and the serving workload at one rate and in a burst
         t_c = time.perf_counter()
-        line["configs"] = {"pairs": pair_configs(m, 3, os.cpu_count() or 1),
-                           "serve": serve_configs(args.seed, args.config_rates, os.cpu_count() or 1),
+        pairs_rec = pair_configs(m, 3, os.cpu_count() or 1)
+        sclk = Clocks(dev)
+        sclk.start()
+        serve_rec = serve_configs(args.seed, args.config_rates, os.cpu_count() or 1)
+        serve_rec["clocks"] = sclk.stop()
+        line["configs"] = {"pairs": pairs_rec,
+                           "serve": serve_rec,
                            "ransac_scoring": ransac_configs(m, os.cpu_count() or 1),
                            "descriptor_producer": features_configs(m, os.cpu_count() or 1)}
         line["configs"]["wall_s"] = time.perf_counter() - t_c
