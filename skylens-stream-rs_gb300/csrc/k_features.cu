@@ -476,10 +476,15 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
         DescSample q{};
         if (t < total) {
             const int px = xi + (t % side) - r, py = yi + (t / side) - r;
-            if (!(px < 1 || py < 1 || px >= w - 1 || py >= h - 1)) {
-                const float fx = (float)px - x, fy = (float)py - y;
-                const float u = (c * fx + sn * fy) / cell;
-                const float v = (-sn * fx + c * fy) / cell;
+            const float fx = (float)px - x, fy = (float)py - y;
+            const float pu = c * fx + sn * fy, pv_ = -sn * fx + c * fy;
+            // |numerator| above 2.6 cells puts bu or bv beyond (-1, 4) whatever
+            // the division rounds to: such samples skip the divisions (NaN goes on
+            // to the reference's test)
+            const float lim = 2.6f * cell;
+            if (!(px < 1 || py < 1 || px >= w - 1 || py >= h - 1) && !(fabsf(pu) > lim) && !(fabsf(pv_) > lim)) {
+                const float u = pu / cell;
+                const float v = pv_ / cell;
                 const float bu = u + (float)NC / 2.0f - 0.5f, bv = v + (float)NC / 2.0f - 0.5f;
                 if (!(bu <= -1.0f || bv <= -1.0f || bu >= (float)NC || bv >= (float)NC)) {
                     const float2 gm = grad[(uint64_t)py * w + px];
@@ -519,19 +524,30 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
             if (lane == 0) rel[row][warp] = m;
         }
         __syncthreads();
-        // warp `warp` owns spatial row iv = warp
+        // warp `warp` owns spatial row iv = warp; samples two at a time (both
+        // contributions formed first, then added in sample order)
+        auto contrib = [&](const DescSample &s) {
+            const float pv = s.iv0 == warp ? s.pv0 : s.pv1;
+            const float wu = (s.second_u & my_bit) ? s.wu1 : s.wu0;
+            const float wo = (s.second_o & my_bit) ? s.wo1 : s.wo0;
+            return pv * wu * wo;
+        };
         for (int g = 0; g < kDescThreads / 32; ++g) {
             unsigned m = rel[warp][g];
             while (m) {
-                const int j = g * 32 + __ffs(m) - 1;
+                const int j1 = g * 32 + __ffs(m) - 1;
                 m &= m - 1;
-                const DescSample &s = smp[j];
-                const uint32_t hit = s.hit;
-                if (hit & my_bit) {
-                    const float pv = s.iv0 == warp ? s.pv0 : s.pv1;
-                    const float wu = (s.second_u & my_bit) ? s.wu1 : s.wu0;
-                    const float wo = (s.second_o & my_bit) ? s.wo1 : s.wo0;
-                    acc += pv * wu * wo;
+                const DescSample &s1 = smp[j1];
+                if (m) {
+                    const int j2 = g * 32 + __ffs(m) - 1;
+                    m &= m - 1;
+                    const DescSample &s2 = smp[j2];
+                    const bool h1 = s1.hit & my_bit, h2 = s2.hit & my_bit;
+                    const float c1 = contrib(s1), c2 = contrib(s2);
+                    if (h1) acc += c1;
+                    if (h2) acc += c2;
+                } else if (s1.hit & my_bit) {
+                    acc += contrib(s1);
                 }
             }
         }
