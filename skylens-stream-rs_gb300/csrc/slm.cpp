@@ -2956,10 +2956,19 @@ slm_status check_detector_config(const slm_detector_config *cfg) {
     return SLM_OK;
 }
 
-// Shared body of the gray and RGB8 entry points; d_gray holds the n images.
-slm_status detect_describe_dev(slm_ctx *c, Workspace *ws, const float *d_gray, uint32_t n, uint32_t w, uint32_t h,
-                               const slm_detector_config &cfg, slm_keypoint *kps, float *desc, uint64_t cap,
-                               uint64_t *off) {
+// One batch's features, held in its workspace until they are copied out:
+// per image the keypoints of the input-size and of the upsampled detection,
+// and where their descriptors lie in the two device staging arrays.
+struct FeatOut {
+    std::vector<std::vector<slm_keypoint>> kp, kp2;
+    std::vector<uint64_t> first1, first2;
+    float *d_desc1 = nullptr, *d_desc2 = nullptr;
+};
+
+// detect_and_describe of the n images at d_gray (in the workspace), up to
+// the copies out.
+slm_status detect_describe_run(slm_ctx *c, Workspace *ws, const float *d_gray, uint32_t n, uint32_t w, uint32_t h,
+                               const slm_detector_config &cfg, FeatOut &fo) {
     cudaStream_t st = ws->stream;
     FeatCore run;
     SLM_TRY(feat_core(c, ws, d_gray, n, (int)w, (int)h, cfg, 0.5f, run));
@@ -3048,31 +3057,122 @@ slm_status detect_describe_dev(slm_ctx *c, Workspace *ws, const float *d_gray, u
         first2[n] = acc;
         SLM_TRY(feat_describe(c, st, ws->feat_desc[1], run2, all2, &d_desc2));
     }
-    uint64_t total = 0;
+    fo.kp = std::move(kp);
+    fo.kp2 = std::move(kp2);
+    fo.first1 = std::move(first1);
+    fo.first2 = std::move(first2);
+    fo.d_desc1 = d_desc1;
+    fo.d_desc2 = d_desc2;
+    return SLM_OK;
+}
+
+// Copies a batch's features out: image k to kps / desc rows from off[k] on.
+slm_status feat_emit(const FeatOut &fo, uint32_t n, const uint64_t *off, slm_keypoint *kps, float *desc,
+                     cudaStream_t st) {
     for (uint32_t k = 0; k < n; ++k) {
-        off[k] = total;
-        total += kp[k].size() + kp2[k].size();
-    }
-    off[n] = total;
-    if (total > cap) return fail(SLM_CAPACITY, "feature output holds " + std::to_string(cap) + " of " +
-                                                   std::to_string(total) + " features");
-    for (uint32_t k = 0; k < n; ++k) {
-        const uint64_t n1 = kp[k].size(), n2 = kp2[k].size();
+        const uint64_t n1 = fo.kp[k].size(), n2 = fo.kp2[k].size();
         if (kps) {
-            std::memcpy(kps + off[k], kp[k].data(), sizeof(slm_keypoint) * n1);
-            if (n2) std::memcpy(kps + off[k] + n1, kp2[k].data(), sizeof(slm_keypoint) * n2);
+            std::memcpy(kps + off[k], fo.kp[k].data(), sizeof(slm_keypoint) * n1);
+            if (n2) std::memcpy(kps + off[k] + n1, fo.kp2[k].data(), sizeof(slm_keypoint) * n2);
         }
         if (desc) {
             if (n1)
-                SLM_CU(cudaMemcpyAsync(desc + off[k] * kDesc, d_desc1 + first1[k] * kDesc, 4ull * kDesc * n1,
+                SLM_CU(cudaMemcpyAsync(desc + off[k] * kDesc, fo.d_desc1 + fo.first1[k] * kDesc, 4ull * kDesc * n1,
                                        cudaMemcpyDefault, st));
             if (n2)
-                SLM_CU(cudaMemcpyAsync(desc + (off[k] + n1) * kDesc, d_desc2 + first2[k] * kDesc, 4ull * kDesc * n2,
-                                       cudaMemcpyDefault, st));
+                SLM_CU(cudaMemcpyAsync(desc + (off[k] + n1) * kDesc, fo.d_desc2 + fo.first2[k] * kDesc,
+                                       4ull * kDesc * n2, cudaMemcpyDefault, st));
         }
     }
-    SLM_CU(cudaStreamSynchronize(st));
     return SLM_OK;
+}
+
+// The body of both entry points: the images (gray f32, or RGB8 converted on
+// the device) go in two halves to two workspaces run from two host threads,
+// so one half's host work (candidate ordering, keypoints) overlaps the other
+// half's kernels; one workspace below 4 images. Features come out in image
+// order whatever the split.
+slm_status feat_call(slm_ctx *c, const void *imgs, bool rgb, uint32_t n, uint32_t w, uint32_t h,
+                     const slm_detector_config &cfg, slm_keypoint *kps, float *desc, uint64_t cap, uint64_t *off) {
+    const uint64_t wh = (uint64_t)w * h;
+    const uint32_t parts = n >= 4 ? 2 : 1;
+    const uint32_t bnd[3] = {0, parts == 2 ? n / 2 : n, n};
+    Workspace *ws[2] = {nullptr, nullptr};
+    for (uint32_t p = 0; p < parts; ++p) {
+        slm_status a = ws_acquire(c, &ws[p]);
+        if (a != SLM_OK) {
+            for (uint32_t q = 0; q < p; ++q) ws_release(c, ws[q]);
+            return a;
+        }
+    }
+    FeatOut outs[2];
+    slm_status sts[2] = {SLM_OK, SLM_OK};
+    std::string errs[2];
+    auto job = [&](uint32_t p) {
+        Workspace *W = ws[p];
+        const uint32_t np = bnd[p + 1] - bnd[p];
+        slm_status r = SLM_OK;
+        if (np) {
+            cudaSetDevice(c->device);
+            const uint64_t o_rgb = feat_align(4 * np * wh);
+            r = W->feat_in.ensure(c, rgb ? o_rgb + 3 * np * wh : 4 * np * wh);
+            unsigned char *d = W->feat_in.as<unsigned char>();
+            if (r == SLM_OK) {
+                const unsigned char *src = static_cast<const unsigned char *>(imgs) + (rgb ? 3 : 4) * bnd[p] * wh;
+                if (cudaMemcpyAsync(rgb ? d + o_rgb : d, src, (rgb ? 3 : 4) * np * wh, cudaMemcpyDefault,
+                                    W->stream) != cudaSuccess)
+                    r = fail(SLM_CUDA_ERROR, std::string("image upload: ") + cudaGetErrorString(cudaGetLastError()));
+            }
+            if (r == SLM_OK && rgb) {
+                launch_gray_from_rgb8(d + o_rgb, reinterpret_cast<float *>(d), np * wh, W->stream);
+                if (cudaGetLastError() != cudaSuccess) r = fail(SLM_CUDA_ERROR, "gray conversion launch failed");
+            }
+            if (r == SLM_OK) r = detect_describe_run(c, W, W->feat_in.as<float>(), np, w, h, cfg, outs[p]);
+        }
+        sts[p] = r;
+        if (r != SLM_OK) errs[p] = g_last_error;
+    };
+    if (parts == 2) {
+        std::thread helper;
+        try {
+            helper = std::thread(job, 1u);
+        } catch (...) {  // no thread to be had: the halves one after the other
+        }
+        job(0);
+        if (helper.joinable())
+            helper.join();
+        else
+            job(1);
+    } else {
+        job(0);
+    }
+    slm_status st = SLM_OK;
+    for (uint32_t p = 0; p < parts && st == SLM_OK; ++p)
+        if (sts[p] != SLM_OK) {
+            st = sts[p];
+            g_last_error = errs[p];
+        }
+    if (st == SLM_OK) {
+        uint64_t total = 0;
+        for (uint32_t p = 0; p < parts; ++p)
+            for (uint32_t k = 0; k < bnd[p + 1] - bnd[p]; ++k) {
+                off[bnd[p] + k] = total;
+                total += outs[p].kp[k].size() + outs[p].kp2[k].size();
+            }
+        off[n] = total;
+        if (total > cap)
+            st = fail(SLM_CAPACITY, "feature output holds " + std::to_string(cap) + " of " + std::to_string(total) +
+                                        " features");
+    }
+    for (uint32_t p = 0; p < parts && st == SLM_OK; ++p)
+        if (bnd[p + 1] > bnd[p]) st = feat_emit(outs[p], bnd[p + 1] - bnd[p], off + bnd[p], kps, desc, ws[p]->stream);
+    for (uint32_t p = 0; p < parts; ++p) {
+        const cudaError_t e = cudaStreamSynchronize(ws[p]->stream);
+        if (st == SLM_OK && e != cudaSuccess)
+            st = fail(SLM_CUDA_ERROR, std::string("slm_detect_and_describe: ") + cudaGetErrorString(e));
+        ws_release(c, ws[p]);
+    }
+    return st;
 }
 
 slm_status feat_entry_checks(slm_ctx *c, const void *imgs, uint32_t n, uint32_t w, uint32_t h,
@@ -3107,18 +3207,9 @@ extern "C" slm_status slm_detect_and_describe(slm_ctx *c, const float *imgs, uin
     NvtxRange range_("slm_detect_and_describe");
     SLM_TRY(feat_entry_checks(c, imgs, n, w, h, cfg, off));
     for (uint32_t k = 0; k <= n; ++k) off[k] = 0;
-    const uint64_t wh = (uint64_t)w * h;
-    if (!n || !wh) return SLM_OK;
+    if (!n || !((uint64_t)w * h)) return SLM_OK;
     SLM_TRY(ctx_check_device(c));
-    Workspace *ws = nullptr;
-    SLM_TRY(ws_acquire(c, &ws));
-    slm_status st = ws->feat_in.ensure(c, 4 * n * wh);
-    if (st == SLM_OK && cudaMemcpyAsync(ws->feat_in.p, imgs, 4 * n * wh, cudaMemcpyDefault, ws->stream) != cudaSuccess)
-        st = fail(SLM_CUDA_ERROR, std::string("slm_detect_and_describe: ") + cudaGetErrorString(cudaGetLastError()));
-    if (st == SLM_OK) st = detect_describe_dev(c, ws, ws->feat_in.as<float>(), n, w, h, *cfg, kps, desc, cap, off);
-    if (st != SLM_OK) cudaStreamSynchronize(ws->stream);
-    ws_release(c, ws);
-    return st;
+    return feat_call(c, imgs, false, n, w, h, *cfg, kps, desc, cap, off);
 }
 
 extern "C" slm_status slm_detect_and_describe_rgb8(slm_ctx *c, const uint8_t *rgb, uint32_t n, uint32_t w,
@@ -3127,26 +3218,9 @@ extern "C" slm_status slm_detect_and_describe_rgb8(slm_ctx *c, const uint8_t *rg
     NvtxRange range_("slm_detect_and_describe_rgb8");
     SLM_TRY(feat_entry_checks(c, rgb, n, w, h, cfg, off));
     for (uint32_t k = 0; k <= n; ++k) off[k] = 0;
-    const uint64_t wh = (uint64_t)w * h;
-    if (!n || !wh) return SLM_OK;
+    if (!n || !((uint64_t)w * h)) return SLM_OK;
     SLM_TRY(ctx_check_device(c));
-    Workspace *ws = nullptr;
-    SLM_TRY(ws_acquire(c, &ws));
-    // the gray images first in feat_in, the RGB bytes staged after them
-    const uint64_t o_rgb = feat_align(4 * n * wh);
-    slm_status st = ws->feat_in.ensure(c, o_rgb + 3 * n * wh);
-    unsigned char *d = ws->feat_in.as<unsigned char>();
-    if (st == SLM_OK && cudaMemcpyAsync(d + o_rgb, rgb, 3 * n * wh, cudaMemcpyDefault, ws->stream) != cudaSuccess)
-        st = fail(SLM_CUDA_ERROR, std::string("slm_detect_and_describe_rgb8: ") +
-                                      cudaGetErrorString(cudaGetLastError()));
-    if (st == SLM_OK) {
-        launch_gray_from_rgb8(d + o_rgb, reinterpret_cast<float *>(d), n * wh, ws->stream);
-        if (cudaGetLastError() != cudaSuccess) st = fail(SLM_CUDA_ERROR, "gray conversion launch failed");
-    }
-    if (st == SLM_OK) st = detect_describe_dev(c, ws, ws->feat_in.as<float>(), n, w, h, *cfg, kps, desc, cap, off);
-    if (st != SLM_OK) cudaStreamSynchronize(ws->stream);
-    ws_release(c, ws);
-    return st;
+    return feat_call(c, rgb, true, n, w, h, *cfg, kps, desc, cap, off);
 }
 
 extern "C" slm_status slm_describe(slm_ctx *c, const float *img, uint32_t w, uint32_t h, const slm_keypoint *kps,

@@ -203,3 +203,16 @@ def test_images_to_store_to_matches_on_the_device(matcher):
     assert len(got[0]) > 50
     plan.close()
     store.close()
+
+
+@pytest.mark.parametrize("n,w,h,seed", [(5, 320, 200, 31), (4, 150, 110, 32), (9, 64, 48, 33)])
+def test_batches_split_over_two_workspaces(matcher, n, w, h, seed):
+    # from 4 images a call runs its two halves on two workspaces; the features
+    # come back in image order, each image's equal to the oracle's (the small
+    # sizes take the upsampled detection in both halves)
+    views = synth.scene_views(n, w, h, seed=seed)
+    cfg = F.detector_config()
+    got = F.detect_and_describe(matcher, views, cfg)
+    assert len(got) == n
+    for k in range(n):
+        check_equal(got[k], O.gray_from_rgb8(views[k]), cfg)
