@@ -25,6 +25,7 @@ of the reference (oracle/, all host threads) on a bounded sample.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -262,7 +263,13 @@ def serve_configs(seed: int, rates: str, threads: int, prec_list=("bf16", "fp32"
             runs = []
             for _ in range(1 if rate else 3):
                 srv = serve.Server(int(z.counts.sum()), len(z.counts), prec, slots=3)
-                res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
+                # the client's garbage collector stays out of the measured latencies
+                gc.collect()
+                gc.disable()
+                try:
+                    res, lats, wall = serve.stream_zone(srv, z, rate, seed=int(rate or 0))
+                finally:
+                    gc.enable()
                 st = srv.stats()
                 srv.close()
                 runs.append((wall, res, lats, st))
