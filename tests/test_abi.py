@@ -90,3 +90,29 @@ def test_no_device_is_an_error_not_a_fallback():
     with pytest.raises(sm.SlmError) as e:
         sm.Matcher()
     assert e.value.status == _lib.SLM_NO_DEVICE
+
+
+def test_detector_config_default_is_the_reference_default():
+    # DetectorConfig::default() (features.rs:278-293), without a GPU
+    from skylens_match import features as F
+    c = F.detector_config()
+    o = O.DetectorConfig()
+    for f in ("octaves", "scales", "max_features", "upscale_below", "upscale_fill"):
+        assert getattr(c, f) == getattr(o, f), f
+    for f in ("sigma0", "contrast", "edge_ratio"):
+        assert np.float32(getattr(c, f)) == np.float32(getattr(o, f)), f
+
+
+def test_descriptor_producer_argument_checks_need_no_device():
+    from skylens_match import features as F
+    L = sm.load()
+    cfg = F.detector_config()
+    off = np.zeros(2, np.uint64)
+    offp = off.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    img = np.zeros((8, 8), np.float32)
+    # NULL context, NULL images with n > 0, oversized images, too many (image, layer) grid slots
+    assert L.slm_detect_and_describe(None, ctypes.c_void_p(img.ctypes.data), 1, 8, 8, ctypes.byref(cfg), None, None,
+                                     0, offp) == _lib.SLM_INVALID_ARG
+    bad = F.detector_config(scales=0)
+    assert L.slm_detect_and_describe(None, None, 0, 8, 8, ctypes.byref(bad), None, None, 0, offp) == _lib.SLM_INVALID_ARG
+    assert L.slm_describe(None, None, 8, 8, None, 0, None) == _lib.SLM_INVALID_ARG
