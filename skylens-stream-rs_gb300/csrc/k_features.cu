@@ -428,13 +428,16 @@ struct DescSample {
 
 // One CTA per feature (describe_with, features.rs:521-592). The (2r+1)^2
 // window goes through in chunks of 128 samples in raster order: each thread
-// computes one sample (rotated cell coordinates, the trilinear weights), then
-// warp iv owns the 32 bins of spatial row iv (lane = iu * 8 + io) and adds,
-// sample by sample in raster order, the contributions of the samples that
-// touch that row: every bin's sum is the reference's, in its order.
+// computes one sample (rotated cell coordinates, the trilinear weights) and
+// marks, for each bin it adds to, its bit in that bin's mask of the chunk's
+// 32-sample group; then thread (warp iv, lane iu * 8 + io) owns bin (iv, iu,
+// io) and adds the contributions of the samples whose bits its masks hold,
+// in sample order: every bin's sum is the reference's, in its order, and a
+// thread steps only through the samples that touch its own bin.
 __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) {
     __shared__ DescSample smp[kDescThreads];
-    __shared__ unsigned rel[4][kDescThreads / 32];  // per warp: samples touching its row, by 32-sample group
+    // per chunk parity, 32-sample group, spatial row and lane: the group's samples adding to that bin
+    __shared__ uint32_t bmask[2][kDescThreads / 32][4][32];
     __shared__ float hist[kDesc];
     __shared__ float norm_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -470,7 +473,10 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
     const int total = side * side;
     float acc = 0.0f;  // bin (warp, lane)
     const uint32_t my_bit = 1u << lane;
-    for (int base = 0; base < total; base += kDescThreads) {
+    for (int e = tid; e < (kDescThreads / 32) * 4 * 32; e += kDescThreads) (&bmask[0][0][0][0])[e] = 0u;
+    __syncthreads();
+    int par = 0;
+    for (int base = 0; base < total; base += kDescThreads, par ^= 1) {
         const int t = base + tid;
         bool valid = false;
         DescSample q{};
@@ -518,14 +524,21 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
             }
         }
         smp[tid] = q;
+        if (valid) {
 #pragma unroll
-        for (int row = 0; row < 4; ++row) {
-            const unsigned m = __ballot_sync(0xffffffffu, valid && (q.iv0 == row || q.iv0 + 1 == row));
-            if (lane == 0) rel[row][warp] = m;
+            for (int dv = 0; dv < 2; ++dv) {
+                const int row = q.iv0 + dv;
+                if (row < 0 || row >= NC) continue;
+                uint32_t hm = q.hit;
+                while (hm) {
+                    const int l = __ffs(hm) - 1;
+                    hm &= hm - 1;
+                    atomicOr(&bmask[par][warp][row][l], my_bit);
+                }
+            }
         }
         __syncthreads();
-        // warp `warp` owns spatial row iv = warp; samples two at a time (both
-        // contributions formed first, then added in sample order)
+        // thread (warp, lane) owns bin (iv = warp, iu = lane / 8, io = lane % 8)
         auto contrib = [&](const DescSample &s) {
             const float pv = s.iv0 == warp ? s.pv0 : s.pv1;
             const float wu = (s.second_u & my_bit) ? s.wu1 : s.wu0;
@@ -533,24 +546,15 @@ __global__ void __launch_bounds__(kDescThreads) describe_kernel(DescribeArgs a) 
             return pv * wu * wo;
         };
         for (int g = 0; g < kDescThreads / 32; ++g) {
-            unsigned m = rel[warp][g];
+            unsigned m = bmask[par][g][warp][lane];
             while (m) {
-                const int j1 = g * 32 + __ffs(m) - 1;
+                const int j = g * 32 + __ffs(m) - 1;
                 m &= m - 1;
-                const DescSample &s1 = smp[j1];
-                if (m) {
-                    const int j2 = g * 32 + __ffs(m) - 1;
-                    m &= m - 1;
-                    const DescSample &s2 = smp[j2];
-                    const bool h1 = s1.hit & my_bit, h2 = s2.hit & my_bit;
-                    const float c1 = contrib(s1), c2 = contrib(s2);
-                    if (h1) acc += c1;
-                    if (h2) acc += c2;
-                } else if (s1.hit & my_bit) {
-                    acc += contrib(s1);
-                }
+                acc += contrib(smp[j]);
             }
         }
+        // the other parity's masks, free since the last chunk's barrier, for the next chunk
+        for (int e = tid; e < (kDescThreads / 32) * 4 * 32; e += kDescThreads) (&bmask[par ^ 1][0][0][0])[e] = 0u;
         __syncthreads();
     }
     hist[warp * 32 + lane] = acc;  // (iv * 4 + iu) * 8 + io
