@@ -216,3 +216,16 @@ def test_batches_split_over_two_workspaces(matcher, n, w, h, seed):
     assert len(got) == n
     for k in range(n):
         check_equal(got[k], O.gray_from_rgb8(views[k]), cfg)
+
+
+def test_candidate_overflow_reruns_with_room(matcher):
+    # a dense texture of 2400 x 2400 with the contrast test off gives about
+    # 23,000 refined extrema (23,182 distinct keypoints in the oracle), more
+    # than the first candidate buffer of a one-image call holds (16,384): the
+    # library runs the pyramid again with room for all of them, and the list
+    # (cut at max_features) equals the oracle's
+    img = synth.scene_canvas(2400, 2400, seed=41, density=0.012)
+    cfg = F.detector_config(contrast=0.0, edge_ratio=1000.0, upscale_below=0)
+    got = F.detect_and_describe(matcher, img, cfg)[0]
+    assert len(got[0]) == int(cfg.max_features)
+    check_equal(got, img, cfg)
