@@ -520,6 +520,76 @@ def features_configs(m, threads: int, n: int = 24, reps: int = 5, cpu_images: in
                              "sample": f"{cpu_images} images of the same scene, one per thread, median of 2"}}
 
 
+def tracks_configs(m, z, res, off, reps: int = 3) -> dict:
+    """build_tracks with ConflictPolicy::Drop (tracks.rs:190) over the zone's
+    match lists (every pair's BF16 list as its verified matches; the
+    reference feeds RANSAC inliers). GPU: slm_build_tracks_drop from host
+    arrays (upload, edge set, components on the device, grouping and the cap
+    on the host); CPU: the oracle's restatement (one thread, as the
+    reference's union-find). Tracks and counts must be equal."""
+    import ctypes
+
+    import oracle as O
+    from skylens_match import tracks as T
+    pairs = [(int(u), int(v), res[int(off[k]):int(off[k + 1])]) for k, (u, v) in enumerate(z.pairs.tolist())]
+    nf = np.ascontiguousarray(z.counts, dtype=np.uint32)
+    arr, flat = T.pack(pairs)
+    oarr, oflat = O.pack_pairs(pairs)
+    n_match = len(flat)
+    P = ctypes.POINTER
+    cap_t, cap_o = max(n_match, 1), max(2 * n_match, 1)
+    toff = np.zeros(cap_t + 1, np.uint64)
+    obs = np.zeros((cap_o, 2), np.uint32)
+    nt, no = ctypes.c_uint64(), ctypes.c_uint64()
+    gst = T.SlmTrackStats()
+
+    def gpu():
+        st = m._L.slm_build_tracks_drop(m.handle, nf.ctypes.data_as(P(ctypes.c_uint32)), len(nf), arr, len(pairs),
+                                        flat.ctypes.data_as(P(T.SlmPair)), 3, 100000,
+                                        toff.ctypes.data_as(P(ctypes.c_uint64)), cap_t, obs.ctypes.data_as(P(T.SlmPair)),
+                                        cap_o, ctypes.byref(nt), ctypes.byref(no), ctypes.byref(gst))
+        if st:
+            raise RuntimeError(f"slm_build_tracks_drop: status {st}")
+
+    otoff = np.zeros(cap_t + 1, np.uint64)
+    onodes = np.zeros(cap_o, np.uint64)
+    ost = O.TrackStats()
+
+    def cpu():
+        return O.lib().orc_build_tracks_drop(nf.ctypes.data_as(P(ctypes.c_uint32)), len(nf),
+                                             ctypes.cast(oarr, ctypes.c_void_p), len(pairs),
+                                             oflat.ctypes.data_as(P(ctypes.c_uint32)), 3, 100000,
+                                             otoff.ctypes.data_as(P(ctypes.c_uint64)), cap_t,
+                                             onodes.ctypes.data_as(P(ctypes.c_uint64)), cap_o, ctypes.byref(ost))
+
+    gpu()
+    g = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        gpu()
+        g.append(time.perf_counter() - t0)
+    c = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        ont = cpu()
+        c.append(time.perf_counter() - t0)
+    # equal: the same track boundaries and nodes ((image, feature) from nodes)
+    noff = np.concatenate([[0], np.cumsum(z.counts, dtype=np.uint64)])
+    nobs = int(no.value)
+    nodes_g = noff[obs[:nobs, 0].astype(np.int64)] + obs[:nobs, 1].astype(np.uint64)
+    equal = (int(nt.value) == int(ont) and np.array_equal(toff[:int(nt.value) + 1], otoff[:int(ont) + 1])
+             and np.array_equal(nodes_g, onodes[:nobs]) and gst.as_dict() == ost.as_dict())
+    gm, cm = float(np.median(g)), float(np.median(c))
+    return {"metric": "tracks (ConflictPolicy::Drop): verified matches/s into tracks",
+            "config": {"workload": "zone240 match lists", "pairs": len(pairs), "matches": n_match,
+                       "nodes": int(nf.sum()), "min_length": 3, "max_tracks": 100000},
+            "stats": gst.as_dict(),
+            "gpu": {"ms": gm * 1e3, "matches_per_s": n_match / gm,
+                    "timed": "slm_build_tracks_drop from host arrays (upload and read-back included)"},
+            "cpu": {"ms": cm * 1e3, "matches_per_s": n_match / cm, "threads": 1, "kind": "port"},
+            "equal": bool(equal)}
+
+
 def settled_frac(s, na, prec):
     """Fractions of a single pair's rows settled by each tier: by the FP8 bound,
     by the BF16 bound (BF16 pairs, and FP8 pairs rescued by the BF16 passes),
@@ -836,6 +906,9 @@ def main():
                            "serve": serve_rec,
                            "ransac_scoring": ransac_configs(m, os.cpu_count() or 1),
                            "descriptor_producer": features_configs(m, os.cpu_count() or 1)}
+        if prec in ("bf16", "fp8", "fp32") and args.positions == 80:
+            pr_, of_ = plan.results()
+            line["configs"]["tracks"] = tracks_configs(m, z, pr_, of_)
         line["configs"]["wall_s"] = time.perf_counter() - t_c
     if rank == 0:
         s = json.dumps(line)

@@ -431,6 +431,44 @@ slm_status slm_detect_and_describe_rgb8(slm_ctx *ctx, const uint8_t *rgb, uint32
 slm_status slm_describe(slm_ctx *ctx, const float *img, uint32_t w, uint32_t h, const slm_keypoint *kps, uint32_t n,
                         float *desc);
 
+/* ---------------------------------------------------------- tracks */
+
+/* One image pair's verified matches (PairMatches, tracks.rs:44-50):
+ * matches[first .. first + count) of a flat slm_pair array, i = feature of
+ * image_a, j = feature of image_b. */
+typedef struct {
+    uint32_t image_a, image_b;
+    uint64_t first, count;
+} slm_pair_matches;
+
+/* TrackStats (tracks.rs:130-152) of ConflictPolicy::Drop. */
+typedef struct {
+    uint64_t edges;           /* distinct (image, feature) edges */
+    uint64_t invalid_matches; /* same-image pairs and out-of-range indices */
+    uint64_t conflicts;       /* components dropped for holding two features of one image */
+    uint64_t too_short;       /* components below min_length */
+    uint64_t truncated;       /* tracks beyond max_tracks */
+    uint64_t tracks;
+} slm_track_stats;
+
+/* build_tracks(pairs, keypoints, &TrackConfig { policy: ConflictPolicy::Drop,
+ * min_length, max_tracks }) (tracks.rs:190): the connected components of the
+ * verified matches over nodes (image, feature), n_features[i] features in
+ * image i; a component holding two features of one image is dropped, one
+ * shorter than max(min_length, 2) too; select_tracks (tracks.rs:786) keeps at
+ * most max_tracks (longest, then widest image span, then first observation),
+ * in first-observation order. Track t is obs[track_off[t] .. track_off[t+1])
+ * (i = image, j = feature, ascending); track_off has cap_tracks + 1 entries.
+ * SLM_CAPACITY when the tracks or observations do not fit (*n_tracks and
+ * *n_obs give the sizes needed). The graph work (edge set, components) runs
+ * on the GPU; the result is the reference's exactly (integer work). The
+ * default policy, ConflictPolicy::Split, is not provided. */
+slm_status slm_build_tracks_drop(slm_ctx *ctx, const uint32_t *n_features, uint32_t n_images,
+                                 const slm_pair_matches *pairs, uint32_t n_pairs, const slm_pair *matches,
+                                 uint32_t min_length, uint64_t max_tracks, uint64_t *track_off, uint64_t cap_tracks,
+                                 slm_pair *obs, uint64_t cap_obs, uint64_t *n_tracks, uint64_t *n_obs,
+                                 slm_track_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SRC = os.path.join(HERE, "oracle.c")
-SRCS = [SRC, os.path.join(HERE, "features.c")]
+SRCS = [SRC, os.path.join(HERE, "features.c"), os.path.join(HERE, "tracks.c")]
 
 _lock = threading.Lock()
 _lib = None
@@ -101,6 +101,9 @@ def lib():
             L.orc_dominant_orientations.restype = i64
             L.orc_detect_and_describe.argtypes = [f32p, i64, i64, ctypes.c_void_p, i32, f32p, f32p, i64]
             L.orc_detect_and_describe.restype = i64
+            L.orc_build_tracks_drop.argtypes = [u32p, i64, ctypes.c_void_p, i64, u32p, i64, i64, u64p, i64, u64p, i64,
+                                                ctypes.c_void_p]
+            L.orc_build_tracks_drop.restype = i64
             _lib = L
     return _lib
 
@@ -385,3 +388,53 @@ def detect_and_describe(img, cfg: DetectorConfig | None = None, cr: bool = False
                                   _p(kps, ctypes.c_float), _p(desc, ctypes.c_float), cap)
     assert n <= cap
     return kps[:n].copy(), desc[:n].copy()
+
+
+# ---- tracks, ConflictPolicy::Drop (tracks.c; crates/core/src/tracks.rs) ---
+
+class PairMatches(ctypes.Structure):
+    """PairMatches (tracks.rs:44-50): matches[first .. first + count) of a flat array."""
+    _fields_ = [("image_a", ctypes.c_uint32), ("image_b", ctypes.c_uint32), ("first", ctypes.c_uint64),
+                ("count", ctypes.c_uint64)]
+
+
+class TrackStats(ctypes.Structure):
+    _fields_ = [("edges", ctypes.c_uint64), ("invalid_matches", ctypes.c_uint64), ("conflicts", ctypes.c_uint64),
+                ("too_short", ctypes.c_uint64), ("truncated", ctypes.c_uint64), ("tracks", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+def pack_pairs(pairs):
+    """[(image_a, image_b, [(fa, fb), ...]), ...] -> (PairMatches array, flat uint32 (M, 2))."""
+    arr = (PairMatches * max(len(pairs), 1))()
+    flat, first = [], 0
+    for k, (a, b, m) in enumerate(pairs):
+        m = np.asarray(m, dtype=np.uint32).reshape(-1, 2)
+        arr[k] = PairMatches(a, b, first, len(m))
+        flat.append(m)
+        first += len(m)
+    flat = np.ascontiguousarray(np.concatenate(flat) if flat else np.zeros((0, 2), np.uint32))
+    return arr, flat
+
+
+def build_tracks_drop(n_features, pairs, min_length: int = 3, max_tracks: int = 100_000):
+    """build_tracks with ConflictPolicy::Drop (tracks.rs:190-259) -> (tracks as
+    lists of (image, feature), stats dict)."""
+    nf = np.ascontiguousarray(n_features, dtype=np.uint32)
+    arr, flat = pack_pairs(pairs)
+    off = np.concatenate([[0], np.cumsum(nf, dtype=np.uint64)])
+    cap_n = max(2 * len(flat), 1)
+    toff = np.zeros(cap_n + 1, np.uint64)
+    nodes = np.zeros(cap_n, np.uint64)
+    st = TrackStats()
+    nt = lib().orc_build_tracks_drop(_p(nf, ctypes.c_uint32), len(nf), ctypes.cast(arr, ctypes.c_void_p), len(pairs),
+                                     _p(flat, ctypes.c_uint32), min_length, max_tracks, _p(toff, ctypes.c_uint64),
+                                     cap_n, _p(nodes, ctypes.c_uint64), cap_n, ctypes.byref(st))
+    img = np.searchsorted(off, np.arange(int(off[-1])), side="right") - 1 if len(off) > 1 else np.zeros(0, int)
+    tracks = []
+    for t in range(nt):
+        ns = nodes[int(toff[t]):int(toff[t + 1])]
+        tracks.append([(int(img[x]), int(x - off[img[x]])) for x in ns])
+    return tracks, st.as_dict()

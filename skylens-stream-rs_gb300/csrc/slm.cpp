@@ -3278,3 +3278,179 @@ extern "C" slm_status slm_describe(slm_ctx *c, const float *img, uint32_t w, uin
     ws_release(c, ws);
     return st;
 }
+
+// ------------------------------------------------------------------- tracks
+//
+// build_tracks with ConflictPolicy::Drop (tracks.rs:190-259): the edge set
+// and the connected components on the device (k_tracks.cu), then the
+// components in node order, the conflict and length rules and select_tracks
+// (tracks.rs:472-500, 786-799) on the host from the representatives.
+
+extern "C" slm_status slm_build_tracks_drop(slm_ctx *c, const uint32_t *n_features, uint32_t n_images,
+                                            const slm_pair_matches *pairs, uint32_t n_pairs, const slm_pair *matches,
+                                            uint32_t min_length, uint64_t max_tracks, uint64_t *track_off,
+                                            uint64_t cap_tracks, slm_pair *obs, uint64_t cap_obs, uint64_t *n_tracks,
+                                            uint64_t *n_obs, slm_track_stats *stats) {
+    NvtxRange range_("slm_build_tracks_drop");
+    if (!c || !n_tracks || !n_obs || (n_images && !n_features) || (n_pairs && !pairs) || (cap_tracks && !track_off) ||
+        (cap_obs && !obs))
+        return fail(SLM_INVALID_ARG, "NULL argument");
+    *n_tracks = *n_obs = 0;
+    slm_track_stats stt{};
+    // node offsets, the matches the pairs name, validity of the ranges
+    std::vector<uint64_t> off(n_images + 1, 0);
+    for (uint32_t i = 0; i < n_images; ++i) off[i + 1] = off[i] + n_features[i];
+    const uint64_t n = off[n_images];
+    if (n >= 0xffffffffull) return fail(SLM_INVALID_ARG, "at most 2^32 - 2 features in all");
+    uint64_t n_match = 0;
+    for (uint32_t p = 0; p < n_pairs; ++p) {
+        if (pairs[p].count > ~0ull - pairs[p].first) return fail(SLM_INVALID_ARG, "a pair's match range overflows");
+        n_match = std::max(n_match, pairs[p].first + pairs[p].count);
+    }
+    if (n_match && !matches) return fail(SLM_INVALID_ARG, "NULL matches");
+    if (n_match > (1ull << 34)) return fail(SLM_INVALID_ARG, "more than 2^34 matches");
+    std::vector<uint32_t> node_image(n);
+    for (uint32_t i = 0; i < n_images; ++i)
+        std::fill(node_image.begin() + off[i], node_image.begin() + off[i + 1], i);
+    SLM_TRY(ctx_check_device(c));
+    Workspace *ws = nullptr;
+    SLM_TRY(ws_acquire(c, &ws));
+    cudaStream_t s = ws->stream;
+    uint64_t slots = 1024;
+    while (slots < 2 * n_match) slots <<= 1;
+    const uint64_t o_pairs = 0, o_match = feat_align(sizeof(TrackPair) * (uint64_t)n_pairs),
+                   o_nf = feat_align(o_match + 8 * n_match), o_off = feat_align(o_nf + 4ull * n_images),
+                   o_table = feat_align(o_off + 8ull * (n_images + 1)), o_edges = feat_align(o_table + 8 * slots),
+                   o_cnt = feat_align(o_edges + 8 * (n_match + 1)), o_parent = feat_align(o_cnt + 32),
+                   o_used = feat_align(o_parent + 4 * (n + 1)), bytes = feat_align(o_used + n + 1);
+    slm_status st = ws->feat_pyr.ensure(c, bytes);
+    std::vector<uint32_t> parent;
+    std::vector<uint8_t> used;
+    if (st == SLM_OK) {
+        unsigned char *d = ws->feat_pyr.as<unsigned char>();
+        std::vector<TrackPair> tp(n_pairs);
+        for (uint32_t p = 0; p < n_pairs; ++p)
+            tp[p] = TrackPair{pairs[p].image_a, pairs[p].image_b, pairs[p].first, pairs[p].count};
+        TrackArgs a{};
+        a.pairs = reinterpret_cast<const TrackPair *>(d + o_pairs);
+        a.matches = reinterpret_cast<const uint2 *>(d + o_match);
+        a.nf = reinterpret_cast<const uint32_t *>(d + o_nf);
+        a.off = reinterpret_cast<const uint64_t *>(d + o_off);
+        a.n_images = n_images;
+        a.table = reinterpret_cast<unsigned long long *>(d + o_table);
+        a.table_mask = slots - 1;
+        a.edges = reinterpret_cast<unsigned long long *>(d + o_edges);
+        unsigned long long *cnt = reinterpret_cast<unsigned long long *>(d + o_cnt);
+        a.n_edges = cnt;
+        a.n_invalid = cnt + 1;
+        uint32_t *changed = reinterpret_cast<uint32_t *>(cnt + 2);
+        uint32_t *d_parent = reinterpret_cast<uint32_t *>(d + o_parent);
+        uint8_t *d_used = d + o_used;
+        const int grid = 4 * c->sms;
+        cudaError_t e = n_pairs ? cudaMemcpyAsync(d + o_pairs, tp.data(), sizeof(TrackPair) * n_pairs,
+                                                  cudaMemcpyHostToDevice, s)
+                                : cudaSuccess;
+        if (e == cudaSuccess && n_match) e = cudaMemcpyAsync(d + o_match, matches, 8 * n_match, cudaMemcpyDefault, s);
+        if (e == cudaSuccess && n_images)
+            e = cudaMemcpyAsync(d + o_nf, n_features, 4ull * n_images, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d + o_off, off.data(), 8ull * (n_images + 1), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.table, 0xff, 8 * slots, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, 32, s);
+        if (e == cudaSuccess) {
+            launch_track_edges(a, n_pairs, s);
+            launch_track_init(d_parent, d_used, n, grid, s);
+            launch_track_mark(a.edges, a.n_edges, d_used, grid, s);
+            e = cudaGetLastError();
+        }
+        // hooking and pointer jumping until no edge joins two roots (each round
+        // at least halves the number of roots joined by an edge in practice;
+        // bounded by the node count in any case)
+        for (uint64_t round = 0; e == cudaSuccess && round <= n + 1; ++round) {
+            uint32_t h_changed = 0;
+            e = cudaMemsetAsync(changed, 0, 4, s);
+            if (e == cudaSuccess) {
+                launch_track_hook(a.edges, a.n_edges, d_parent, changed, grid, s);
+                launch_track_jump(d_parent, n, grid, s);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&h_changed, changed, 4, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess || !h_changed) break;
+        }
+        unsigned long long h_cnt[2] = {0, 0};
+        parent.resize(n);
+        used.resize(n);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h_cnt, cnt, 16, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(parent.data(), d_parent, 4 * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && n) e = cudaMemcpyAsync(used.data(), d_used, n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = fail(SLM_CUDA_ERROR, std::string("slm_build_tracks_drop: ") + cudaGetErrorString(e));
+        stt.edges = h_cnt[0];
+        stt.invalid_matches = h_cnt[1];
+    }
+    if (st != SLM_OK) cudaStreamSynchronize(s);
+    ws_release(c, ws);
+    if (st != SLM_OK) return st;
+    // components in node order: count per representative, then fill
+    std::vector<uint64_t> start(n + 1, 0);
+    for (uint64_t x = 0; x < n; ++x)
+        if (used[x]) start[parent[x] + 1]++;
+    for (uint64_t x = 0; x < n; ++x) start[x + 1] += start[x];
+    std::vector<uint32_t> members(start[n]);
+    {
+        std::vector<uint64_t> fill(start.begin(), start.end() - 1);
+        for (uint64_t x = 0; x < n; ++x)
+            if (used[x]) members[fill[parent[x]]++] = (uint32_t)x;
+    }
+    struct TrackRef {
+        uint64_t first, begin, len, span;
+    };
+    std::vector<TrackRef> tr;
+    const uint64_t min_len = std::max<uint64_t>(min_length, 2);
+    for (uint64_t r = 0; r < n; ++r) {
+        const uint64_t b = start[r], e = start[r + 1];
+        if (b == e) continue;
+        bool conflict = false;
+        for (uint64_t q = b + 1; q < e && !conflict; ++q)
+            conflict = node_image[members[q]] == node_image[members[q - 1]];
+        if (conflict) {
+            stt.conflicts++;
+        } else if (e - b < min_len) {
+            stt.too_short++;
+        } else {
+            tr.push_back(TrackRef{members[b], b, e - b, node_image[members[e - 1]] - node_image[members[b]]});
+        }
+    }
+    // select_tracks (tracks.rs:786-799); tr is already in first-observation order
+    if (tr.size() > max_tracks) {
+        std::sort(tr.begin(), tr.end(), [](const TrackRef &x, const TrackRef &y) {
+            if (x.len != y.len) return x.len > y.len;
+            if (x.span != y.span) return x.span > y.span;
+            return x.first < y.first;
+        });
+        stt.truncated = tr.size() - max_tracks;
+        tr.resize(max_tracks);
+        std::sort(tr.begin(), tr.end(), [](const TrackRef &x, const TrackRef &y) { return x.first < y.first; });
+    }
+    stt.tracks = tr.size();
+    uint64_t total = 0;
+    for (const TrackRef &t : tr) total += t.len;
+    *n_tracks = tr.size();
+    *n_obs = total;
+    if (stats) *stats = stt;
+    if (tr.size() > cap_tracks || total > cap_obs)
+        return fail(SLM_CAPACITY, "track output holds " + std::to_string(cap_tracks) + " tracks / " +
+                                      std::to_string(cap_obs) + " observations of " + std::to_string(tr.size()) +
+                                      " / " + std::to_string(total));
+    uint64_t w = 0;
+    if (cap_tracks) track_off[0] = 0;
+    for (uint64_t t = 0; t < tr.size(); ++t) {
+        for (uint64_t q = 0; q < tr[t].len; ++q, ++w) {
+            const uint32_t x = members[tr[t].begin + q];
+            obs[w].i = node_image[x];
+            obs[w].j = (uint32_t)(x - off[node_image[x]]);
+        }
+        track_off[t + 1] = w;
+    }
+    return SLM_OK;
+}

@@ -242,4 +242,32 @@ void launch_extrema(const ExtremaArgs &a, int nimg, cudaStream_t s);
 void launch_orient(const OrientArgs &a, uint32_t n, cudaStream_t s);
 void launch_describe(const DescribeArgs &a, uint32_t njobs, cudaStream_t s);
 
+// ------------------------------------------------------ tracks (k_tracks.cu)
+
+struct TrackPair {  // slm_pair_matches
+    uint32_t image_a, image_b;
+    uint64_t first, count;
+};
+
+struct TrackArgs {
+    const TrackPair *pairs;
+    const uint2 *matches;     // (feature of image_a, feature of image_b)
+    const uint32_t *nf;       // features per image
+    const uint64_t *off;      // first node of each image
+    uint32_t n_images;
+    unsigned long long *table;  // open-addressing edge set, all ones = empty
+    uint64_t table_mask;      // slots - 1 (a power of two)
+    unsigned long long *edges;  // the distinct edges, in insertion order
+    unsigned long long *n_edges;
+    unsigned long long *n_invalid;
+};
+
+void launch_track_edges(const TrackArgs &a, uint32_t n_pairs, cudaStream_t s);
+void launch_track_init(uint32_t *parent, uint8_t *used, uint64_t n, int grid, cudaStream_t s);
+void launch_track_mark(const unsigned long long *edges, const unsigned long long *n_edges, uint8_t *used, int grid,
+                       cudaStream_t s);
+void launch_track_hook(const unsigned long long *edges, const unsigned long long *n_edges, uint32_t *parent,
+                       uint32_t *changed, int grid, cudaStream_t s);
+void launch_track_jump(uint32_t *parent, uint64_t n, int grid, cudaStream_t s);
+
 }  // namespace slm

@@ -12,9 +12,9 @@ BUILT_PRECISIONS = ("fp32", "bf16", "fp8")
 from .matching import (CAM_FRONT, CAM_LEFT, CAM_RIGHT, PAIR_CROSS, PAIR_POW2_MAX, PAIR_TEMPORAL, USIZE_MAX,
                        BatchPlan, DescriptorStore, Matcher, PairSchedule, candidate_pairs, default_matcher,
                        match_pairs, match_scheduled_pairs, ratio_match, scheduled_pairs)
-from . import features
+from . import features, tracks
 
 __all__ = ["SlmError", "load", "library_path", "build", "Matcher", "DescriptorStore", "BatchPlan", "PairSchedule",
            "ratio_match", "match_pairs", "match_scheduled_pairs", "candidate_pairs", "scheduled_pairs", "default_matcher",
            "PAIR_TEMPORAL", "PAIR_CROSS", "PAIR_POW2_MAX", "CAM_FRONT", "CAM_RIGHT", "CAM_LEFT", "USIZE_MAX",
-           "features"]
+           "features", "tracks"]

@@ -77,6 +77,18 @@ class SlmDetectorConfig(ctypes.Structure):
                 ("upscale_fill", ctypes.c_int32)]
 
 
+class SlmPairMatches(ctypes.Structure):
+    _fields_ = [("image_a", c_u32), ("image_b", c_u32), ("first", c_u64), ("count", c_u64)]
+
+
+class SlmTrackStats(ctypes.Structure):
+    _fields_ = [("edges", c_u64), ("invalid_matches", c_u64), ("conflicts", c_u64), ("too_short", c_u64),
+                ("truncated", c_u64), ("tracks", c_u64)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 class SlmError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str):
         self.status = status
@@ -149,6 +161,9 @@ SIGNATURES = {
                                              P(c_u64)]),
     "slm_describe": (c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p, c_u32,
                              ctypes.c_void_p]),
+    "slm_build_tracks_drop": (c_int, [ctypes.c_void_p, P(c_u32), c_u32, P(SlmPairMatches), c_u32, P(SlmPair), c_u32,
+                                      c_u64, P(c_u64), c_u64, P(SlmPair), c_u64, P(c_u64), P(c_u64),
+                                      P(SlmTrackStats)]),
 }
 
 _lock = threading.Lock()

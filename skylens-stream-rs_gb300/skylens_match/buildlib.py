@@ -20,7 +20,7 @@ OUT = os.path.join(ROOT, "build")
 LIB = os.path.join(OUT, "libslm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["k_exact.cu", "k_compact.cu", "k_shortlist.cu", "k_noalloc.cu", "k_sampson.cu", "k_features.cu"]
+CU_SOURCES = ["k_exact.cu", "k_compact.cu", "k_shortlist.cu", "k_noalloc.cu", "k_sampson.cu", "k_features.cu", "k_tracks.cu"]
 CPP_SOURCES = ["slm.cpp"]
 HEADERS = ["pack.cuh", "ptx.cuh", "slm_internal.h", "slm_shortlist.h", "fmath_cr.h", "fmath_tables.h"]
 

@@ -116,3 +116,10 @@ def test_descriptor_producer_argument_checks_need_no_device():
     bad = F.detector_config(scales=0)
     assert L.slm_detect_and_describe(None, None, 0, 8, 8, ctypes.byref(bad), None, None, 0, offp) == _lib.SLM_INVALID_ARG
     assert L.slm_describe(None, None, 8, 8, None, 0, None) == _lib.SLM_INVALID_ARG
+
+
+def test_track_builder_argument_checks_need_no_device():
+    L = sm.load()
+    nt, no = ctypes.c_uint64(), ctypes.c_uint64()
+    assert L.slm_build_tracks_drop(None, None, 0, None, 0, None, 3, 10, None, 0, None, 0, ctypes.byref(nt),
+                                   ctypes.byref(no), None) == _lib.SLM_INVALID_ARG
