@@ -97,6 +97,26 @@ pub struct slm_keypoint {
     pub response: f32,
     pub angle: f32,
 }
+/// PairMatches (tracks.rs:44-50): matches[first .. first + count) of a flat slm_pair array.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct slm_pair_matches {
+    pub image_a: u32,
+    pub image_b: u32,
+    pub first: u64,
+    pub count: u64,
+}
+/// TrackStats (tracks.rs:130-152) of ConflictPolicy::Drop.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default, PartialEq, Eq)]
+pub struct slm_track_stats {
+    pub edges: u64,
+    pub invalid_matches: u64,
+    pub conflicts: u64,
+    pub too_short: u64,
+    pub truncated: u64,
+    pub tracks: u64,
+}
 /// DetectorConfig (features.rs:253-293).
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
@@ -180,4 +200,9 @@ extern "C" {
                                         cap: u64, off: *mut u64) -> SlmStatus;
     pub fn slm_describe(ctx: *mut slm_ctx, img: *const f32, w: u32, h: u32, kps: *const slm_keypoint, n: u32,
                         desc: *mut f32) -> SlmStatus;
+    pub fn slm_build_tracks_drop(ctx: *mut slm_ctx, n_features: *const u32, n_images: u32,
+                                 pairs: *const slm_pair_matches, n_pairs: u32, matches: *const slm_pair,
+                                 min_length: u32, max_tracks: u64, track_off: *mut u64, cap_tracks: u64,
+                                 obs: *mut slm_pair, cap_obs: u64, n_tracks: *mut u64, n_obs: *mut u64,
+                                 stats: *mut slm_track_stats) -> SlmStatus;
 }

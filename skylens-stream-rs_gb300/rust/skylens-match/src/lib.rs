@@ -7,6 +7,8 @@
 //!   pipeline.rs:485-493 as one GPU batch.
 //! * `detect_and_describe_rgb8(images, w, h, cfg)`: features of images of one
 //!   size (features.rs:594 detect_and_describe after GrayImage::from_rgb).
+//! * `build_tracks_drop(n_features, pairs, min_length, max_tracks)`: tracks of
+//!   verified matches with ConflictPolicy::Drop (tracks.rs:190).
 //! * `sampson_counts(pts, th, hyps)`: inlier counts of essential-matrix
 //!   hypotheses over one pair's matches (two_view.rs:804-823, count_at_least),
 //!   for a block of RANSAC iterations at once.
@@ -296,4 +298,39 @@ pub fn detect_and_describe_rgb8(images: &[&[u8]], w: u32, h: u32, cfg: &sys::slm
             (kps[a..b].to_vec(), desc[a..b].to_vec())
         })
         .collect()
+}
+
+/// `build_tracks(pairs, keypoints, &TrackConfig { policy: ConflictPolicy::Drop,
+/// min_length, max_tracks })` (tracks.rs:190) on the GPU: per track its
+/// (image, feature) observations in ascending order (the caller attaches
+/// `keypoints[image][feature]`), tracks in first-observation order, and the
+/// counts. `pairs` holds (image_a, image_b, matches of (feature a, feature b)).
+pub fn build_tracks_drop(n_features: &[usize], pairs: &[(usize, usize, Vec<(usize, usize)>)], min_length: usize,
+                         max_tracks: usize) -> (Vec<Vec<(usize, usize)>>, sys::slm_track_stats) {
+    let nf: Vec<u32> = n_features.iter().map(|&n| n as u32).collect();
+    let mut pm = Vec::with_capacity(pairs.len());
+    let mut flat: Vec<sys::slm_pair> = Vec::new();
+    for (a, b, m) in pairs {
+        pm.push(sys::slm_pair_matches { image_a: *a as u32, image_b: *b as u32, first: flat.len() as u64,
+                                        count: m.len() as u64 });
+        flat.extend(m.iter().map(|&(i, j)| sys::slm_pair { i: i as u32, j: j as u32 }));
+    }
+    let cap_t = flat.len().max(1);
+    let cap_o = (2 * flat.len()).max(1);
+    let mut toff = vec![0u64; cap_t + 1];
+    let mut obs = vec![sys::slm_pair { i: 0, j: 0 }; cap_o];
+    let (mut nt, mut no) = (0u64, 0u64);
+    let mut st = sys::slm_track_stats::default();
+    check(
+        unsafe {
+            sys::slm_build_tracks_drop(ctx(), nf.as_ptr(), nf.len() as u32, pm.as_ptr(), pm.len() as u32,
+                                       flat.as_ptr(), min_length as u32, max_tracks as u64, toff.as_mut_ptr(),
+                                       cap_t as u64, obs.as_mut_ptr(), cap_o as u64, &mut nt, &mut no, &mut st)
+        },
+        "slm_build_tracks_drop",
+    );
+    let tracks = (0..nt as usize)
+        .map(|t| obs[toff[t] as usize..toff[t + 1] as usize].iter().map(|o| (o.i as usize, o.j as usize)).collect())
+        .collect();
+    (tracks, st)
 }
