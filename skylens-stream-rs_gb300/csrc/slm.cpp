@@ -3333,7 +3333,14 @@ extern "C" slm_status slm_build_tracks_drop(slm_ctx *c, const uint32_t *n_featur
             tp[p] = TrackPair{pairs[p].image_a, pairs[p].image_b, pairs[p].first, pairs[p].count};
         TrackArgs a{};
         a.pairs = reinterpret_cast<const TrackPair *>(d + o_pairs);
-        a.matches = reinterpret_cast<const uint2 *>(d + o_match);
+        // matches in device memory, or in host memory the device reads directly
+        // (8-byte aligned): read where they lie; otherwise copied first
+        cudaPointerAttributes pa{};
+        const bool on_device = n_match && cudaPointerGetAttributes(&pa, matches) == cudaSuccess &&
+                               pa.type == cudaMemoryTypeDevice;
+        cudaGetLastError();
+        const bool in_place = n_match && (reinterpret_cast<uintptr_t>(matches) & 7) == 0 && (on_device || c->host_direct);
+        a.matches = in_place ? reinterpret_cast<const uint2 *>(matches) : reinterpret_cast<const uint2 *>(d + o_match);
         a.nf = reinterpret_cast<const uint32_t *>(d + o_nf);
         a.off = reinterpret_cast<const uint64_t *>(d + o_off);
         a.n_images = n_images;
@@ -3350,7 +3357,8 @@ extern "C" slm_status slm_build_tracks_drop(slm_ctx *c, const uint32_t *n_featur
         cudaError_t e = n_pairs ? cudaMemcpyAsync(d + o_pairs, tp.data(), sizeof(TrackPair) * n_pairs,
                                                   cudaMemcpyHostToDevice, s)
                                 : cudaSuccess;
-        if (e == cudaSuccess && n_match) e = cudaMemcpyAsync(d + o_match, matches, 8 * n_match, cudaMemcpyDefault, s);
+        if (e == cudaSuccess && n_match && !in_place)
+            e = cudaMemcpyAsync(d + o_match, matches, 8 * n_match, cudaMemcpyDefault, s);
         if (e == cudaSuccess && n_images)
             e = cudaMemcpyAsync(d + o_nf, n_features, 4ull * n_images, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d + o_off, off.data(), 8ull * (n_images + 1), cudaMemcpyHostToDevice, s);

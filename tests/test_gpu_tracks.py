@@ -107,3 +107,31 @@ def test_argument_checks(matcher):
     # a pair naming an image beyond the list is an invalid match, not an error
     t, stats = T.build_tracks_drop(matcher, [1, 1], [(0, 5, [(0, 0)])], min_length=2)
     assert t == [] and stats["invalid_matches"] == 1
+
+
+def test_matches_read_in_place_or_copied(matcher):
+    # 8-byte aligned host matches are read where they lie (where the device can
+    # read host memory); a buffer 4 bytes off is copied first; device matches
+    # are read in place: the same tracks every way
+    import torch
+    nf, pairs = random_graph(7)
+    want = T.build_tracks_drop(matcher, nf, pairs)
+    arr, flat = T.pack(pairs)
+    P = ctypes.POINTER
+    nfa = np.ascontiguousarray(nf, dtype=np.uint32)
+    odd = np.zeros(flat.size + 1, np.uint32)
+    odd[1:] = flat.reshape(-1)
+    dev = torch.from_numpy(flat.reshape(-1).astype(np.int32)).cuda()
+    for ptr in (odd.ctypes.data + 4, dev.data_ptr()):
+        cap_t, cap_o = len(flat) + 1, 2 * len(flat) + 1
+        toff = np.zeros(cap_t + 1, np.uint64)
+        obs = np.zeros((cap_o, 2), np.uint32)
+        nt, no = ctypes.c_uint64(), ctypes.c_uint64()
+        st = T.SlmTrackStats()
+        assert matcher._L.slm_build_tracks_drop(matcher.handle, nfa.ctypes.data_as(P(ctypes.c_uint32)), len(nfa), arr,
+                                                len(pairs), ctypes.cast(ptr, P(T.SlmPair)), 3, 100000,
+                                                toff.ctypes.data_as(P(ctypes.c_uint64)), cap_t,
+                                                obs.ctypes.data_as(P(T.SlmPair)), cap_o, ctypes.byref(nt),
+                                                ctypes.byref(no), ctypes.byref(st)) == 0
+        got = [[(int(i), int(f)) for i, f in obs[int(toff[t]):int(toff[t + 1])]] for t in range(nt.value)]
+        assert got == want[0] and st.as_dict() == want[1]
