@@ -93,22 +93,25 @@ class Server:
             pass
 
 
-def zone_requests(z: synth.Zone):
+def zone_requests(z: synth.Zone, view_offset: int = 0):
     """Views arrive in zone order (trajectory order); view v asks for every
-    candidate pair (u, v) with u < v, oriented as candidate_pairs orients it."""
+    candidate pair (u, v) with u < v, oriented as candidate_pairs orients it.
+    view_offset: the server's id of the zone's first view (a server that has
+    taken other views before)."""
     by_v = {}
     for u, v in z.pairs.tolist():
-        by_v.setdefault(v, []).append((u, SELF))
+        by_v.setdefault(v, []).append((u + view_offset, SELF))
     return [(v, by_v.get(v, [])) for v in range(len(z.counts))]
 
 
-def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0, copy: bool = False):
+def stream_zone(srv: Server, z: synth.Zone, rate: float | None, seed: int = 0, copy: bool = False,
+                view_offset: int = 0):
     """Submit the zone's views with Poisson arrivals at `rate` views/s (None:
     all at once) and collect every result. Returns (results per view, latencies
     ms, wall seconds from first submit to last result). copy=False submits the
     zone's rows where they lie (slm_server_submit_ptr), copy=True copies each
-    view at submission (slm_server_submit)."""
-    reqs = zone_requests(z)
+    view at submission (slm_server_submit). view_offset: as zone_requests."""
+    reqs = zone_requests(z, view_offset)
     rng = np.random.Generator(np.random.PCG64(seed))
     gaps = rng.exponential(1.0 / rate, size=len(reqs)) if rate else np.zeros(len(reqs))
     tickets = [None] * len(reqs)
