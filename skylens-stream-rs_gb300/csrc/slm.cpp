@@ -2114,6 +2114,17 @@ extern "C" slm_status slm_server_create(const slm_server_opts *opts, slm_server 
         g_last_error = keep;
         return s;
     }
+    // the store's operand images for its whole capacity now, not in the first
+    // batch (with no views yet this allocates and packs nothing else)
+    if (s == SLM_OK) s = store_sync_plan_images(srv->store, srv->opts.prec, srv->ctx->stream);
+    if (s == SLM_OK && cudaStreamSynchronize(srv->ctx->stream) != cudaSuccess)
+        s = fail(SLM_CUDA_ERROR, "cudaStreamSynchronize");
+    if (s != SLM_OK) {
+        std::string keep = g_last_error;
+        slm_server_destroy(srv);
+        g_last_error = keep;
+        return s;
+    }
     const uint64_t used = srv->ctx->used.load();
     const uint64_t left = srv->ctx->budget > used ? srv->ctx->budget - used : 0;
     srv->slot_budget = left / srv->opts.slots;
