@@ -5,7 +5,8 @@
 //! smallest of the multiset, `d1 < (r*r)*d2`, and the cross-check against the
 //! column's best (smallest distance, lowest i). Needs a GB300 and libslm
 //! (SLM_LIB_DIR at build time, LD_LIBRARY_PATH at run time).
-use skylens_match::{candidate_pairs, match_pairs, ratio_match, ratio_match_with, Descriptor, Precision};
+use skylens_match::{build_tracks_drop, candidate_pairs, detect_and_describe_rgb8, detector_config_default, match_pairs,
+                    ratio_match, ratio_match_with, Descriptor, Precision};
 
 struct Feat([f32; 128]);
 
@@ -178,5 +179,50 @@ fn match_pairs_equals_one_call_per_pair() {
     assert_eq!(got.len(), pairs.len());
     for (k, &(u, v)) in pairs.iter().enumerate() {
         assert_eq!(got[k], naive(&views[u], &views[v], 0.8, true), "pair ({u}, {v})");
+    }
+}
+
+/// build_tracks with ConflictPolicy::Drop: the reference's known answers
+/// (tracks.rs:1346-1447, the Drop half): the conflicting component dropped
+/// whole, invalid and short matches counted.
+#[test]
+fn tracks_drop_known_answers() {
+    let pairs = vec![
+        (0, 1, vec![(0, 0), (2, 2)]),
+        (1, 2, vec![(0, 0), (2, 2)]),
+        (2, 0, vec![(0, 1)]),
+        (2, 3, vec![(2, 2)]),
+    ];
+    let (t, st) = build_tracks_drop(&[3, 3, 3, 3], &pairs, 3, 100_000);
+    assert_eq!(st.conflicts, 1);
+    assert_eq!(t, vec![vec![(0, 2), (1, 2), (2, 2), (3, 2)]]);
+    let pairs = vec![(0, 0, vec![(0, 1)]), (0, 1, vec![(5, 0), (0, 0)])];
+    let (t, st) = build_tracks_drop(&[2, 2, 2], &pairs, 3, 100_000);
+    assert_eq!((st.invalid_matches, st.too_short), (2, 1));
+    assert!(t.is_empty());
+}
+
+/// detect_and_describe on a gaussian blob (features.rs:846-885): the
+/// strongest keypoint at the blob's centre within 0.1 px, unit descriptors.
+#[test]
+fn detect_and_describe_finds_the_blob() {
+    let (w, h) = (140u32, 120u32);
+    let (cx, cy, s) = (61.3f32, 47.6f32, 4.0f32);
+    let mut rgb = vec![0u8; (w * h * 3) as usize];
+    for y in 0..h {
+        for x in 0..w {
+            let r2 = (x as f32 - cx).powi(2) + (y as f32 - cy).powi(2);
+            let v = ((0.2 + 0.6 * (-r2 / (2.0 * s * s)).exp()) * 255.0).round() as u8;
+            let o = ((y * w + x) * 3) as usize;
+            rgb[o..o + 3].copy_from_slice(&[v, v, v]);
+        }
+    }
+    let out = detect_and_describe_rgb8(&[&rgb], w, h, &detector_config_default());
+    let (kps, descs) = &out[0];
+    assert!(!kps.is_empty());
+    assert!(((kps[0].x - cx).powi(2) + (kps[0].y - cy).powi(2)).sqrt() < 0.1);
+    for d in descs {
+        let n = d.iter().map(|v| v * v).sum::<f32>().sqrt();
+        assert!((n - 1.0).abs() < 1e-4);
     }
 }
